@@ -1,0 +1,159 @@
+"""Synthetic initial conditions for the benchmarked workloads.
+
+Each generator returns ``(params, fields)`` where ``fields`` maps field names to float64 numpy
+arrays in particle order (vector fields shaped ``(N, DIM)``).  The shapes, sizes and value
+distributions are those of the workloads the reference is measured on; the reference's own
+sample generators (src/sample/*.cpp) use different lattices and are noted per function.
+"""
+from __future__ import annotations
+
+import math
+from typing import Dict, Tuple
+
+import numpy as np
+
+from .params import SPHParameters
+
+Fields = Dict[str, np.ndarray]
+
+
+def sod(n_left: int = 800, n_right: int = 100) -> Tuple[SPHParameters, Fields]:
+    """1D Sod shock tube, plain ssph with the cubic spline: x in [-0.5, 0.5], n_left equally
+    spaced particles on [-0.5, 0) with rho = 1, p = 1 and n_right on [0, 0.5] with rho = 0.125,
+    p = 0.1; equal mass; v = 0; gamma = 1.4; neighborNumber 4; avAlpha 1; endTime 0.2;
+    not periodic.  (src/sample/shock_tube.cpp uses 400/100 particles with other states.)"""
+    p = SPHParameters(dim=1, sph_type="ssph", kernel="cubic_spline", gamma=1.4, neighbor_number=4,
+                      av_alpha=1.0, end_time=0.2, periodic=False)
+    dxl = 0.5 / n_left
+    dxr = 0.5 / n_right
+    xl = -0.5 + (np.arange(n_left) + 0.5) * dxl
+    xr = (np.arange(n_right) + 0.5) * dxr
+    x = np.concatenate([xl, xr])
+    rho = np.concatenate([np.full(n_left, 1.0), np.full(n_right, 0.125)])
+    pres = np.concatenate([np.full(n_left, 1.0), np.full(n_right, 0.1)])
+    mass = np.full(x.size, 1.0 * dxl)
+    ene = pres / ((p.gamma - 1.0) * rho)
+    f = dict(pos=x.reshape(-1, 1), vel=np.zeros((x.size, 1)), mass=mass, dens=rho, pres=pres, ene=ene)
+    return p, f
+
+
+def khi(n_in: int = 1024, n_out: int = 724) -> Tuple[SPHParameters, Fields]:
+    """2D Kelvin-Helmholtz instability, disph + Wendland C4 + artificial conductivity, periodic
+    unit box, gamma = 5/3, p = 2.5.  The strip |y - 0.5| < 0.25 is a square lattice of spacing
+    1/n_in with rho = 2, vx = -0.5; outside, a square lattice of spacing 1/n_out with rho = 1,
+    vx = +0.5; all particles have the mass 2/n_in^2.  vy = 0.1 sin(4 pi x) [exp(-(y-0.25)^2/0.005)
+    + exp(-(y-0.75)^2/0.005)] (two Gaussians, as src/sample/khi.cpp:33-36 adds them).
+    neighborNumber 64, endTime 2, leafParticleNumber 16, Balsara switch and time-dependent AV as
+    in sample/khi/khi.json.  Default sizes give 786,376 particles."""
+    p = SPHParameters(dim=2, sph_type="disph", kernel="wendland", gamma=5.0 / 3.0,
+                      neighbor_number=64, end_time=2.0, leaf_num=16, use_balsara=True,
+                      use_tdav=True, use_ac=True, alpha_ac=1.0, periodic=True,
+                      range_min=[0.0, 0.0, 0.0], range_max=[1.0, 1.0, 0.0])
+    yi = (np.arange(n_in) + 0.5) / n_in
+    yi = yi[np.abs(yi - 0.5) < 0.25]
+    xi = (np.arange(n_in) + 0.5) / n_in
+    yo = (np.arange(n_out) + 0.5) / n_out
+    yo = yo[np.abs(yo - 0.5) >= 0.25]
+    xo = (np.arange(n_out) + 0.5) / n_out
+    Xi, Yi = np.meshgrid(xi, yi)
+    Xo, Yo = np.meshgrid(xo, yo)
+    x = np.concatenate([Xo.ravel(), Xi.ravel()])
+    y = np.concatenate([Yo.ravel(), Yi.ravel()])
+    inner = np.concatenate([np.zeros(Xo.size, bool), np.ones(Xi.size, bool)])
+    # order particles row by row (lower outer rows, strip, upper outer rows) like a lattice scan
+    order = np.lexsort((x, y))
+    x, y, inner = x[order], y[order], inner[order]
+    n = x.size
+    rho = np.where(inner, 2.0, 1.0)
+    pres = np.full(n, 2.5)
+    vx = np.where(inner, -0.5, 0.5)
+    vy = 0.1 * np.sin(4.0 * math.pi * x) * (np.exp(-(y - 0.25) ** 2 / 0.005) + np.exp(-(y - 0.75) ** 2 / 0.005))
+    mass = np.full(n, 2.0 / (n_in * n_in))
+    ene = pres / ((p.gamma - 1.0) * rho)
+    f = dict(pos=np.stack([x, y], 1), vel=np.stack([vx, vy], 1), mass=mass, dens=rho, pres=pres, ene=ene)
+    return p, f
+
+
+def evrard(n: int = 1 << 20, seed: int = 20261203) -> Tuple[SPHParameters, Fields]:
+    """3D Evrard collapse with self-gravity, disph + Wendland C4 + Balsara + time-dependent AV,
+    gamma = 5/3, G = 1, theta = 0.5: n equal-mass particles in a sphere of radius 1 and mass 1
+    with rho ~ 1/r (radius r = sqrt(s), s ~ U(0,1) from the seed, isotropic directions), initial
+    density 1/(2 pi r) for the smoothing-length guess (src/sample/evrard.cpp:58), u = 0.05, v = 0,
+    neighborNumber 50, leafParticleNumber 32 (sample/evrard/evrard.json), endTime 3.
+    (src/sample/evrard.cpp stretches a cubic lattice instead of sampling.)"""
+    p = SPHParameters(dim=3, sph_type="disph", kernel="wendland", gamma=5.0 / 3.0,
+                      neighbor_number=50, end_time=3.0, leaf_num=32, use_balsara=True,
+                      use_tdav=True, use_gravity=True, g_constant=1.0, theta=0.5, periodic=False)
+    rng = np.random.default_rng(seed)
+    s = rng.random(n)
+    r = np.sqrt(s)
+    cth = rng.uniform(-1.0, 1.0, n)
+    phi = rng.uniform(0.0, 2.0 * math.pi, n)
+    sth = np.sqrt(1.0 - cth * cth)
+    pos = np.stack([r * sth * np.cos(phi), r * sth * np.sin(phi), r * cth], 1)
+    rr = np.sqrt((pos * pos).sum(1))
+    dens = 1.0 / (2.0 * math.pi * rr)
+    u = 0.05 * p.g_constant
+    f = dict(pos=pos, vel=np.zeros((n, 3)), mass=np.full(n, 1.0 / n), dens=dens,
+             pres=(p.gamma - 1.0) * dens * u, ene=np.full(n, u))
+    return p, f
+
+
+def gresho(n_side: int = 256) -> Tuple[SPHParameters, Fields]:
+    """2D Gresho-Chan vortex, ssph + cubic spline, periodic [-0.5, 0.5]^2, n_side^2 lattice,
+    rho = 1, gamma = 5/3; v_phi = 5r (r < 0.2), 2 - 5r (0.2 <= r < 0.4), 0 beyond;
+    p = 5 + 12.5 r^2, 9 + 12.5 r^2 - 20 r + 4 ln(5r), 3 + 4 ln 2 in the same bands
+    (src/sample/gresho_chan_vortex.cpp:12-32,40-70); neighborNumber 32."""
+    p = SPHParameters(dim=2, sph_type="ssph", kernel="cubic_spline", gamma=5.0 / 3.0,
+                      neighbor_number=32, end_time=1.0, leaf_num=32, use_balsara=True,
+                      periodic=True, range_min=[-0.5, -0.5, 0.0], range_max=[0.5, 0.5, 0.0])
+    dx = 1.0 / n_side
+    c = -0.5 + (np.arange(n_side) + 0.5) * dx
+    X, Y = np.meshgrid(c, c)
+    x, y = X.ravel(), Y.ravel()
+    r = np.sqrt(x * x + y * y)
+    vphi = np.where(r < 0.2, 5.0 * r, np.where(r < 0.4, 2.0 - 5.0 * r, 0.0))
+    with np.errstate(divide="ignore"):
+        pres = np.where(r < 0.2, 5.0 + 12.5 * r * r,
+                        np.where(r < 0.4, 9.0 + 12.5 * r * r - 20.0 * r + 4.0 * np.log(np.maximum(5.0 * r, 1e-300)),
+                                 3.0 + 4.0 * math.log(2.0)))
+    vel = np.stack([-y / r * vphi, x / r * vphi], 1)
+    n = x.size
+    rho = np.ones(n)
+    ene = pres / ((p.gamma - 1.0) * rho)
+    f = dict(pos=np.stack([x, y], 1), vel=vel, mass=np.full(n, 1.0 / n), dens=rho, pres=pres, ene=ene)
+    return p, f
+
+
+def shock_tube_gsph(n_left: int, n_right: int, rho_l: float, rho_r: float, p_l: float, p_r: float,
+                    neighbor_number: int = 4) -> Tuple[SPHParameters, Fields]:
+    """One 1D tube of the gsph ensemble: x in [-0.5, 0.5], interface at 0, equal mass within the
+    tube, particles split n_left / n_right, states (rho, p) left and right, gamma = 1.4, 2nd-order
+    gsph with the cubic spline, not periodic."""
+    p = SPHParameters(dim=1, sph_type="gsph", kernel="cubic_spline", gamma=1.4,
+                      neighbor_number=neighbor_number, gsph_2nd_order=True, periodic=False)
+    xl = -0.5 + (np.arange(n_left) + 0.5) * (0.5 / n_left)
+    xr = (np.arange(n_right) + 0.5) * (0.5 / n_right)
+    x = np.concatenate([xl, xr])
+    rho = np.concatenate([np.full(n_left, rho_l), np.full(n_right, rho_r)])
+    pres = np.concatenate([np.full(n_left, p_l), np.full(n_right, p_r)])
+    mass = np.full(x.size, rho_l * 0.5 / n_left)
+    f = dict(pos=x.reshape(-1, 1), vel=np.zeros((x.size, 1)), mass=mass, dens=rho, pres=pres,
+             ene=pres / ((p.gamma - 1.0) * rho))
+    return p, f
+
+
+def ensemble_tubes(n_runs: int = 4096, n_min: int = 200, n_max: int = 5000, seed: int = 20261203):
+    """The gsph ensemble: n_runs independent tubes with particle counts ~ U{n_min..n_max},
+    rho_L, rho_R, p_L, p_R log-uniform in [0.1, 1] from the seed, particle split
+    n_L / n_R = rho_L / rho_R (equal mass within a tube).  Returns a list of per-tube dicts."""
+    rng = np.random.default_rng(seed)
+    counts = rng.integers(n_min, n_max + 1, n_runs)
+    states = np.exp(rng.uniform(math.log(0.1), math.log(1.0), (n_runs, 4)))
+    tubes = []
+    for k in range(n_runs):
+        rl, rr, pl, pr = states[k]
+        nl = int(round(counts[k] * rl / (rl + rr)))
+        nl = min(max(nl, 1), counts[k] - 1)
+        tubes.append(dict(n_left=nl, n_right=int(counts[k] - nl), rho_l=rl, rho_r=rr, p_l=pl, p_r=pr))
+    return tubes
