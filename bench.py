@@ -1,0 +1,375 @@
+"""Benchmark of the SPH particle hot path on one GB300: particle-steps/s.
+
+Default workload: the 2D Kelvin-Helmholtz step, disph + Wendland C4 + artificial conductivity,
+786,376 particles (square lattices of spacing 1/1024 in the dense strip and 1/724 outside),
+periodic unit box, neighborNumber 64.  One step = TimeStep, predict, octree build, PreInteraction,
+FluidForce, (GravityForce), correct, all on the device (Solver::integrate).  Inputs are synthetic
+(the seeded/lattice initial conditions of sphcode_gb300/ics.py).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload khi|evrard|gresho|sod]
+  python bench.py --impl reference ...   # the reference's own CPU modules on the host cores
+
+Timing: W warm-up steps, then K steps, each bracketed by CUDA events on the library's stream
+with a 2 x L2 buffer overwritten between steps outside the brackets; max over ranks.  Under
+torchrun every rank runs an independent replica of the workload (the path does not shard).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s on 1 GB300, FP32-pair vs FP64 form at stated rel err"
+
+# Static flop counts of the reference's pair bodies (FMA = 2, add/mul/div/sqrt = 1 each), per
+# interacting pair, used for the compute roofline of the force kernel.
+FLUID_FLOPS_PER_PAIR = {("disph", 2): 120, ("disph", 3): 135, ("ssph", 2): 110, ("ssph", 3): 125,
+                        ("ssph", 1): 90, ("gsph", 1): 180, ("disph", 1): 100}
+# Compulsory HBM bytes of the force stage per particle: FP64 reads of pos(D), vel(D), mass,
+# dens, pres, ene, sml, sound, alpha, balsara, gradh + FP32 mirror write/read (48 B) + writes of
+# acc(D), dene.
+def fluid_bytes_per_particle(D):
+    return 8 * (2 * D + 9) + 48 * 2 + 8 * (D + 1)
+
+
+def workload(name):
+    from sphcode_gb300 import ics
+    if name == "khi":
+        p, f = ics.khi()
+        desc = "khi_2d_disph_wendland_ac"
+    elif name == "evrard":
+        p, f = ics.evrard()
+        desc = "evrard_3d_disph_wendland_balsara_tdav_gravity"
+    elif name == "gresho":
+        p, f = ics.gresho(256)
+        desc = "gresho_chan_2d_ssph_cubic"
+    elif name == "sod":
+        p, f = ics.sod()
+        desc = "sod_1d_ssph_cubic"
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    return p, f, desc
+
+
+# ---- clocks --------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---- reference-layout host particles (SPHParticle, include/particle.hpp:8-33) --------------
+def aos_dtype(D):
+    fields = [("pos", "f8", (D,)), ("vel", "f8", (D,)), ("vel_p", "f8", (D,)), ("acc", "f8", (D,))]
+    fields += [(n, "f8") for n in ("mass", "dens", "pres", "ene", "ene_p", "dene", "sml", "sound",
+                                   "balsara", "alpha", "gradh", "phi")]
+    fields += [("id", "i4"), ("neighbor", "i4"), ("next", "u8")]
+    return np.dtype(fields, align=True)
+
+
+def aos_layout(dt):
+    from sphcode_gb300 import sphgpu
+    lay = sphgpu.AosLayout()
+    lay.stride = dt.itemsize
+    for name in ("pos", "vel", "vel_p", "acc", "mass", "dens", "pres", "ene", "ene_p", "dene", "sml",
+                 "sound", "balsara", "alpha", "gradh", "phi", "neighbor"):
+        setattr(lay, name, dt.fields[name][1])
+    return lay
+
+
+def pinned_array(nbytes):
+    import torch
+    t = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    return t, t.numpy()
+
+
+# ---- CPU baseline / reference arm ------------------------------------------------------------
+def cpu_reference_run(name, steps, threads):
+    """Time the reference's own modules (oracle/_ref, built from the reference sources with the
+    reference Makefile's flags) or, where they are not built, the C restatement in oracle/, on
+    the host cores.  Returns (particle-steps/s, kind, sample text, seconds)."""
+    from oracle import pyoracle
+    p, f, desc = workload(name)
+    kind = "reference" if pyoracle.reference_available("fast") else "port"
+    sim = pyoracle.OracleSim(p, f, kind="ref" if kind == "reference" else "port", flavor="fast",
+                             threads=threads)
+    t0 = time.perf_counter()
+    sim.initialize()
+    t_init = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        sim.step()
+    dt = time.perf_counter() - t0
+    n = sim.n
+    sim.close()
+    sample = (f"{desc}: {n} particles, Solver::initialize ({t_init:.1f} s, untimed) then {steps} "
+              f"timed Solver::integrate steps on {threads} OpenMP threads")
+    return n * steps / dt, kind, sample, dt
+
+
+def run_reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    steps = max(1, min(args.steps, args.ref_steps))
+    value, kind, sample, secs = cpu_reference_run(args.workload, steps, threads)
+    _, _, desc = workload(args.workload)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "particle-steps/s",
+            "n_gpus": args.gpus, "steps": steps, "warmup": 0, "ms_per_step": secs / steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": desc},
+            "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads,
+                             "kind": kind, "sample": sample},
+            "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---- GPU arm -----------------------------------------------------------------------------------
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="khi")
+    ap.add_argument("--ref-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference_arm(args)
+        return
+    if args.warmup < 3:
+        raise SystemExit("at least 3 warm-up steps")
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    import __graft_entry__ as g
+    if rank == 0 or world == 1:
+        g.build()
+    if dist:
+        dist.barrier()
+    from sphcode_gb300 import sphgpu
+
+    p, f, desc = workload(args.workload)
+    n = int(f["mass"].shape[0])
+    D = p.dim
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- FP32-pair form: device-resident throughput --------------------------------------
+    sim = sphgpu.GpuSimulation(p, f, precision="fp32")
+    sim.initialize()
+    sim.step(args.warmup)
+    launches_per_step = sim.get_tuning("graph_kernels")
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    ms = sim.bench_steps(args.steps, flush_l2=True)
+    barrier()
+    clk = clocks.stop()
+    ms = max_over_ranks(ms)
+    value = world * n * args.steps / (ms * 1e-3)
+
+    # per-stage device times (eager launches, CUDA events between stages)
+    sim.set_tuning("timing", 1)
+    sim.step(1)
+    stages = {k: 0.0 for k in ("tree", "pre", "fluid", "gravity", "integrate")}
+    reps = 3
+    for _ in range(reps):
+        sim.step(1)
+        for k, v in sim.stage_times().items():
+            stages[k] += v / reps
+    sim.set_tuning("timing", 0)
+    pairs = sim.neighbor_counts(True).astype(np.int64) - 1   # r = 0 (self) is skipped
+    mean_pairs = float(pairs.mean())
+    newton_fail = sim.newton_failures()
+    sim.close()
+
+    # ---- FP64 plain form and the FP32-vs-FP64 error after initialize + 1 step -----------------
+    fp64 = None
+    errs = {}
+    if not args.no_fp64:
+        s64 = sphgpu.GpuSimulation(p, f, precision="fp64")
+        s32 = sphgpu.GpuSimulation(p, f, precision="fp32")
+        s64.initialize()
+        s32.initialize()
+        s64.step(1)
+        s32.step(1)
+        for name in ("dens", "sml", "pres", "acc", "dene", "pos", "vel", "ene"):
+            a, b = s32.get(name), s64.get(name)
+            errs[name] = float(np.max(np.abs(a - b)) / max(float(np.max(np.abs(b))), 1e-300))
+        s32.close()
+        s64.step(args.warmup - 1)
+        k64 = max(3, args.steps // 4)
+        barrier()
+        ms64 = max_over_ranks(s64.bench_steps(k64, flush_l2=True))
+        fp64 = {"value": world * n * k64 / (ms64 * 1e-3), "steps": k64, "ms_per_step": ms64 / k64}
+        s64.close()
+
+    # ---- end to end through the reference-facing AoS boundary, host buffers ------------------
+    dt = aos_dtype(D)
+    holder, raw = pinned_array(n * dt.itemsize)
+    aos = raw.view(dt)
+    aos[:] = 0
+    aos["pos"] = f["pos"].reshape(n, D)
+    aos["vel"] = f["vel"].reshape(n, D)
+    aos["mass"] = f["mass"]
+    aos["dens"] = f["dens"]
+    aos["pres"] = f["pres"]
+    aos["ene"] = f["ene"]
+    aos["id"] = np.arange(n)
+    lay = aos_layout(dt)
+    import ctypes
+    e2e_sim = sphgpu.GpuSimulation(p, f, precision="fp32")
+    e2e_sim.initialize()
+    e2e_sim.lib.sphgpu_download_aos(e2e_sim._h, ctypes.c_void_p(raw.ctypes.data), ctypes.byref(lay))
+    e2e_sim.step(args.warmup)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        rc = e2e_sim.lib.sphgpu_upload_aos(e2e_sim._h, ctypes.c_void_p(raw.ctypes.data), ctypes.byref(lay))
+        rc |= e2e_sim.lib.sphgpu_step(e2e_sim._h, 1)
+        rc |= e2e_sim.lib.sphgpu_download_aos(e2e_sim._h, ctypes.c_void_p(raw.ctypes.data), ctypes.byref(lay))
+        if rc:
+            raise RuntimeError(e2e_sim.lib.sphgpu_last_error(e2e_sim._h))
+    barrier()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e_sim.close()
+    e2e = {"value": world * n * args.steps / e2e_s, "unit": "particle-steps/s",
+           "h2d_bytes_per_step": 2 * n * dt.itemsize, "d2h_bytes_per_step": n * dt.itemsize,
+           "path": "sphgpu_upload_aos + sphgpu_step(1) + sphgpu_download_aos on a pinned "
+                   "std::vector<SPHParticle>-layout buffer"}
+
+    # ---- roofline of the dominant kernel ----------------------------------------------------
+    fp32_peak, fp64_peak = sphgpu.measure_peaks()
+    dom = max(("pre", "fluid", "gravity", "tree"), key=lambda k: stages[k])
+    flops_pair = FLUID_FLOPS_PER_PAIR.get((p.sph_type, D), 120)
+    fluid_flops = mean_pairs * n * flops_pair
+    fluid_ms = stages["fluid"]
+    import json as _json
+    peaks = {}
+    try:
+        peaks = _json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    fluid_bytes = fluid_bytes_per_particle(D) * n
+    roofline = {"kernel": "fluid_kernel (FluidForce, FP32 pairs)", "bound": "fp32",
+                "achieved": fluid_flops / (fluid_ms * 1e-3) / 1e12, "peak": fp32_peak,
+                "unit": "TFLOP/s", "frac": None, "traffic": None,
+                "algorithmic_flops_per_launch": fluid_flops, "pairs_per_particle": mean_pairs,
+                "flops_per_pair": flops_pair, "launch_ms": fluid_ms,
+                "peak_source": "sphgpu_measure_peaks FP32 FMA loop on this GPU",
+                "hbm": {"achieved": fluid_bytes / (fluid_ms * 1e-3) / 1e9, "peak": hbm_peak,
+                        "unit": "GB/s", "frac": fluid_bytes / (fluid_ms * 1e-3) / 1e9 / hbm_peak,
+                        "algorithmic_bytes_per_launch": fluid_bytes,
+                        "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}}
+    roofline["frac"] = roofline["achieved"] / fp32_peak if fp32_peak > 0 else None
+
+    # ---- CPU baseline (rank 0, N = 1) -------------------------------------------------------------
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, kind, sample, _ = cpu_reference_run(args.workload, args.ref_steps, threads)
+        cpu = {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": kind, "sample": sample}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic",
+                "config": {"workload": desc, "n_particles": n, "dim": D, "sph_type": p.sph_type,
+                           "kernel": p.kernel, "neighbor_number": p.neighbor_number,
+                           "form": "fp32_pair (FP32 pair sums, Kahan totals, FP64 state)",
+                           "l2": "2 x L2 buffer overwritten between timed steps",
+                           "parallelism": f"replicas{world}"},
+                "fp64_form": fp64,
+                "fp32_over_fp64": (value / fp64["value"]) if fp64 else None,
+                "fp32_rel_err_vs_fp64_after_1_step": errs,
+                "stage_ms": stages, "newton_failures": newton_fail,
+                "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+                "gpu_launches": launches_per_step * args.steps,
+                "peaks": {"fp32_tflops": fp32_peak, "fp64_tflops": fp64_peak}}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,218 @@
+/*
+ * sphgpu — C ABI of the GB300 (sm_103a) implementation of SPHCODE's per-step particle hot path.
+ *
+ * The reference has no FFI: its hot path is the sph::Module interface
+ * (include/module.hpp:10-14: initialize(shared_ptr<SPHParameters>),
+ * calculation(shared_ptr<Simulation>)) called by sph::Solver (src/solver.cpp:387-429).
+ * Each entry point below is the device-side body of one of those calls, so a GPU Module
+ * subclass is a drop-in that forwards its calculation() here (see INTEGRATION.md for the
+ * Module subclasses and the ctypes binding).  Plain pointers and sizes only; no C++ or CUDA
+ * types cross this boundary.  Every function returns an sphgpu_status code; no exception
+ * crosses the ABI.
+ *
+ * Particle data at the boundary is in the caller's particle order (SPHParticle::id == index,
+ * include/particle.hpp:30), FP64, vector fields interleaved per particle (x0 y0 z0 x1 ...).
+ * Inside the library the particles live on the device as structure-of-arrays, reordered by
+ * octree key; results are scattered back to the caller's order on download.
+ */
+#ifndef SPHGPU_H
+#define SPHGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Mirrors sph::SPHParameters (include/parameters.hpp:20-79); JSON keys and defaults of
+ * Solver::read_parameterfile (src/solver.cpp:193-298).  Same layout as the oracle's struct. */
+typedef struct sphgpu_params {
+    int    sph_type;          /* 0 ssph, 1 disph, 2 gsph                                       */
+    int    kernel;            /* 0 cubic spline, 1 Wendland C4                                 */
+    double cfl_sound;         /* cflSound                                                      */
+    double cfl_force;         /* cflForce                                                      */
+    double av_alpha;          /* avAlpha                                                       */
+    int    use_balsara;       /* useBalsaraSwitch                                              */
+    int    use_tdav;          /* useTimeDependentAV                                            */
+    double alpha_max;         /* alphaMax                                                      */
+    double alpha_min;         /* alphaMin                                                      */
+    double epsilon_av;        /* epsilonAV                                                     */
+    int    use_ac;            /* useArtificialConductivity                                     */
+    double alpha_ac;          /* alphaAC                                                       */
+    int    max_level;         /* maxTreeLevel                                                  */
+    int    leaf_num;          /* leafParticleNumber                                            */
+    int    neighbor_number;   /* neighborNumber                                                */
+    double gamma;             /* gamma                                                         */
+    int    iterative_sml;     /* iterativeSmoothingLength                                      */
+    int    periodic;          /* periodic                                                      */
+    double range_min[3];      /* rangeMin                                                      */
+    double range_max[3];      /* rangeMax                                                      */
+    int    use_gravity;       /* useGravity                                                    */
+    double g_constant;        /* G                                                             */
+    double theta;             /* theta                                                         */
+    int    gsph_2nd_order;    /* use2ndOrderGSPH                                               */
+} sphgpu_params;
+
+typedef struct sphgpu_ctx sphgpu_ctx;
+
+/* Arithmetic of the pair sums.  FP32_PAIR: pair terms in FP32 on offsets relative to the
+ * target group's origin, per-particle totals Kahan-compensated; FP64 kept for absolute
+ * positions/velocities/energies, the leapfrog, the smoothing-length Newton test, neighbour
+ * membership decisions and global sums.  FP64: every pair term in FP64. */
+enum sphgpu_precision { SPHGPU_FP32_PAIR = 0, SPHGPU_FP64 = 1 };
+
+enum sphgpu_status {
+    SPHGPU_OK = 0,
+    SPHGPU_ERR_ARG = 1,          /* invalid argument / unsupported configuration               */
+    SPHGPU_ERR_CUDA = 2,         /* CUDA runtime error (text in sphgpu_last_error)             */
+    SPHGPU_ERR_NODE_POOL = 3,    /* octree needs more than 5 N nodes ("There is no free node",
+                                    src/bhtree.cpp:179-181)                                    */
+    SPHGPU_ERR_CAPACITY = 4,     /* a per-group walk stack, leaf list or source tile overflowed
+                                    its capacity (the reference's neighbour list overflow is
+                                    unchecked, src/pre_interaction.cpp:58)                     */
+    SPHGPU_ERR_NOT_FINITE = 5,   /* NaN/Inf detected in a state field                          */
+    SPHGPU_ERR_STATE = 6,        /* call order violated (e.g. forces before the tree)          */
+    SPHGPU_ERR_NO_DEVICE = 7     /* no CUDA device / library built without a usable device     */
+};
+
+/* Field identifiers for sphgpu_set_field / sphgpu_get_field (SPHParticle members and the gsph
+ * gradient arrays of src/solver.cpp:373-385).  Vector fields carry DIM doubles per particle;
+ * GRAD_V carries DIM*DIM doubles per particle laid out [k][d] = d v_k / d x_d. */
+enum sphgpu_field {
+    SPHGPU_POS = 0, SPHGPU_VEL, SPHGPU_VEL_P, SPHGPU_ACC, SPHGPU_MASS, SPHGPU_DENS, SPHGPU_PRES,
+    SPHGPU_ENE, SPHGPU_ENE_P, SPHGPU_DENE, SPHGPU_SML, SPHGPU_SOUND, SPHGPU_BALSARA,
+    SPHGPU_ALPHA, SPHGPU_GRADH, SPHGPU_PHI, SPHGPU_NEIGHBOR, SPHGPU_GRAD_D, SPHGPU_GRAD_P,
+    SPHGPU_GRAD_V, SPHGPU_NFIELDS
+};
+
+/* Simulation scalars (include/simulation.hpp:24-30). */
+enum sphgpu_scalar { SPHGPU_TIME = 0, SPHGPU_DT = 1, SPHGPU_H_PER_V_SIG = 2 };
+
+/* Byte offsets of SPHParticle members in a caller's array-of-structures (offsetof on the
+ * caller's side), for the zero-repack upload/download used by the Module drop-in. */
+typedef struct sphgpu_aos_layout {
+    size_t stride;                           /* sizeof(SPHParticle)                            */
+    long   pos, vel, vel_p, acc, mass, dens, pres, ene, ene_p, dene, sml, sound, balsara,
+           alpha, gradh, phi;                /* offsets of FP64 members, -1 = absent          */
+    long   neighbor;                         /* offset of the int member, -1 = absent         */
+} sphgpu_aos_layout;
+
+/* ---- lifetime ------------------------------------------------------------------------- */
+
+/* One simulation of n particles in `dim` dimensions on the current CUDA device.
+ * Replaces Simulation(param) + BHTree::initialize/resize (src/simulation.cpp:12-30,
+ * src/bhtree.cpp:12-53) and each Module::initialize (e.g. src/pre_interaction.cpp:19-37). */
+int sphgpu_create(const sphgpu_params* params, int dim, int n, int precision, sphgpu_ctx** out);
+
+/* n_runs independent simulations of run_sizes[r] particles sharing one parameter set, advanced
+ * together (each run keeps its own tree root, dt and time).  Particles of run r occupy the
+ * index range [sum(run_sizes[0..r-1]), sum(run_sizes[0..r])) at the boundary.  No reference
+ * counterpart (the reference runs one simulation per process). */
+int sphgpu_create_batch(const sphgpu_params* params, int dim, int n_runs, const int* run_sizes,
+                        int precision, sphgpu_ctx** out);
+
+int sphgpu_destroy(sphgpu_ctx* ctx);
+
+/* ---- data movement ---------------------------------------------------------------------- */
+
+/* Host <-> device copies of one field in the caller's particle order (FP64; NEIGHBOR as
+ * double).  Replace the reads/writes the modules do on Simulation::get_particles(). */
+int sphgpu_set_field(sphgpu_ctx* ctx, int field, const double* host);
+int sphgpu_get_field(sphgpu_ctx* ctx, int field, double* host);
+
+/* Upload / download of a caller's std::vector<SPHParticle> storage in one contiguous copy;
+ * only the members named in the layout are read or written back. */
+int sphgpu_upload_aos(sphgpu_ctx* ctx, const void* base, const sphgpu_aos_layout* layout);
+int sphgpu_download_aos(sphgpu_ctx* ctx, void* base, const sphgpu_aos_layout* layout);
+
+/* Simulation::{set,get}_{time,dt,h_per_v_sig}; `run` selects the run of a batch (0 otherwise). */
+int sphgpu_set_scalar(sphgpu_ctx* ctx, int which, int run, double value);
+int sphgpu_get_scalar(sphgpu_ctx* ctx, int which, int run, double* value);
+
+/* ---- the hot path ---------------------------------------------------------------------- */
+
+/* Simulation::make_tree -> BHTree::make (src/simulation.cpp:37-40, src/bhtree.cpp:55-107). */
+int sphgpu_make_tree(sphgpu_ctx* ctx);
+
+/* PreInteraction::calculation for the context's SPH type (src/pre_interaction.cpp:39-169,
+ * src/disph/d_pre_interaction.cpp:21-162, src/gsph/g_pre_interaction.cpp:27-144), including
+ * the first-call initial_smoothing (:171-215) and the closing BHTree::set_kernel. */
+int sphgpu_pre_interaction(sphgpu_ctx* ctx);
+
+/* FluidForce::calculation (src/fluid_force.cpp:26-86, src/disph/d_fluid_force.cpp:26-86,
+ * src/gsph/g_fluid_force.cpp:39-166). */
+int sphgpu_fluid_force(sphgpu_ctx* ctx);
+
+/* GravityForce::calculation with the tree (src/gravity_force.cpp:52-89,
+ * src/bhtree.cpp:128-132,273-331); adds to the fluid acceleration. */
+int sphgpu_gravity_force(sphgpu_ctx* ctx);
+
+/* TimeStep::calculation (src/timestep.cpp:18-38). */
+int sphgpu_timestep(sphgpu_ctx* ctx);
+
+/* Solver::predict / Solver::correct (src/solver.cpp:431-474). */
+int sphgpu_predict(sphgpu_ctx* ctx);
+int sphgpu_correct(sphgpu_ctx* ctx);
+
+/* Solver::initialize from the field start-up to the first force evaluation
+ * (src/solver.cpp:392-414). */
+int sphgpu_initialize(sphgpu_ctx* ctx);
+
+/* n_steps of Solver::integrate + Simulation::update_time (src/solver.cpp:319-325,417-429),
+ * replayed as one CUDA graph per step; the state stays on the device. */
+int sphgpu_step(sphgpu_ctx* ctx, int n_steps);
+
+/* Block until the context's stream is idle; returns any deferred device-side status. */
+int sphgpu_synchronize(sphgpu_ctx* ctx);
+
+/* ---- diagnostics and parity --------------------------------------------------------------- */
+
+/* Neighbour sets for the current smoothing lengths in the caller's order: is_ij = 0 gives
+ * {j : r_ij^2 < h_i^2}, is_ij = 1 gives {j : r_ij^2 < max(h_i^2, h_j^2)} — the sets of
+ * exhaustive_search (src/exhaustive_search.cpp:11-42) and of the BHTree walk
+ * (src/bhtree.cpp:234-270).  list holds cap ids per particle (unordered); list = NULL with
+ * cap = 0 returns the counts only. */
+int sphgpu_neighbors(sphgpu_ctx* ctx, int is_ij, int* counts, int* list, int cap);
+
+/* Output::output_energy sums (src/output.cpp:66-90) plus momentum, summed in FP64:
+ * out = {kinetic, thermal, potential, total, p_0 .. p_{DIM-1}} for run `run`. */
+int sphgpu_energy(sphgpu_ctx* ctx, int run, double* out);
+
+/* Tree shape: out[0] nodes (roots excluded), out[1] leaves, out[2+L] nodes at level L,
+ * out[66+L] leaves at level L (130 ints). */
+int sphgpu_tree_stats(sphgpu_ctx* ctx, int* out);
+
+/* Particles whose smoothing-length Newton iteration did not converge in the last
+ * PreInteraction (the reference logs them, src/pre_interaction.cpp:277-280). */
+int sphgpu_newton_failures(sphgpu_ctx* ctx, int* count);
+
+/* Text of the last error on this context (or of the last failed create if ctx is NULL). */
+const char* sphgpu_last_error(const sphgpu_ctx* ctx);
+
+/* Kernel schedule knobs (chosen by the autotuner; exposed for tests and the tuner):
+ * which = 0 target-group size in warps, 1 FluidForce warps, 2 GravityForce warps,
+ * 3 source-tile capacity (0 = automatic), 4 autotune on/off, 5 per-stage event timing on/off
+ * (steps then run eagerly), 6 CUDA-graph replay of steps on/off; 7 (read only) kernel launches
+ * in one captured step. */
+int sphgpu_set_tuning(sphgpu_ctx* ctx, int which, int value);
+int sphgpu_get_tuning(sphgpu_ctx* ctx, int which, int* value);
+
+/* Per-stage device time of the last sphgpu_step / stage call in milliseconds, measured with
+ * CUDA events on the context's stream: out = {tree, pre, fluid, gravity, integrate}. */
+int sphgpu_stage_times(sphgpu_ctx* ctx, double* out);
+
+/* Benchmark helper (no reference counterpart): runs n_steps steps like sphgpu_step, each
+ * bracketed by CUDA events on the context's stream; with flush_l2 != 0 a buffer of twice the
+ * L2 size is overwritten before every step, outside the timed brackets.  *ms = sum of the
+ * per-step device times. */
+int sphgpu_bench_steps(sphgpu_ctx* ctx, int n_steps, int flush_l2, double* ms);
+
+/* Calibration (no reference counterpart): sustained FP32 and FP64 FMA throughput of the current
+ * device in TFLOP/s, the denominators of the pair kernels' compute rooflines. */
+int sphgpu_measure_peaks(double* fp32_tflops, double* fp64_tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPHGPU_H */

@@ -1,0 +1,981 @@
+// The extern "C" entry points of include/sphgpu.h: context lifetime, field movement between the
+// caller's particle order and the device's key-ordered structure of arrays, the hot-path stages
+// and the step loop captured as a CUDA graph.
+//
+// Each stage call corresponds to one sph::Module::calculation() (include/module.hpp:10-14) or
+// one Solver step (src/solver.cpp:392-474); it runs on the context's stream and synchronises
+// before returning, so a status code is available at once.  sphgpu_step runs whole steps on the
+// device and synchronises once at the end.
+#include <algorithm>
+#include <cstdio>
+#include <map>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "context.cuh"
+
+struct sphgpu_ctx {
+    sphgpu::Ctx c;
+};
+
+namespace sphgpu {
+
+namespace {
+
+std::mutex g_err_mutex;
+std::string g_create_error;
+
+constexpr int THREADS = 256;
+
+// caller order <-> key order, for one field of width w (w doubles per particle in the caller's
+// layout, component k of the caller's record in slot array dst[k])
+struct FieldMap {
+    double* f[9];
+    int w;
+};
+
+__global__ void scatter_field_kernel(FieldMap fm, const int* id, int n, const double* stage)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int src = id[i];
+    for (int k = 0; k < fm.w; ++k) fm.f[k][i] = stage[(size_t)src * fm.w + k];
+}
+
+__global__ void gather_field_kernel(FieldMap fm, const int* id, int n, double* stage)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int dst = id[i];
+    for (int k = 0; k < fm.w; ++k) stage[(size_t)dst * fm.w + k] = fm.f[k][i];
+}
+
+__global__ void scatter_int_as_double_kernel(int* dst, const int* id, int n, const double* stage)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = (int)stage[id[i]];
+}
+
+__global__ void gather_int_as_double_kernel(const int* src, const int* id, int n, double* stage)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) stage[id[i]] = (double)src[i];
+}
+
+__global__ void init_ids_kernel(int* id, int* run, const int* run_begin, int R, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    id[i] = i;
+    int lo = 0, hi = R;   // last r with run_begin[r] <= i
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (run_begin[mid] <= i) lo = mid; else hi = mid;
+    }
+    run[i] = lo;
+}
+
+__global__ void fill_ord_kernel(long long* p, int n, double v)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = dbl_to_ord(v);
+}
+
+struct AosMap {
+    long off[16];     // byte offsets of FP64 members (-1 absent), field ids F_* in order below
+    int slot[16];
+    int width[16];
+    long off_nb;
+    size_t stride;
+    int nf;
+};
+
+__global__ void aos_upload_kernel(State st, AosMap m, const unsigned char* aos, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned char* rec = aos + (size_t)st.id[i] * m.stride;
+    for (int q = 0; q < m.nf; ++q) {
+        const double* src = reinterpret_cast<const double*>(rec + m.off[q]);
+        for (int k = 0; k < m.width[q]; ++k) st.f[m.slot[q] + k][i] = src[k];
+    }
+    if (m.off_nb >= 0) st.neighbor[i] = *reinterpret_cast<const int*>(rec + m.off_nb);
+}
+
+__global__ void aos_download_kernel(State st, AosMap m, unsigned char* aos, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    unsigned char* rec = aos + (size_t)st.id[i] * m.stride;
+    for (int q = 0; q < m.nf; ++q) {
+        double* dst = reinterpret_cast<double*>(rec + m.off[q]);
+        for (int k = 0; k < m.width[q]; ++k) dst[k] = st.f[m.slot[q] + k][i];
+    }
+    if (m.off_nb >= 0) *reinterpret_cast<int*>(rec + m.off_nb) = st.neighbor[i];
+}
+
+__global__ void nonfinite_kernel(State st, int n, int dim, unsigned* err)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    bool bad = false;
+    for (int k = 0; k < dim; ++k) {
+        bad |= !isfinite(st.f[F_POS + k][i]);
+        bad |= !isfinite(st.f[F_VEL + k][i]);
+        bad |= !isfinite(st.f[F_ACC + k][i]);
+    }
+    bad |= !isfinite(st.f[F_DENS][i]) || !isfinite(st.f[F_ENE][i]) || !isfinite(st.f[F_SML][i]);
+    if (bad) atomicOr(err, (unsigned)ERR_NOT_FINITE);
+}
+
+// Slot of an API field id and its width in doubles.
+bool field_slot(const Ctx& c, int field, int* slot, int* width)
+{
+    const int D = c.dim;
+    switch (field) {
+    case SPHGPU_POS: *slot = F_POS; *width = D; return true;
+    case SPHGPU_VEL: *slot = F_VEL; *width = D; return true;
+    case SPHGPU_VEL_P: *slot = F_VELP; *width = D; return true;
+    case SPHGPU_ACC: *slot = F_ACC; *width = D; return true;
+    case SPHGPU_MASS: *slot = F_MASS; *width = 1; return true;
+    case SPHGPU_DENS: *slot = F_DENS; *width = 1; return true;
+    case SPHGPU_PRES: *slot = F_PRES; *width = 1; return true;
+    case SPHGPU_ENE: *slot = F_ENE; *width = 1; return true;
+    case SPHGPU_ENE_P: *slot = F_ENEP; *width = 1; return true;
+    case SPHGPU_DENE: *slot = F_DENE; *width = 1; return true;
+    case SPHGPU_SML: *slot = F_SML; *width = 1; return true;
+    case SPHGPU_SOUND: *slot = F_SOUND; *width = 1; return true;
+    case SPHGPU_BALSARA: *slot = F_BALSARA; *width = 1; return true;
+    case SPHGPU_ALPHA: *slot = F_ALPHA; *width = 1; return true;
+    case SPHGPU_GRADH: *slot = F_GRADH; *width = 1; return true;
+    case SPHGPU_PHI: *slot = F_PHI; *width = 1; return true;
+    case SPHGPU_GRAD_D: *slot = F_GRADD; *width = D; return c.p.sph_type == 2;
+    case SPHGPU_GRAD_P: *slot = F_GRADP; *width = D; return c.p.sph_type == 2;
+    case SPHGPU_GRAD_V: *slot = F_GRADV; *width = D * D; return c.p.sph_type == 2;
+    default: return false;
+    }
+}
+
+FieldMap field_map(const State& st, int slot, int width, int dim)
+{
+    FieldMap fm{};
+    fm.w = width;
+    if (slot == F_GRADV) {
+        for (int k = 0; k < dim; ++k)
+            for (int d = 0; d < dim; ++d) fm.f[k * dim + d] = st.f[F_GRADV + 3 * k + d];
+    } else {
+        for (int k = 0; k < width; ++k) fm.f[k] = st.f[slot + k];
+    }
+    return fm;
+}
+
+unsigned err_bits_to_status(unsigned bits)
+{
+    if (bits & ERR_NODE_POOL) return SPHGPU_ERR_NODE_POOL;
+    if (bits & (ERR_STACK | ERR_LEAVES | ERR_TILE | ERR_LIST | ERR_GSTACK)) return SPHGPU_ERR_CAPACITY;
+    if (bits & ERR_NOT_FINITE) return SPHGPU_ERR_NOT_FINITE;
+    return SPHGPU_OK;
+}
+
+std::string err_bits_text(unsigned bits)
+{
+    std::string s;
+    if (bits & ERR_NODE_POOL) s += "octree needs more than 5 N nodes (There is no free node); ";
+    if (bits & ERR_STACK) s += "walk stack overflow; ";
+    if (bits & ERR_LEAVES) s += "leaf list overflow; ";
+    if (bits & ERR_TILE) s += "source tile overflow in the large-capacity pass; ";
+    if (bits & ERR_LIST) s += "neighbour list longer than the caller's capacity; ";
+    if (bits & ERR_GSTACK) s += "gravity walk stack overflow; ";
+    if (bits & ERR_NOT_FINITE) s += "non-finite value in the particle state; ";
+    return s;
+}
+
+int cuda_status(Ctx& c, cudaError_t e, const char* what)
+{
+    if (e == cudaSuccess) return SPHGPU_OK;
+    c.last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return SPHGPU_ERR_CUDA;
+}
+
+// Synchronise the stream and fold launch errors and the device status word into a status.
+int finish(Ctx& c, const char* what)
+{
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+    if (e != cudaSuccess) return cuda_status(c, e, what);
+    unsigned bits = 0;
+    e = cudaMemcpy(&bits, c.d_err, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_status(c, e, what);
+    if (bits) {
+        cudaMemset(c.d_err, 0, sizeof(unsigned));
+        c.last_error = std::string(what) + ": " + err_bits_text(bits);
+        return (int)err_bits_to_status(bits);
+    }
+    return SPHGPU_OK;
+}
+
+int alloc_state(Ctx& c, State& s, bool primary)
+{
+    const size_t n = (size_t)c.n;
+    const int D = c.dim;
+    cudaError_t e = cudaSuccess;
+    auto A = [&](double** p) { if (e == cudaSuccess) e = cudaMalloc((void**)p, sizeof(double) * std::max<size_t>(n, 1)); };
+    for (int f = 0; f < F_COUNT; ++f) s.f[f] = nullptr;
+    for (int k = 0; k < D; ++k) {
+        A(&s.f[F_POS + k]); A(&s.f[F_VEL + k]); A(&s.f[F_VELP + k]); A(&s.f[F_ACC + k]);
+    }
+    for (int f = F_MASS; f <= F_PHI; ++f) A(&s.f[f]);
+    if (c.p.sph_type == 2) {
+        for (int k = 0; k < D; ++k) {
+            A(&s.f[F_GRADD + k]); A(&s.f[F_GRADP + k]);
+            for (int d = 0; d < D; ++d) A(&s.f[F_GRADV + 3 * k + d]);
+        }
+    }
+    if (e == cudaSuccess) e = cudaMalloc((void**)&s.id, sizeof(int) * std::max<size_t>(n, 1));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&s.neighbor, sizeof(int) * std::max<size_t>(n, 1));
+    if (primary) {
+        if (e == cudaSuccess) e = cudaMalloc((void**)&s.run, sizeof(int) * std::max<size_t>(n, 1));
+    }
+    if (e != cudaSuccess) return cuda_status(c, e, "state allocation");
+    for (int f = 0; f < F_COUNT; ++f)
+        if (s.f[f]) cudaMemset(s.f[f], 0, sizeof(double) * n);
+    cudaMemset(s.neighbor, 0, sizeof(int) * n);
+    return SPHGPU_OK;
+}
+
+void free_state(State& s, bool primary)
+{
+    for (int f = 0; f < F_COUNT; ++f)
+        if (s.f[f]) cudaFree(s.f[f]);
+    if (s.id) cudaFree(s.id);
+    if (s.neighbor) cudaFree(s.neighbor);
+    if (primary && s.run) cudaFree(s.run);
+}
+
+void free_ctx(Ctx& c)
+{
+    if (c.graph) cudaGraphExecDestroy(c.graph);
+    tree_free(c);
+    free_state(c.st, true);
+    c.alt.run = nullptr;
+    free_state(c.alt, false);
+    void* ptrs[] = {c.d_run_begin, c.d_time, c.d_dt, c.d_hvs, c.d_dtmin, c.d_sums, c.d_err,
+                    c.d_newton_fail, c.d_work, c.d_ovf_list, c.d_stage, c.d_aos, c.d_flush};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    for (void* p : c.mir)
+        if (p) cudaFree(p);
+    for (cudaEvent_t ev : c.ev)
+        if (ev) cudaEventDestroy(ev);
+    if (c.stream) cudaStreamDestroy(c.stream);
+}
+
+int validate(const sphgpu_params* p, int dim, std::string& why)
+{
+    if (!p) { why = "params is NULL"; return SPHGPU_ERR_ARG; }
+    if (dim < 1 || dim > 3) { why = "dim must be 1, 2 or 3"; return SPHGPU_ERR_ARG; }
+    if (p->sph_type < 0 || p->sph_type > 2) { why = "Unknown SPH type"; return SPHGPU_ERR_ARG; }
+    if (p->kernel < 0 || p->kernel > 1) { why = "kernel is unknown."; return SPHGPU_ERR_ARG; }
+    if (p->kernel == 1 && dim == 1) { why = "the Wendland C4 kernel is not defined in 1D (include/kernel/wendland_kernel.hpp:15-27)"; return SPHGPU_ERR_ARG; }
+    if (p->neighbor_number <= 0) { why = "neighborNumber must be positive"; return SPHGPU_ERR_ARG; }
+    if (p->max_level < 1 || p->max_level > MAX_LEVELS - 4) { why = "maxTreeLevel must be in [1, 60]"; return SPHGPU_ERR_ARG; }
+    if (p->leaf_num < 1) { why = "leafParticleNumber must be >= 1"; return SPHGPU_ERR_ARG; }
+    if (p->use_tdav && p->alpha_max < p->alpha_min) { why = "alphaMax < alphaMin"; return SPHGPU_ERR_ARG; }
+    if (p->periodic) {
+        for (int k = 0; k < dim; ++k)
+            if (!(p->range_max[k] > p->range_min[k])) { why = "periodic range must have rangeMax > rangeMin"; return SPHGPU_ERR_ARG; }
+    }
+    if (p->use_gravity && !(p->theta > 0.0)) { why = "theta must be positive"; return SPHGPU_ERR_ARG; }
+    return SPHGPU_OK;
+}
+
+int create_impl(const sphgpu_params* params, int dim, int n_runs, const int* run_sizes,
+                int precision, sphgpu_ctx** out)
+{
+    std::string why;
+    if (!out) return SPHGPU_ERR_ARG;
+    *out = nullptr;
+    int st = validate(params, dim, why);
+    if (st == SPHGPU_OK && (n_runs < 1 || !run_sizes)) { why = "need at least one run"; st = SPHGPU_ERR_ARG; }
+    if (st == SPHGPU_OK && precision != SPHGPU_FP32_PAIR && precision != SPHGPU_FP64) { why = "unknown precision"; st = SPHGPU_ERR_ARG; }
+    long long total = 0;
+    if (st == SPHGPU_OK) {
+        for (int r = 0; r < n_runs; ++r) {
+            if (run_sizes[r] < 1) { why = "every run needs at least one particle"; st = SPHGPU_ERR_ARG; break; }
+            total += run_sizes[r];
+        }
+        if (st == SPHGPU_OK && total > (1LL << 30)) { why = "too many particles"; st = SPHGPU_ERR_ARG; }
+    }
+    int run_bits = 0;
+    while ((1 << run_bits) < n_runs) ++run_bits;
+    if (st == SPHGPU_OK && dim * params->max_level + run_bits > 64) {
+        why = "maxTreeLevel too deep for 64-bit octree keys";
+        st = SPHGPU_ERR_ARG;
+    }
+    if (st == SPHGPU_OK) {
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+            cudaGetLastError();
+            why = "no CUDA device";
+            st = SPHGPU_ERR_NO_DEVICE;
+        }
+    }
+    if (st != SPHGPU_OK) {
+        std::lock_guard<std::mutex> lk(g_err_mutex);
+        g_create_error = why;
+        return st;
+    }
+    sphgpu_ctx* h = new (std::nothrow) sphgpu_ctx();
+    if (!h) return SPHGPU_ERR_ARG;
+    Ctx& c = h->c;
+    c.p = *params;
+    c.dim = dim;
+    c.n = (int)total;
+    c.R = n_runs;
+    c.precision = precision;
+    c.key_levels = params->max_level;
+    c.run_bits = run_bits;
+    c.pb.on = params->periodic;
+    for (int k = 0; k < 3; ++k) {
+        c.pb.lo[k] = params->range_min[k];
+        c.pb.hi[k] = params->range_max[k];
+        c.pb.len[k] = params->range_max[k] - params->range_min[k];
+    }
+    c.run_begin.assign(n_runs + 1, 0);
+    for (int r = 0; r < n_runs; ++r) c.run_begin[r + 1] = c.run_begin[r] + run_sizes[r];
+
+    int rc = SPHGPU_OK;
+    cudaError_t e = cudaGetDevice(&c.device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, c.device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) rc = cuda_status(c, e, "create");
+    if (rc == SPHGPU_OK) rc = alloc_state(c, c.st, true);
+    if (rc == SPHGPU_OK) { rc = alloc_state(c, c.alt, false); c.alt.run = c.st.run; }
+    if (rc == SPHGPU_OK) rc = tree_alloc(c);
+    if (rc == SPHGPU_OK) {
+        const size_t n = (size_t)c.n, R = (size_t)c.R;
+        int maxc = 1;
+        for (int r = 0; r < c.R; ++r) maxc = std::max(maxc, ceil_div(run_sizes[r], 8192));
+        auto A = [&](void** p, size_t bytes) { if (e == cudaSuccess) e = cudaMalloc(p, std::max<size_t>(bytes, 16)); };
+        A((void**)&c.d_run_begin, sizeof(int) * (R + 1));
+        A((void**)&c.d_time, sizeof(double) * R);
+        A((void**)&c.d_dt, sizeof(double) * R);
+        A((void**)&c.d_hvs, sizeof(long long) * R);
+        A((void**)&c.d_dtmin, sizeof(long long) * R);
+        A((void**)&c.d_sums, sizeof(double) * (R * maxc * 7 + R * 7));
+        A((void**)&c.d_err, sizeof(unsigned));
+        A((void**)&c.d_newton_fail, sizeof(int));
+        A((void**)&c.d_work, sizeof(int) * 16);
+        A((void**)&c.d_ovf_list, sizeof(int) * c.max_groups);
+        c.stage_bytes = sizeof(double) * n * (size_t)std::max(9, dim * dim);
+        A((void**)&c.d_stage, c.stage_bytes);
+        // key-ordered mirrors in the pair type, sized for FP64
+        A(&c.mir[0], sizeof(double4_32a) * n);                       // Pre {v, c}
+        A(&c.mir[1], sizeof(double) * n);                        // Pre u
+        A(&c.mir[2], sizeof(double4_32a) * n);                       // Fluid rec0
+        A(&c.mir[3], sizeof(double4_32a) * n);                       // Fluid rec1
+        A(&c.mir[4], sizeof(double4_32a) * n);                       // Fluid rec2
+        A(&c.mir[5], c.p.sph_type == 2 ? sizeof(double) * 16 * n : 16);   // gsph gradients
+        A(&c.mir[6], c.p.use_gravity ? sizeof(double4_32a) * n : 16);          // gravity leaf offsets
+        A(&c.mir[7], c.p.use_gravity ? sizeof(double) * n : 16);           // gravity h
+        for (int q = 0; q < 6 && e == cudaSuccess; ++q) e = cudaEventCreate(&c.ev[q]);
+        if (e != cudaSuccess) rc = cuda_status(c, e, "create");
+    }
+    if (rc == SPHGPU_OK) {
+        cudaMemcpy(c.d_run_begin, c.run_begin.data(), sizeof(int) * (c.R + 1), cudaMemcpyHostToDevice);
+        cudaMemset(c.d_time, 0, sizeof(double) * c.R);
+        cudaMemset(c.d_dt, 0, sizeof(double) * c.R);
+        cudaMemset(c.d_err, 0, sizeof(unsigned));
+        cudaMemset(c.d_newton_fail, 0, sizeof(int));
+        cudaMemset(c.d_work, 0, sizeof(int) * 16);
+        fill_ord_kernel<<<ceil_div(c.R, 128), 128>>>(c.d_hvs, c.R, 1.7976931348623157e308);
+        fill_ord_kernel<<<ceil_div(c.R, 128), 128>>>(c.d_dtmin, c.R, 1.7976931348623157e308);
+        init_ids_kernel<<<ceil_div(c.n, THREADS), THREADS>>>(c.st.id, c.st.run, c.d_run_begin, c.R, c.n);
+        e = cudaDeviceSynchronize();
+        if (e == cudaSuccess) e = cudaGetLastError();
+        if (e != cudaSuccess) rc = cuda_status(c, e, "create");
+    }
+    if (rc != SPHGPU_OK) {
+        {
+            std::lock_guard<std::mutex> lk(g_err_mutex);
+            g_create_error = c.last_error;
+        }
+        free_ctx(c);
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return SPHGPU_OK;
+}
+
+std::map<std::pair<const void*, long long>, int> g_occ;
+std::mutex g_occ_mutex;
+
+// Stages as the Solver calls them.
+void run_pre_stage(Ctx& c)
+{
+    if (c.first_pre) {
+        launch_pre(c, true);    // PreInteraction::initial_smoothing (src/pre_interaction.cpp:171-215)
+        c.first_pre = false;
+    }
+    launch_pre(c, false);
+    launch_set_kernel_size(c);   // BHTree::set_kernel at the end of PreInteraction::calculation
+}
+
+void run_step(Ctx& c, bool timed)
+{
+    cudaStream_t s = c.stream;
+    if (timed) cudaEventRecord(c.ev[0], s);
+    launch_timestep(c);
+    launch_predict(c);
+    if (timed) cudaEventRecord(c.ev[1], s);
+    launch_make_tree(c, false);
+    if (timed) cudaEventRecord(c.ev[2], s);
+    run_pre_stage(c);
+    if (timed) cudaEventRecord(c.ev[3], s);
+    launch_fluid(c);
+    if (timed) cudaEventRecord(c.ev[4], s);
+    if (c.p.use_gravity) launch_gravity(c);
+    if (timed) cudaEventRecord(c.ev[5], s);
+    launch_correct(c);
+    launch_update_time(c);
+}
+
+}  // namespace
+
+// ---- helpers shared with the other translation units ----------------------------------------
+
+int max_optin_smem(const Ctx& c)
+{
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device);
+    return v;
+}
+
+int kernel_occupancy(const void* kern, int threads, size_t smem)
+{
+    const auto key = std::make_pair(kern, (long long)threads * (1LL << 32) + (long long)smem);
+    {
+        std::lock_guard<std::mutex> lk(g_occ_mutex);
+        auto it = g_occ.find(key);
+        if (it != g_occ.end()) return it->second;
+    }
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, threads, smem) != cudaSuccess) {
+        cudaGetLastError();
+        nb = 1;
+    }
+    std::lock_guard<std::mutex> lk(g_occ_mutex);
+    g_occ[key] = nb;
+    return nb;
+}
+
+void reset_work_counters(Ctx& c) { cudaMemsetAsync(c.d_work, 0, sizeof(int) * 16, c.stream); }
+
+void launch_pre(Ctx& c, bool initial)
+{
+    if (c.dim == 1) launch_pre_dim<1>(c, initial);
+    else if (c.dim == 2) launch_pre_dim<2>(c, initial);
+    else launch_pre_dim<3>(c, initial);
+}
+
+void launch_fluid(Ctx& c)
+{
+    if (c.dim == 1) launch_fluid_dim<1>(c);
+    else if (c.dim == 2) launch_fluid_dim<2>(c);
+    else launch_fluid_dim<3>(c);
+}
+
+}  // namespace sphgpu
+
+using sphgpu::Ctx;
+
+#define CTX_OR_FAIL(h)                                                                              \
+    if (!(h)) return SPHGPU_ERR_ARG;                                                                 \
+    Ctx& c = (h)->c;                                                                                 \
+    cudaSetDevice(c.device)
+
+extern "C" {
+
+int sphgpu_create(const sphgpu_params* params, int dim, int n, int precision, sphgpu_ctx** out)
+{
+    if (n < 1) {
+        std::lock_guard<std::mutex> lk(sphgpu::g_err_mutex);
+        sphgpu::g_create_error = "particle number must be positive";
+        if (out) *out = nullptr;
+        return SPHGPU_ERR_ARG;
+    }
+    return sphgpu::create_impl(params, dim, 1, &n, precision, out);
+}
+
+int sphgpu_create_batch(const sphgpu_params* params, int dim, int n_runs, const int* run_sizes,
+                        int precision, sphgpu_ctx** out)
+{
+    return sphgpu::create_impl(params, dim, n_runs, run_sizes, precision, out);
+}
+
+int sphgpu_destroy(sphgpu_ctx* h)
+{
+    if (!h) return SPHGPU_OK;
+    cudaSetDevice(h->c.device);
+    cudaStreamSynchronize(h->c.stream);
+    sphgpu::free_ctx(h->c);
+    delete h;
+    return SPHGPU_OK;
+}
+
+int sphgpu_set_field(sphgpu_ctx* h, int field, const double* host)
+{
+    CTX_OR_FAIL(h);
+    if (!host) return SPHGPU_ERR_ARG;
+    if (field == SPHGPU_NEIGHBOR) {
+        cudaMemcpyAsync(c.d_stage, host, sizeof(double) * c.n, cudaMemcpyHostToDevice, c.stream);
+        sphgpu::scatter_int_as_double_kernel<<<sphgpu::ceil_div(c.n, 256), 256, 0, c.stream>>>(c.st.neighbor, c.st.id, c.n, c.d_stage);
+        return sphgpu::finish(c, "set_field");
+    }
+    int slot, width;
+    if (!sphgpu::field_slot(c, field, &slot, &width)) { c.last_error = "unknown field"; return SPHGPU_ERR_ARG; }
+    cudaMemcpyAsync(c.d_stage, host, sizeof(double) * c.n * width, cudaMemcpyHostToDevice, c.stream);
+    sphgpu::scatter_field_kernel<<<sphgpu::ceil_div(c.n, 256), 256, 0, c.stream>>>(
+        sphgpu::field_map(c.st, slot, width, c.dim), c.st.id, c.n, c.d_stage);
+    if (field == SPHGPU_POS || field == SPHGPU_MASS) c.tree_valid = false;   // node boxes and moments
+    if (field == SPHGPU_SML) c.kernel_size_valid = false;                    // node kernel sizes
+    c.graph_valid = false;
+    return sphgpu::finish(c, "set_field");
+}
+
+int sphgpu_get_field(sphgpu_ctx* h, int field, double* host)
+{
+    CTX_OR_FAIL(h);
+    if (!host) return SPHGPU_ERR_ARG;
+    if (field == SPHGPU_NEIGHBOR) {
+        sphgpu::gather_int_as_double_kernel<<<sphgpu::ceil_div(c.n, 256), 256, 0, c.stream>>>(c.st.neighbor, c.st.id, c.n, c.d_stage);
+        cudaMemcpyAsync(host, c.d_stage, sizeof(double) * c.n, cudaMemcpyDeviceToHost, c.stream);
+        return sphgpu::finish(c, "get_field");
+    }
+    int slot, width;
+    if (!sphgpu::field_slot(c, field, &slot, &width)) { c.last_error = "unknown field"; return SPHGPU_ERR_ARG; }
+    sphgpu::gather_field_kernel<<<sphgpu::ceil_div(c.n, 256), 256, 0, c.stream>>>(
+        sphgpu::field_map(c.st, slot, width, c.dim), c.st.id, c.n, c.d_stage);
+    cudaMemcpyAsync(host, c.d_stage, sizeof(double) * c.n * width, cudaMemcpyDeviceToHost, c.stream);
+    return sphgpu::finish(c, "get_field");
+}
+
+int sphgpu_upload_aos(sphgpu_ctx* h, const void* base, const sphgpu_aos_layout* layout)
+{
+    CTX_OR_FAIL(h);
+    if (!base || !layout || layout->stride == 0) return SPHGPU_ERR_ARG;
+    const size_t bytes = layout->stride * (size_t)c.n;
+    if (bytes > c.aos_bytes) {
+        if (c.d_aos) cudaFree(c.d_aos);
+        c.d_aos = nullptr;
+        c.aos_bytes = 0;
+        cudaError_t e = cudaMalloc((void**)&c.d_aos, bytes);
+        if (e != cudaSuccess) return sphgpu::cuda_status(c, e, "upload_aos");
+        c.aos_bytes = bytes;
+    }
+    sphgpu::AosMap m{};
+    const long offs[16] = {layout->pos, layout->vel, layout->vel_p, layout->acc, layout->mass,
+                           layout->dens, layout->pres, layout->ene, layout->ene_p, layout->dene,
+                           layout->sml, layout->sound, layout->balsara, layout->alpha,
+                           layout->gradh, layout->phi};
+    const int slots[16] = {sphgpu::F_POS, sphgpu::F_VEL, sphgpu::F_VELP, sphgpu::F_ACC, sphgpu::F_MASS,
+                           sphgpu::F_DENS, sphgpu::F_PRES, sphgpu::F_ENE, sphgpu::F_ENEP, sphgpu::F_DENE,
+                           sphgpu::F_SML, sphgpu::F_SOUND, sphgpu::F_BALSARA, sphgpu::F_ALPHA,
+                           sphgpu::F_GRADH, sphgpu::F_PHI};
+    for (int q = 0; q < 16; ++q) {
+        if (offs[q] < 0) continue;
+        m.off[m.nf] = offs[q];
+        m.slot[m.nf] = slots[q];
+        m.width[m.nf] = q < 4 ? c.dim : 1;
+        ++m.nf;
+    }
+    m.off_nb = layout->neighbor;
+    m.stride = layout->stride;
+    cudaMemcpyAsync(c.d_aos, base, bytes, cudaMemcpyHostToDevice, c.stream);
+    sphgpu::aos_upload_kernel<<<sphgpu::ceil_div(c.n, 256), 256, 0, c.stream>>>(c.st, m, c.d_aos, c.n);
+    c.tree_valid = false;
+    c.kernel_size_valid = false;
+    c.graph_valid = false;
+    return sphgpu::finish(c, "upload_aos");
+}
+
+int sphgpu_download_aos(sphgpu_ctx* h, void* base, const sphgpu_aos_layout* layout)
+{
+    CTX_OR_FAIL(h);
+    if (!base || !layout || layout->stride == 0) return SPHGPU_ERR_ARG;
+    const size_t bytes = layout->stride * (size_t)c.n;
+    if (bytes > c.aos_bytes) {
+        if (c.d_aos) cudaFree(c.d_aos);
+        c.d_aos = nullptr;
+        c.aos_bytes = 0;
+        cudaError_t e = cudaMalloc((void**)&c.d_aos, bytes);
+        if (e != cudaSuccess) return sphgpu::cuda_status(c, e, "download_aos");
+        c.aos_bytes = bytes;
+    }
+    sphgpu::AosMap m{};
+    const long offs[16] = {layout->pos, layout->vel, layout->vel_p, layout->acc, layout->mass,
+                           layout->dens, layout->pres, layout->ene, layout->ene_p, layout->dene,
+                           layout->sml, layout->sound, layout->balsara, layout->alpha,
+                           layout->gradh, layout->phi};
+    const int slots[16] = {sphgpu::F_POS, sphgpu::F_VEL, sphgpu::F_VELP, sphgpu::F_ACC, sphgpu::F_MASS,
+                           sphgpu::F_DENS, sphgpu::F_PRES, sphgpu::F_ENE, sphgpu::F_ENEP, sphgpu::F_DENE,
+                           sphgpu::F_SML, sphgpu::F_SOUND, sphgpu::F_BALSARA, sphgpu::F_ALPHA,
+                           sphgpu::F_GRADH, sphgpu::F_PHI};
+    for (int q = 0; q < 16; ++q) {
+        if (offs[q] < 0) continue;
+        m.off[m.nf] = offs[q];
+        m.slot[m.nf] = slots[q];
+        m.width[m.nf] = q < 4 ? c.dim : 1;
+        ++m.nf;
+    }
+    m.off_nb = layout->neighbor;
+    m.stride = layout->stride;
+    // the members outside the layout keep the caller's values
+    cudaMemcpyAsync(c.d_aos, base, bytes, cudaMemcpyHostToDevice, c.stream);
+    sphgpu::aos_download_kernel<<<sphgpu::ceil_div(c.n, 256), 256, 0, c.stream>>>(c.st, m, c.d_aos, c.n);
+    cudaMemcpyAsync(base, c.d_aos, bytes, cudaMemcpyDeviceToHost, c.stream);
+    return sphgpu::finish(c, "download_aos");
+}
+
+int sphgpu_set_scalar(sphgpu_ctx* h, int which, int run, double value)
+{
+    CTX_OR_FAIL(h);
+    if (run < 0 || run >= c.R) return SPHGPU_ERR_ARG;
+    cudaError_t e = cudaSuccess;
+    if (which == SPHGPU_TIME) e = cudaMemcpy(c.d_time + run, &value, sizeof(double), cudaMemcpyHostToDevice);
+    else if (which == SPHGPU_DT) e = cudaMemcpy(c.d_dt + run, &value, sizeof(double), cudaMemcpyHostToDevice);
+    else if (which == SPHGPU_H_PER_V_SIG) {
+        const long long o = sphgpu::host_dbl_to_ord(value);
+        e = cudaMemcpy(c.d_hvs + run, &o, sizeof(long long), cudaMemcpyHostToDevice);
+    } else return SPHGPU_ERR_ARG;
+    return sphgpu::cuda_status(c, e, "set_scalar");
+}
+
+int sphgpu_get_scalar(sphgpu_ctx* h, int which, int run, double* value)
+{
+    CTX_OR_FAIL(h);
+    if (run < 0 || run >= c.R || !value) return SPHGPU_ERR_ARG;
+    cudaError_t e = cudaStreamSynchronize(c.stream);
+    if (e != cudaSuccess) return sphgpu::cuda_status(c, e, "get_scalar");
+    if (which == SPHGPU_TIME) e = cudaMemcpy(value, c.d_time + run, sizeof(double), cudaMemcpyDeviceToHost);
+    else if (which == SPHGPU_DT) e = cudaMemcpy(value, c.d_dt + run, sizeof(double), cudaMemcpyDeviceToHost);
+    else if (which == SPHGPU_H_PER_V_SIG) {
+        long long o = 0;
+        e = cudaMemcpy(&o, c.d_hvs + run, sizeof(long long), cudaMemcpyDeviceToHost);
+        o = o >= 0 ? o : (o ^ 0x7fffffffffffffffLL);
+        memcpy(value, &o, sizeof(double));
+    } else return SPHGPU_ERR_ARG;
+    return sphgpu::cuda_status(c, e, "get_scalar");
+}
+
+int sphgpu_make_tree(sphgpu_ctx* h)
+{
+    CTX_OR_FAIL(h);
+    sphgpu::launch_make_tree(c, true);
+    return sphgpu::finish(c, "make_tree");
+}
+
+int sphgpu_pre_interaction(sphgpu_ctx* h)
+{
+    CTX_OR_FAIL(h);
+    if (!c.tree_valid) { c.last_error = "pre_interaction before make_tree"; return SPHGPU_ERR_STATE; }
+    sphgpu::run_pre_stage(c);
+    return sphgpu::finish(c, "pre_interaction");
+}
+
+int sphgpu_fluid_force(sphgpu_ctx* h)
+{
+    CTX_OR_FAIL(h);
+    if (!c.tree_valid) { c.last_error = "fluid_force before make_tree"; return SPHGPU_ERR_STATE; }
+    if (!c.kernel_size_valid) sphgpu::launch_set_kernel_size(c);
+    sphgpu::launch_fluid(c);
+    return sphgpu::finish(c, "fluid_force");
+}
+
+int sphgpu_gravity_force(sphgpu_ctx* h)
+{
+    CTX_OR_FAIL(h);
+    if (!c.p.use_gravity) return SPHGPU_OK;   // GravityForce::calculation returns at once
+    if (!c.tree_valid) { c.last_error = "gravity_force before make_tree"; return SPHGPU_ERR_STATE; }
+    sphgpu::launch_gravity(c);
+    return sphgpu::finish(c, "gravity_force");
+}
+
+int sphgpu_timestep(sphgpu_ctx* h)
+{
+    CTX_OR_FAIL(h);
+    sphgpu::launch_timestep(c);
+    return sphgpu::finish(c, "timestep");
+}
+
+int sphgpu_predict(sphgpu_ctx* h)
+{
+    CTX_OR_FAIL(h);
+    sphgpu::launch_predict(c);
+    c.tree_valid = false;
+    return sphgpu::finish(c, "predict");
+}
+
+int sphgpu_correct(sphgpu_ctx* h)
+{
+    CTX_OR_FAIL(h);
+    sphgpu::launch_correct(c);
+    return sphgpu::finish(c, "correct");
+}
+
+int sphgpu_initialize(sphgpu_ctx* h)
+{
+    CTX_OR_FAIL(h);
+    sphgpu::launch_init_fields(c);
+    sphgpu::launch_make_tree(c, true);
+    c.first_pre = true;
+    sphgpu::run_pre_stage(c);
+    sphgpu::launch_fluid(c);
+    if (c.p.use_gravity) sphgpu::launch_gravity(c);
+    c.graph_valid = false;
+    return sphgpu::finish(c, "initialize");
+}
+
+int sphgpu_step(sphgpu_ctx* h, int n_steps)
+{
+    CTX_OR_FAIL(h);
+    if (n_steps < 0) return SPHGPU_ERR_ARG;
+    if (c.first_pre) { c.last_error = "step before initialize"; return SPHGPU_ERR_STATE; }
+    for (int s = 0; s < n_steps; ++s) {
+        if (c.timing || !c.use_graph) {
+            sphgpu::run_step(c, c.timing);
+            if (c.timing) {
+                cudaEventRecord(c.ev[6], c.stream);
+                cudaEventSynchronize(c.ev[6]);
+                float ms[6];
+                for (int q = 0; q < 6; ++q) cudaEventElapsedTime(&ms[q], c.ev[q], c.ev[q + 1]);
+                c.stage_ms[0] = ms[1];            // tree
+                c.stage_ms[1] = ms[2];            // pre
+                c.stage_ms[2] = ms[3];            // fluid
+                c.stage_ms[3] = ms[4];            // gravity
+                c.stage_ms[4] = ms[0] + ms[5];    // timestep, predict, correct
+            }
+            continue;
+        }
+        if (!c.graph_valid) {
+            // the first call on a fresh configuration runs eagerly (caches launch shapes),
+            // then the step is captured once and replayed from then on
+            if (c.graph) { cudaGraphExecDestroy(c.graph); c.graph = nullptr; }
+            if (!c.warm) {
+                sphgpu::run_step(c, false);
+                c.warm = true;
+                continue;
+            }
+            cudaGraph_t g = nullptr;
+            cudaError_t e = cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal);
+            if (e != cudaSuccess) return sphgpu::cuda_status(c, e, "step capture");
+            sphgpu::run_step(c, false);
+            e = cudaStreamEndCapture(c.stream, &g);
+            if (e != cudaSuccess) return sphgpu::cuda_status(c, e, "step capture");
+            {
+                size_t nn = 0;
+                cudaGraphGetNodes(g, nullptr, &nn);
+                std::vector<cudaGraphNode_t> nodes(nn);
+                cudaGraphGetNodes(g, nodes.data(), &nn);
+                int nk = 0;
+                for (auto nd : nodes) {
+                    cudaGraphNodeType ty;
+                    cudaGraphNodeGetType(nd, &ty);
+                    if (ty == cudaGraphNodeTypeKernel) ++nk;
+                }
+                c.graph_kernels = nk;
+            }
+            e = cudaGraphInstantiate(&c.graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) return sphgpu::cuda_status(c, e, "step instantiate");
+            c.graph_valid = true;
+        }
+        cudaError_t e = cudaGraphLaunch(c.graph, c.stream);
+        if (e != cudaSuccess) return sphgpu::cuda_status(c, e, "step launch");
+    }
+    sphgpu::nonfinite_kernel<<<sphgpu::ceil_div(c.n, 256), 256, 0, c.stream>>>(c.st, c.n, c.dim, c.d_err);
+    return sphgpu::finish(c, "step");
+}
+
+int sphgpu_synchronize(sphgpu_ctx* h)
+{
+    CTX_OR_FAIL(h);
+    return sphgpu::finish(c, "synchronize");
+}
+
+int sphgpu_neighbors(sphgpu_ctx* h, int is_ij, int* counts, int* list, int cap)
+{
+    CTX_OR_FAIL(h);
+    if (!counts || (list && cap < 1) || (!list && cap != 0)) return SPHGPU_ERR_ARG;
+    if (!c.tree_valid) sphgpu::launch_make_tree(c, true);
+    if (is_ij && !c.kernel_size_valid) sphgpu::launch_set_kernel_size(c);
+    int *dc = nullptr, *dl = nullptr;
+    cudaError_t e = cudaMalloc((void**)&dc, sizeof(int) * c.n);
+    if (e == cudaSuccess && list) e = cudaMalloc((void**)&dl, sizeof(int) * (size_t)c.n * cap);
+    if (e != cudaSuccess) {
+        if (dc) cudaFree(dc);
+        return sphgpu::cuda_status(c, e, "neighbors");
+    }
+    sphgpu::launch_neighbors(c, is_ij, dc, dl, cap);
+    cudaMemcpyAsync(counts, dc, sizeof(int) * c.n, cudaMemcpyDeviceToHost, c.stream);
+    if (list) cudaMemcpyAsync(list, dl, sizeof(int) * (size_t)c.n * cap, cudaMemcpyDeviceToHost, c.stream);
+    const int rc = sphgpu::finish(c, "neighbors");
+    cudaFree(dc);
+    if (dl) cudaFree(dl);
+    return rc;
+}
+
+int sphgpu_energy(sphgpu_ctx* h, int run, double* out)
+{
+    CTX_OR_FAIL(h);
+    if (run < 0 || run >= c.R || !out) return SPHGPU_ERR_ARG;
+    int maxc = 1;
+    for (int r = 0; r < c.R; ++r) maxc = std::max(maxc, sphgpu::ceil_div(c.run_begin[r + 1] - c.run_begin[r], 8192));
+    double* d_out = c.d_sums + (size_t)c.R * maxc * 7;
+    sphgpu::launch_energy(c, d_out);
+    double v[7];
+    cudaMemcpyAsync(v, d_out + (size_t)run * 7, sizeof(v), cudaMemcpyDeviceToHost, c.stream);
+    const int rc = sphgpu::finish(c, "energy");
+    if (rc != SPHGPU_OK) return rc;
+    for (int q = 0; q < 4; ++q) out[q] = v[q];
+    for (int k = 0; k < c.dim; ++k) out[4 + k] = v[4 + k];
+    return SPHGPU_OK;
+}
+
+int sphgpu_tree_stats(sphgpu_ctx* h, int* out)
+{
+    CTX_OR_FAIL(h);
+    if (!out) return SPHGPU_ERR_ARG;
+    if (!c.tree_valid) { c.last_error = "no tree"; return SPHGPU_ERR_STATE; }
+    int rc = sphgpu::finish(c, "tree_stats");
+    if (rc != SPHGPU_OK) return rc;
+    int total = 0;
+    cudaMemcpy(&total, c.node_total, sizeof(int), cudaMemcpyDeviceToHost);
+    std::vector<int> first(total), level(total);
+    cudaMemcpy(first.data(), c.nd_first, sizeof(int) * total, cudaMemcpyDeviceToHost);
+    cudaMemcpy(level.data(), c.nd_level, sizeof(int) * total, cudaMemcpyDeviceToHost);
+    for (int q = 0; q < 130; ++q) out[q] = 0;
+    for (int i = c.R; i < total; ++i) {
+        out[0]++;
+        const int L = std::min(level[i], 63);
+        out[2 + L]++;
+        if (first[i] < 0) { out[1]++; out[66 + L]++; }
+    }
+    return SPHGPU_OK;
+}
+
+int sphgpu_newton_failures(sphgpu_ctx* h, int* count)
+{
+    CTX_OR_FAIL(h);
+    if (!count) return SPHGPU_ERR_ARG;
+    cudaError_t e = cudaStreamSynchronize(c.stream);
+    if (e == cudaSuccess) e = cudaMemcpy(count, c.d_newton_fail, sizeof(int), cudaMemcpyDeviceToHost);
+    return sphgpu::cuda_status(c, e, "newton_failures");
+}
+
+const char* sphgpu_last_error(const sphgpu_ctx* h)
+{
+    if (!h) {
+        std::lock_guard<std::mutex> lk(sphgpu::g_err_mutex);
+        return sphgpu::g_create_error.c_str();
+    }
+    return h->c.last_error.c_str();
+}
+
+int sphgpu_set_tuning(sphgpu_ctx* h, int which, int value)
+{
+    CTX_OR_FAIL(h);
+    switch (which) {
+    case 0:
+        if (value < 1 || value > 8) return SPHGPU_ERR_ARG;
+        c.gw_pre = value;
+        c.tree_valid = false;
+        c.kernel_size_valid = false;
+        break;
+    case 1: case 2:
+        if (value < 1 || value > 8) return SPHGPU_ERR_ARG;
+        if (which == 1) c.gw_fluid = value; else c.gw_grav = value;
+        break;
+    case 3:
+        if (value < 0 || (value % 32) != 0 || value > 16384) return SPHGPU_ERR_ARG;
+        c.tile_cap = value;
+        break;
+    case 4: c.autotune = value != 0; break;
+    case 5: c.timing = value != 0; break;
+    case 6: c.use_graph = value != 0; break;
+    default: return SPHGPU_ERR_ARG;
+    }
+    c.graph_valid = false;
+    c.warm = false;
+    return SPHGPU_OK;
+}
+
+int sphgpu_get_tuning(sphgpu_ctx* h, int which, int* value)
+{
+    CTX_OR_FAIL(h);
+    if (!value) return SPHGPU_ERR_ARG;
+    switch (which) {
+    case 0: *value = c.gw_pre; break;
+    case 1: *value = c.gw_fluid; break;
+    case 2: *value = c.gw_grav; break;
+    case 3: *value = c.tile_cap; break;
+    case 4: *value = c.autotune; break;
+    case 5: *value = c.timing; break;
+    case 6: *value = c.use_graph; break;
+    case 7: *value = c.graph_kernels; break;
+    default: return SPHGPU_ERR_ARG;
+    }
+    return SPHGPU_OK;
+}
+
+int sphgpu_bench_steps(sphgpu_ctx* h, int n_steps, int flush_l2, double* ms)
+{
+    CTX_OR_FAIL(h);
+    if (n_steps < 1 || !ms) return SPHGPU_ERR_ARG;
+    if (c.first_pre) { c.last_error = "bench before initialize"; return SPHGPU_ERR_STATE; }
+    if (flush_l2 && !c.d_flush) {
+        int l2 = 0;
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, c.device);
+        c.flush_bytes = (size_t)std::max(l2, 1 << 20) * 2;
+        cudaError_t e = cudaMalloc((void**)&c.d_flush, c.flush_bytes);
+        if (e != cudaSuccess) { c.d_flush = nullptr; return sphgpu::cuda_status(c, e, "bench flush buffer"); }
+    }
+    // make sure the step graph exists (the capture path runs its own steps first)
+    if (c.use_graph && !c.timing && !c.graph_valid) {
+        int rc = sphgpu_step(h, 2);
+        if (rc != SPHGPU_OK) return rc;
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    double total = 0.0;
+    for (int s = 0; s < n_steps; ++s) {
+        if (flush_l2) cudaMemsetAsync(c.d_flush, s & 0xff, c.flush_bytes, c.stream);
+        cudaEventRecord(e0, c.stream);
+        if (c.use_graph && !c.timing) cudaGraphLaunch(c.graph, c.stream);
+        else sphgpu::run_step(c, false);
+        cudaEventRecord(e1, c.stream);
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) { cudaEventDestroy(e0); cudaEventDestroy(e1); return sphgpu::cuda_status(c, e, "bench"); }
+        float m = 0.f;
+        cudaEventElapsedTime(&m, e0, e1);
+        total += m;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = total;
+    return sphgpu::finish(c, "bench");
+}
+
+int sphgpu_stage_times(sphgpu_ctx* h, double* out)
+{
+    CTX_OR_FAIL(h);
+    if (!out) return SPHGPU_ERR_ARG;
+    for (int q = 0; q < 5; ++q) out[q] = c.stage_ms[q];
+    return SPHGPU_OK;
+}
+
+}  // extern "C"

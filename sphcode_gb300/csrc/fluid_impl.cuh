@@ -1,0 +1,381 @@
+// FluidForce on the device: pressure-gradient, artificial-viscosity and artificial-conductivity
+// pair sums of the standard SPH form (src/fluid_force.cpp:26-116), of the pressure-energy form
+// (src/disph/d_fluid_force.cpp:26-86) and of the Godunov form with MUSCL reconstruction and the
+// HLL solver (src/gsph/g_fluid_force.cpp:28-199).
+//
+// One CTA per target group (group.cuh).  The pair set of target i is the reference's
+// {j : r_ij < max(h_i, h_j), r_ij != 0}: the octree walk keeps leaves within max(R, node kernel
+// size) of the group box (BHTree::neighbor_search with is_ij, src/bhtree.cpp:237), staging keeps
+// sources within max(R, h_j) per axis, and the membership test runs in the pair type T outside a
+// relative guard band and in the reference's FP64 arithmetic inside it.  Per-source fields are
+// read from key-ordered mirror records in T.
+#pragma once
+
+#include "context.cuh"
+#include "group.cuh"
+
+namespace sphgpu {
+
+template <typename T>
+struct FluidArgs {
+    using V4 = typename Vec4<T>::type;
+    State st;
+    TreeView tv;
+    Periodic pb;
+    SmemLayout L;
+    GroupWork work;
+    const V4* rec0;   // {vx, vy, vz, h}
+    const V4* rec1;   // {rho, P, c, X}   X: ssph P/rho^2 gradh, disph gradh, gsph 0
+    const V4* rec2;   // {alpha, balsara, u, Y}   Y: disph u/P
+    const T* grad;    // gsph: 16 per particle, grad rho [0,D), grad P [3,3+D), grad v [6 + 3k + d]
+    double gamma;
+    int use_ac;
+    int ac_gravity;
+    double alpha_ac;
+    int gsph_2nd;
+    const double* dt_run;
+};
+
+// van Leer limiter (src/gsph/g_fluid_force.cpp:28-36).
+template <typename T>
+__device__ __forceinline__ T van_leer(T dq1, T dq2)
+{
+    const T p = dq1 * dq2;
+    return p <= T(0) ? T(0) : T(2) * p / (dq1 + dq2);
+}
+
+// HLL Riemann solver with Roe-averaged wave speeds (src/gsph/g_fluid_force.cpp:168-199).
+// left/right = {u, rho, p, c}.
+template <typename T>
+__device__ __forceinline__ void hll(const T* l, const T* r, T& pstar, T& vstar)
+{
+    const T roe_l = sqrt(l[1]), roe_r = sqrt(r[1]);
+    const T roe_inv = T(1) / (roe_l + roe_r);
+    const T u_t = (roe_l * l[0] + roe_r * r[0]) * roe_inv;
+    const T c_t = (roe_l * l[3] + roe_r * r[3]) * roe_inv;
+    const T s_l = fmin(l[0] - l[3], u_t - c_t);
+    const T s_r = fmax(r[0] + r[3], u_t + c_t);
+    const T c1 = l[1] * (s_l - l[0]);
+    const T c2 = r[1] * (s_r - r[0]);
+    const T c3 = T(1) / (c1 - c2);
+    const T c4 = l[2] - l[0] * c1;
+    const T c5 = r[2] - r[0] * c2;
+    vstar = (c5 - c4) * c3;
+    pstar = (c1 * c5 - c2 * c4) * c3;
+}
+
+template <int D, typename T, int TYPE, int K>
+__global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
+{
+    using V4 = typename Vec4<T>::type;
+    using KF = Kern<D, K, T>;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const SmemLayout L = a.L;
+    GroupMisc* gm = reinterpret_cast<GroupMisc*>(smem + L.off_misc);
+    const Tile<T> tile = tile_of<T>(smem, L);
+    const State& st = a.st;
+    const int t = threadIdx.x;
+
+    for (;;) {
+        const int g = next_group(gm, a.work);
+        if (g < 0) break;
+        const int gb = a.work.g_begin[g], gn = a.work.g_count[g];
+        const bool active = t < gn;
+        const int i = gb + (active ? t : 0);
+        double xi[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) xi[k] = st.f[F_POS + k][i];
+        const double hi = st.f[F_SML][i];
+        group_box<D>(gm, xi, active, hi, a.pb);
+        const int run = st.run[gb];
+        if (!group_walk<D>(smem, L, gm, a.tv, run, true, a.pb)) { report_overflow(a.work, g); continue; }
+        {
+            const double R = gm->R;
+            double he[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) he[k] = gm->he[k];
+            const int ntile = stage_sources<D, T>(smem, L, gm, st, a.pb, tile, [&](int j, const double* off) {
+                const double r = fmax(R, st.f[F_SML][j]);
+#pragma unroll
+                for (int k = 0; k < D; ++k)
+                    if (fabs(off[k]) > (he[k] + r) * (1.0 + 1e-12)) return false;
+                return true;
+            }, [&](int j) { return (T)st.f[F_MASS][j]; });
+            if (ntile < 0) { report_overflow(a.work, g); continue; }
+            gm->ntile = ntile;
+        }
+        const int ntile = gm->ntile;
+
+        // Relative guard band of the T-precision test r^2 < H^2 for H >= h_min of the group:
+        // |r2_T - r2| <= 2 r E + D E^2 + 2u r^2 with E <= u (2 he + 3 H) + FP64 rounding of the
+        // offsets; at r ~ H this is below delta * H^2.
+        double delta;
+        {
+            double hem = 0.0;
+#pragma unroll
+            for (int k = 0; k < D; ++k) hem = fmax(hem, gm->he[k]);
+            const double u = Unit<T>::u, u64 = Unit<double>::u;
+            const double hm = gm->rmin;
+            const double e_rel = u * (2.0 * hem / hm + 3.0) * 1.5 + 8.0 * u64 * (gm->scale / hm + 1.0);
+            delta = 2.0 * (2.0 * 1.7320508075688772 * e_rel + D * e_rel * e_rel + 8.0 * u);
+        }
+        const T dlo = (T)(1.0 - delta), dhi = (T)(1.0 + delta);
+
+        T xo[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) xo[k] = (T)min_image(xi[k] - gm->gc[k], a.pb, k);
+        const V4 r0i = a.rec0[i], r1i = a.rec1[i], r2i = a.rec2[i];
+        const T vi[3] = {r0i.x, r0i.y, r0i.z};
+        const T hiT = r0i.w;
+        const T rho_i = r1i.x, p_i = r1i.y, c_i = r1i.z, X_i = r1i.w;
+        const T al_i = r2i.x, b_i = r2i.y, u_i = r2i.z;
+        const T m_i = (T)st.f[F_MASS][i];
+        const T gm1 = (T)(a.gamma - 1.0);
+        // ssph: P_i/rho_i^2 gradh_i ; disph: (gamma-1)^2 u_i / P_i, (gamma-1)^2 u_i, 1/(m_i u_i)
+        const T g2u_i = gm1 * gm1 * u_i;
+        const T g2u_per_p_i = g2u_i / p_i;
+        const T mu_inv_i = T(1) / (m_i * u_i);
+        const T rho2_inv_i = T(1) / (rho_i * rho_i);
+        const T dt = (T)a.dt_run[run];
+        const T gamma = (T)a.gamma;
+        const T alpha_ac = (T)a.alpha_ac;
+        T gi[16];
+        if (TYPE == 2 && a.gsph_2nd) {
+#pragma unroll
+            for (int q = 0; q < 16; ++q) gi[q] = a.grad[(size_t)i * 16 + q];
+        }
+
+        Sum<T> acc[D], dene;
+#pragma unroll
+        for (int k = 0; k < D; ++k) acc[k].zero();
+        dene.zero();
+
+        if (active) {
+            for (int s = 0; s < ntile; ++s) {
+                const V4 p = tile.pm[s];
+                T rv[D];
+                const T r2 = tile_r2<D, T>(xo, p, rv);
+                const int j = tile.idx[s];
+                const V4 r0j = a.rec0[j];
+                const T hj = r0j.w;
+                const T H = hiT > hj ? hiT : hj;
+                const T H2 = H * H;
+                if (r2 >= H2 * dhi) continue;
+                if (j == i) continue;
+                if (!(r2 < H2 * dlo) || r2 == T(0)) {
+                    const double r2x = exact_r2<D>(st, xi, j, a.pb);
+                    const double rx = __dsqrt_rn(r2x);
+                    if (rx >= fmax(hi, st.f[F_SML][j]) || rx == 0.0) continue;
+                    if (r2 == T(0)) continue;   // unresolvable in T (coincident offsets)
+                }
+                const T r = sqrt(r2);
+                const T cfi = KF::dw_coef(r, hiT);
+                const T cfj = KF::dw_coef(r, hj);
+                const V4 r1j = a.rec1[j];
+                const T mj = p.w;
+                if (TYPE == 2) {
+                    // ---- Godunov SPH pair (src/gsph/g_fluid_force.cpp:79-163) ----
+                    const T rho_j = r1j.x, p_j = r1j.y, c_j = r1j.z;
+                    const T r_inv = T(1) / r;
+                    T e[D];
+#pragma unroll
+                    for (int k = 0; k < D; ++k) e[k] = rv[k] * r_inv;
+                    const T vj[3] = {r0j.x, r0j.y, r0j.z};
+                    T ve_i = T(0), ve_j = T(0);
+#pragma unroll
+                    for (int k = 0; k < D; ++k) { ve_i += vi[k] * e[k]; ve_j += vj[k] * e[k]; }
+                    T left[4], right[4];
+                    if (a.gsph_2nd) {
+                        const T* gj = a.grad + (size_t)j * 16;
+                        const T delta_i = T(0.5) * (T(1) - c_i * dt * r_inv);
+                        const T delta_j = T(0.5) * (T(1) - c_j * dt * r_inv);
+                        // velocity: e . (grad v) . e * r
+                        T dve_i = T(0), dve_j = T(0);
+#pragma unroll
+                        for (int k = 0; k < D; ++k) {
+                            T si = T(0), sj = T(0);
+#pragma unroll
+                            for (int d = 0; d < D; ++d) { si += gi[6 + 3 * k + d] * e[d]; sj += gj[6 + 3 * k + d] * e[d]; }
+                            dve_i += si * e[k];
+                            dve_j += sj * e[k];
+                        }
+                        dve_i *= r;
+                        dve_j *= r;
+                        const T dv_ij = ve_i - ve_j;
+                        right[0] = ve_i - van_leer(dv_ij, dve_i) * delta_i;
+                        left[0] = ve_j + van_leer(dv_ij, dve_j) * delta_j;
+                        T ddi = T(0), ddj = T(0), dpi = T(0), dpj = T(0);
+#pragma unroll
+                        for (int k = 0; k < D; ++k) {
+                            ddi += gi[k] * e[k]; ddj += gj[k] * e[k];
+                            dpi += gi[3 + k] * e[k]; dpj += gj[3 + k] * e[k];
+                        }
+                        ddi *= r; ddj *= r; dpi *= r; dpj *= r;
+                        const T dd_ij = rho_i - rho_j, dp_ij = p_i - p_j;
+                        right[1] = rho_i - van_leer(dd_ij, ddi) * delta_i;
+                        left[1] = rho_j + van_leer(dd_ij, ddj) * delta_j;
+                        right[2] = p_i - van_leer(dp_ij, dpi) * delta_i;
+                        left[2] = p_j + van_leer(dp_ij, dpj) * delta_j;
+                        right[3] = sqrt(gamma * right[2] / right[1]);
+                        left[3] = sqrt(gamma * left[2] / left[1]);
+                    } else {
+                        right[0] = ve_i; right[1] = rho_i; right[2] = p_i; right[3] = c_i;
+                        left[0] = ve_j; left[1] = rho_j; left[2] = p_j; left[3] = c_j;
+                    }
+                    T pstar, vstar;
+                    hll<T>(left, right, pstar, vstar);
+                    const T ci_ = mj * pstar * rho2_inv_i * cfi + mj * pstar / (rho_j * rho_j) * cfj;
+                    // f = r_ij * ci_ ; dene -= f . (e vstar - v_i)
+                    T fv = T(0);
+#pragma unroll
+                    for (int k = 0; k < D; ++k) {
+                        const T f = rv[k] * ci_;
+                        acc[k].add(-f);
+                        fv += f * (e[k] * vstar - vi[k]);
+                    }
+                    dene.add(-fv);
+                } else {
+                    const V4 r2j = a.rec2[j];
+                    const T rho_j = r1j.x, p_j = r1j.y, c_j = r1j.z, X_j = r1j.w;
+                    T vr = T(0);
+                    vr += rv[0] * (vi[0] - r0j.x);
+                    if (D > 1) vr += rv[D > 1 ? 1 : 0] * (vi[1] - r0j.y);
+                    if (D > 2) vr += rv[D > 2 ? 2 : 0] * (vi[2] - r0j.z);
+                    // Monaghan (1997) signal-velocity viscosity (src/fluid_force.cpp:89-106)
+                    T pi_ij = T(0);
+                    if (vr < T(0)) {
+                        const T alpha = T(0.5) * (al_i + r2j.x);
+                        const T bal = T(0.5) * (b_i + r2j.y);
+                        const T w = vr / r;
+                        const T vsig = c_i + c_j - T(3) * w;
+                        const T rho_ij_inv = T(2) / (rho_i + rho_j);
+                        pi_ij = T(-0.5) * bal * alpha * vsig * w * rho_ij_inv;
+                    }
+                    const T cfij = T(0.5) * (cfi + cfj);
+                    T ac = T(0);
+                    if (a.use_ac) {
+                        // Wadsley et al. (2008) / Price (2008) (src/fluid_force.cpp:108-116)
+                        const T vs = a.ac_gravity ? fabs(vr / r) : sqrt(T(2) * fabs(p_i - p_j) / (rho_i + rho_j));
+                        ac = alpha_ac * mj * vs * (u_i - r2j.z) * (cfij * r2) / r;
+                    }
+                    T ai, aj, de_p;
+                    if (TYPE == 0) {
+                        ai = mj * (X_i + T(0.5) * pi_ij);
+                        aj = mj * (X_j + T(0.5) * pi_ij);
+                        de_p = mj * X_i * cfi * vr;
+                    } else {
+                        const T u_j = r2j.z;
+                        const T f_ij = T(1) - X_i / (mj * u_j);
+                        const T f_ji = T(1) - X_j * mu_inv_i;
+                        const T t_i = g2u_per_p_i * u_j * f_ij;
+                        ai = mj * (t_i + T(0.5) * pi_ij);
+                        aj = mj * (g2u_i * r2j.w * f_ji + T(0.5) * pi_ij);
+                        de_p = mj * t_i * cfi * vr;
+                    }
+                    const T cacc = cfi * ai + cfj * aj;
+#pragma unroll
+                    for (int k = 0; k < D; ++k) acc[k].add(-rv[k] * cacc);
+                    dene.add(de_p + T(0.5) * mj * pi_ij * cfij * vr + ac);
+                }
+            }
+        }
+        if (active) {
+#pragma unroll
+            for (int k = 0; k < D; ++k) st.f[F_ACC + k][i] = (double)acc[k].get();
+            st.f[F_DENE][i] = (double)dene.get();
+        }
+    }
+}
+
+// Key-ordered T mirrors of the per-source fields of the force loop.
+template <int D, typename T, int TYPE>
+__global__ void fluid_mirror_kernel(State st, int n, typename Vec4<T>::type* rec0,
+                                    typename Vec4<T>::type* rec1, typename Vec4<T>::type* rec2,
+                                    T* grad, int gsph_2nd)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    typename Vec4<T>::type v;
+    v.x = (T)st.f[F_VEL][i];
+    v.y = D > 1 ? (T)st.f[F_VEL + (D > 1 ? 1 : 0)][i] : T(0);
+    v.z = D > 2 ? (T)st.f[F_VEL + (D > 2 ? 2 : 0)][i] : T(0);
+    v.w = (T)st.f[F_SML][i];
+    rec0[i] = v;
+    const double rho = st.f[F_DENS][i], p = st.f[F_PRES][i];
+    typename Vec4<T>::type b;
+    b.x = (T)rho;
+    b.y = (T)p;
+    b.z = (T)st.f[F_SOUND][i];
+    b.w = TYPE == 0 ? (T)(p / (rho * rho) * st.f[F_GRADH][i]) : TYPE == 1 ? (T)st.f[F_GRADH][i] : T(0);
+    rec1[i] = b;
+    typename Vec4<T>::type c;
+    c.x = (T)st.f[F_ALPHA][i];
+    c.y = (T)st.f[F_BALSARA][i];
+    c.z = (T)st.f[F_ENE][i];
+    c.w = TYPE == 1 ? (T)(st.f[F_ENE][i] / p) : T(0);
+    rec2[i] = c;
+    if (TYPE == 2 && gsph_2nd) {
+        T* g = grad + (size_t)i * 16;
+#pragma unroll
+        for (int q = 0; q < 16; ++q) g[q] = T(0);
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            g[k] = (T)st.f[F_GRADD + k][i];
+            g[3 + k] = (T)st.f[F_GRADP + k][i];
+#pragma unroll
+            for (int d = 0; d < D; ++d) g[6 + 3 * k + d] = (T)st.f[F_GRADV + 3 * k + d][i];
+        }
+    }
+}
+
+}  // namespace sphgpu
+
+// ---------------------------------------------------------------------------------------------
+// Launcher (host).
+namespace sphgpu {
+
+template <int D>
+constexpr int fluid_default_tile_cap() { return D == 1 ? 128 : D == 2 ? 512 : 1024; }
+
+template <int D, typename T, int TYPE, int K>
+void run_fluid(Ctx& c)
+{
+    using V4 = typename Vec4<T>::type;
+    auto kern = fluid_kernel<D, T, TYPE, K>;
+    cudaStream_t s = c.stream;
+    V4* rec0 = (V4*)c.mir[2];
+    V4* rec1 = (V4*)c.mir[3];
+    V4* rec2 = (V4*)c.mir[4];
+    T* grad = (T*)c.mir[5];
+    fluid_mirror_kernel<D, T, TYPE><<<ceil_div(c.n, 256), 256, 0, s>>>(c.st, c.n, rec0, rec1, rec2, grad, c.p.gsph_2nd_order);
+    reset_work_counters(c);
+    FluidArgs<T> a{};
+    a.st = c.st;
+    a.tv = tree_view(c);
+    a.pb = c.pb;
+    a.rec0 = rec0;
+    a.rec1 = rec1;
+    a.rec2 = rec2;
+    a.grad = grad;
+    a.gamma = c.p.gamma;
+    a.use_ac = c.p.use_ac;
+    a.ac_gravity = c.p.use_gravity;
+    a.alpha_ac = c.p.alpha_ac;
+    a.gsph_2nd = c.p.gsph_2nd_order;
+    a.dt_run = c.d_dt;
+    const int gt = c.group_threads;
+    const int tcap = c.tile_cap ? c.tile_cap : fluid_default_tile_cap<D>();
+    a.L = make_layout(gt, tcap, sizeof(V4), 256, 256);
+    a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 0, nullptr, nullptr,
+                       c.d_ovf_list, c.d_work + 1, c.d_err};
+    cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, max_optin_smem(c));
+    const int nb = std::max(1, kernel_occupancy((const void*)kern, gt, a.L.total));
+    kern<<<nb * c.num_sms, gt, a.L.total, s>>>(a);
+    const int big = big_tile_cap(c, gt, sizeof(V4), 1024, 2048);
+    a.L = make_layout(gt, big, sizeof(V4), 1024, 2048);
+    a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 2, c.d_ovf_list, c.d_work + 1,
+                       nullptr, nullptr, c.d_err};
+    kern<<<c.num_sms, gt, a.L.total, s>>>(a);
+}
+
+}  // namespace sphgpu

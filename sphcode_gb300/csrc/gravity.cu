@@ -1,0 +1,263 @@
+// GravityForce on the device: Barnes-Hut walk with kernel-softened particle pairs
+// (GravityForce::calculation, src/gravity_force.cpp:52-89; BHTree::tree_force and
+// BHNode::calc_force, src/bhtree.cpp:128-132,301-331; Hernquist & Katz (1989) softening f, g,
+// src/bhtree.cpp:273-299).
+//
+// A warp walks the octree for 32 key-consecutive targets at once.  Each stack entry carries the
+// lanes for which the node is still to be visited; every lane makes the reference's own opening
+// decision for its particle (edge^2 > theta^2 |x_i - com|^2, in FP64 with the reference's
+// rounding), so each particle interacts with exactly the node set of the reference's recursive
+// walk: lanes that do not open a node take its monopole, lanes that open a leaf take its
+// particles one by one (self term included in the potential, like the reference), lanes that
+// open an inner node continue with its children.  The roots carry zero mass, as in the
+// reference, whose root never receives its mass and centre (src/bhtree.cpp:57,152).
+//
+// FP32 pair form: leaf particles are stored as offsets from their leaf's centre in T, and each
+// lane forms x_i - centre once per leaf in FP64, so pair separations are T differences of
+// small numbers.  FP64 form: separations use the reference's periodic FP64 arithmetic.
+#include "context.cuh"
+
+namespace sphgpu {
+
+namespace {
+
+template <typename T>
+struct GravArgs {
+    using V4 = typename Vec4<T>::type;
+    State st;
+    TreeView tv;
+    Periodic pb;
+    GroupWork work;
+    const V4* grel;   // {x_j - centre of j's leaf (T), m_j}
+    const T* gh;      // h_j
+    double G;
+    double theta2;
+    int stack_cap;
+};
+
+// Softened potential and force kernels (src/bhtree.cpp:273-299).
+template <typename T>
+__device__ __forceinline__ T hk_f(T r, T h)
+{
+    const T e = h * T(0.5);
+    const T u = r / e;
+    if (u < T(1)) {
+        return (T(-0.5) * u * u * (T(1.0 / 3.0) - T(3.0 / 20) * u * u + u * u * u / T(20)) + T(1.4)) / e;
+    } else if (u < T(2)) {
+        return T(-1) / (T(15) * r) + (-u * u * (T(4.0 / 3.0) - u + T(0.3) * u * u - u * u * u / T(30)) + T(1.6)) / e;
+    }
+    return T(1) / r;
+}
+
+template <typename T>
+__device__ __forceinline__ T hk_g(T r, T h)
+{
+    const T e = h * T(0.5);
+    const T u = r / e;
+    if (u < T(1)) {
+        return (T(4.0 / 3.0) - T(1.2) * u * u + T(0.5) * u * u * u) / (e * e * e);
+    } else if (u < T(2)) {
+        const T u3 = u * u * u;
+        return (T(-1.0 / 15) + T(8.0 / 3) * u3 - T(3) * u3 * u + T(1.2) * u3 * u * u - u3 * u3 / T(6.0)) / (r * r * r);
+    }
+    return T(1) / (r * r * r);
+}
+
+template <int D, typename T>
+__global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
+{
+    using V4 = typename Vec4<T>::type;
+    extern __shared__ __align__(16) int2 gstack[];
+    __shared__ int s_group;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int2* stack = gstack + (size_t)w * a.stack_cap;
+    const State& st = a.st;
+    const TreeView& tv = a.tv;
+    const T G = (T)a.G;
+    constexpr bool exact_pairs = sizeof(T) == 8;
+
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const int k = atomicAdd(a.work.counter, 1);
+            s_group = k < *a.work.n_groups ? k : -1;
+        }
+        __syncthreads();
+        const int g = s_group;
+        if (g < 0) break;
+        const int gb = a.work.g_begin[g], gn = a.work.g_count[g];
+        if (w * 32 >= gn) continue;
+        const int t = w * 32 + lane;
+        const bool active = t < gn;
+        const int i = gb + (active ? t : 0);
+        double xi[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) xi[k] = st.f[F_POS + k][i];
+        const double hi = st.f[F_SML][i];
+        const T hiT = (T)hi;
+        Sum<T> phi, acc[D];
+        phi.zero();
+#pragma unroll
+        for (int k = 0; k < D; ++k) acc[k].zero();
+
+        const unsigned amask = __ballot_sync(FULL, active);
+        if (lane == 0) stack[0] = make_int2(st.run[gb], (int)amask);
+        int sp = 1;
+        bool overflow = false;
+        __syncwarp();
+        while (sp > 0) {
+            const int2 e = stack[sp - 1];
+            --sp;
+            __syncwarp();
+            const int node = e.x;
+            const unsigned m = (unsigned)e.y;
+            const bool in = (m >> lane) & 1u;
+            bool open = false;
+            if (in) {
+                double d[D];
+#pragma unroll
+                for (int k = 0; k < D; ++k) d[k] = ref_axis(xi[k], tv.com[k][node], a.pb, k);
+                double d2 = __dmul_rn(d[0], d[0]);
+#pragma unroll
+                for (int k = 1; k < D; ++k) d2 = __dadd_rn(d2, __dmul_rn(d[k], d[k]));
+                const double edge = tv.edge[node];
+                open = __dmul_rn(edge, edge) > __dmul_rn(a.theta2, d2);
+                if (!open) {
+                    const double M = tv.mass[node];
+                    if (M != 0.0) {
+                        // monopole: phi -= G M / r, acc -= d G M / r^3 (src/bhtree.cpp:327-329)
+                        T dT[D];
+                        T r2 = T(0);
+#pragma unroll
+                        for (int k = 0; k < D; ++k) { dT[k] = (T)d[k]; r2 += dT[k] * dT[k]; }
+                        const T r_inv = T(1) / sqrt(r2);
+                        const T gmr = G * (T)M * r_inv;
+                        phi.add(-gmr);
+                        const T c = gmr * r_inv * r_inv;
+#pragma unroll
+                        for (int k = 0; k < D; ++k) acc[k].add(-dT[k] * c);
+                    }
+                }
+            }
+            const unsigned om = __ballot_sync(FULL, open);
+            if (!om) continue;
+            const int fc = tv.first_child[node];
+            if (fc < 0) {
+                if (open) {
+                    const int b = tv.begin[node], cnt = tv.count[node];
+                    T base[D];
+                    if (!exact_pairs) {
+#pragma unroll
+                        for (int k = 0; k < D; ++k) base[k] = (T)min_image(xi[k] - tv.center[k][node], a.pb, k);
+                    }
+                    for (int j = b; j < b + cnt; ++j) {
+                        T rv[D], mj, hj;
+                        if (exact_pairs) {
+#pragma unroll
+                            for (int k = 0; k < D; ++k) rv[k] = (T)ref_axis(xi[k], st.f[F_POS + k][j], a.pb, k);
+                            mj = (T)st.f[F_MASS][j];
+                            hj = (T)st.f[F_SML][j];
+                        } else {
+                            const V4 q = a.grel[j];
+                            rv[0] = base[0] - q.x;
+                            if (D > 1) rv[D > 1 ? 1 : 0] = base[D > 1 ? 1 : 0] - q.y;
+                            if (D > 2) rv[D > 2 ? 2 : 0] = base[D > 2 ? 2 : 0] - q.z;
+                            mj = q.w;
+                            hj = a.gh[j];
+                        }
+                        T r2 = rv[0] * rv[0];
+#pragma unroll
+                        for (int k = 1; k < D; ++k) r2 += rv[k] * rv[k];
+                        const T r = sqrt(r2);
+                        const T gm = G * mj * T(0.5);
+                        phi.add(-gm * (hk_f(r, hiT) + hk_f(r, hj)));
+                        const T c = gm * (hk_g(r, hiT) + hk_g(r, hj));
+#pragma unroll
+                        for (int k = 0; k < D; ++k) acc[k].add(-rv[k] * c);
+                    }
+                }
+            } else {
+                const int nc = tv.nchild[node];
+                if (sp + nc > a.stack_cap) { overflow = true; break; }
+                if (lane < nc) stack[sp + nc - 1 - lane] = make_int2(fc + lane, (int)om);
+                sp += nc;
+                __syncwarp();
+            }
+        }
+        if (overflow) {
+            if (lane == 0) atomicOr(a.work.err, (unsigned)ERR_GSTACK);
+            continue;
+        }
+        if (active) {
+#pragma unroll
+            for (int k = 0; k < D; ++k) st.f[F_ACC + k][i] += (double)acc[k].get();
+            st.f[F_PHI][i] = (double)phi.get();
+        }
+    }
+}
+
+// Leaf-relative offsets and softening lengths of every particle, in T.
+template <int D, typename T>
+__global__ void gravity_mirror_kernel(State st, const int* node_total_p, TreeView tv,
+                                      typename Vec4<T>::type* grel, T* gh)
+{
+    const int total = *node_total_p;
+    for (int nd = blockIdx.x * blockDim.x + threadIdx.x; nd < total; nd += gridDim.x * blockDim.x) {
+        if (tv.first_child[nd] >= 0) continue;
+        const int b = tv.begin[nd], e = b + tv.count[nd];
+        double c[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) c[k] = tv.center[k][nd];
+        for (int j = b; j < e; ++j) {
+            typename Vec4<T>::type q;
+            q.x = (T)(st.f[F_POS][j] - c[0]);
+            q.y = D > 1 ? (T)(st.f[F_POS + (D > 1 ? 1 : 0)][j] - c[D > 1 ? 1 : 0]) : T(0);
+            q.z = D > 2 ? (T)(st.f[F_POS + (D > 2 ? 2 : 0)][j] - c[D > 2 ? 2 : 0]) : T(0);
+            q.w = (T)st.f[F_MASS][j];
+            grel[j] = q;
+            gh[j] = (T)st.f[F_SML][j];
+        }
+    }
+}
+
+template <int D, typename T>
+void run_gravity(Ctx& c)
+{
+    using V4 = typename Vec4<T>::type;
+    cudaStream_t s = c.stream;
+    V4* grel = (V4*)c.mir[6];
+    T* gh = (T*)c.mir[7];
+    TreeView tv = tree_view(c);
+    if (sizeof(T) == 4)
+        gravity_mirror_kernel<D, T><<<c.num_sms * 8, 256, 0, s>>>(c.st, c.node_total, tv, grel, gh);
+    reset_work_counters(c);
+    GravArgs<T> a{};
+    a.st = c.st;
+    a.tv = tv;
+    a.pb = c.pb;
+    a.grel = grel;
+    a.gh = gh;
+    a.G = c.p.g_constant;
+    a.theta2 = c.p.theta * c.p.theta;
+    a.stack_cap = 1024;
+    a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 0, nullptr, nullptr, nullptr,
+                       nullptr, c.d_err};
+    const int gt = c.group_threads;
+    const size_t smem = sizeof(int2) * (size_t)a.stack_cap * (gt / 32);
+    auto kern = gravity_kernel<D, T>;
+    cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int nb = std::max(1, kernel_occupancy((const void*)kern, gt, smem));
+    kern<<<nb * c.num_sms, gt, smem, s>>>(a);
+}
+
+}  // namespace
+
+void launch_gravity(Ctx& c)
+{
+    const bool f32 = c.precision == SPHGPU_FP32_PAIR;
+    if (c.dim == 1) { if (f32) run_gravity<1, float>(c); else run_gravity<1, double>(c); }
+    else if (c.dim == 2) { if (f32) run_gravity<2, float>(c); else run_gravity<2, double>(c); }
+    else { if (f32) run_gravity<3, float>(c); else run_gravity<3, double>(c); }
+}
+
+}  // namespace sphgpu

@@ -1,0 +1,213 @@
+// Streaming FP64 kernels: TimeStep (src/timestep.cpp:18-38), Solver::predict / correct
+// (src/solver.cpp:431-474), the start-up field values (src/solver.cpp:392-404),
+// Simulation::update_time (src/simulation.cpp:32-35) and the energy/momentum sums
+// (src/output.cpp:66-90).  All per-run: in a batch each run has its own dt and time.
+#include "context.cuh"
+
+namespace sphgpu {
+
+namespace {
+
+constexpr int THREADS = 256;
+
+// dt_force_i = cflForce * sqrt(h_i / |a_i|) for |a_i| > 0, minimum per run.
+template <int D>
+__global__ void timestep_min_kernel(State st, int n, double cfl_force, long long* dtmin)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v = 1.7976931348623157e308;
+    int r = -1;
+    if (i < n) {
+        r = st.run[i];
+        double a2 = 0.0;
+#pragma unroll
+        for (int k = 0; k < D; ++k) { const double a = st.f[F_ACC + k][i]; a2 += a * a; }
+        const double a = sqrt(a2);
+        if (a > 0.0) v = cfl_force * sqrt(st.f[F_SML][i] / a);
+    }
+    const unsigned same = __match_any_sync(FULL, r);
+    if (same == FULL) {
+        for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(FULL, v, o));
+        if ((threadIdx.x & 31) == 0 && r >= 0) atomicMin(&dtmin[r], dbl_to_ord(v));
+    } else if (r >= 0) {
+        atomicMin(&dtmin[r], dbl_to_ord(v));
+    }
+}
+
+// dt = min(cflSound * h_per_v_sig, dt_force); resets the minimum for the next call.
+__global__ void timestep_final_kernel(int R, double cfl_sound, const long long* hvs,
+                                      long long* dtmin, double* dt)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    const double ds = cfl_sound * ord_to_dbl(hvs[r]);
+    const double df = ord_to_dbl(dtmin[r]);
+    dt[r] = ds < df ? ds : df;
+    dtmin[r] = dbl_to_ord(1.7976931348623157e308);
+}
+
+template <int D>
+__global__ void predict_kernel(State st, int n, const double* dt_run, double c_sound, Periodic pb)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double dt = dt_run[st.run[i]];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        const double v = st.f[F_VEL + k][i], a = st.f[F_ACC + k][i];
+        const double vp = v + a * (0.5 * dt);
+        st.f[F_VELP + k][i] = vp;
+        double x = st.f[F_POS + k][i] + vp * dt;
+        if (pb.on) {
+            if (x < pb.lo[k]) x += pb.len[k];
+            else if (x > pb.hi[k]) x -= pb.len[k];
+        }
+        st.f[F_POS + k][i] = x;
+        st.f[F_VEL + k][i] = v + a * dt;
+    }
+    const double u = st.f[F_ENE][i], du = st.f[F_DENE][i];
+    st.f[F_ENEP][i] = u + du * (0.5 * dt);
+    const double un = u + du * dt;
+    st.f[F_ENE][i] = un;
+    st.f[F_SOUND][i] = sqrt(c_sound * un);
+}
+
+template <int D>
+__global__ void correct_kernel(State st, int n, const double* dt_run, double c_sound)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double dt = dt_run[st.run[i]];
+#pragma unroll
+    for (int k = 0; k < D; ++k)
+        st.f[F_VEL + k][i] = st.f[F_VELP + k][i] + st.f[F_ACC + k][i] * (0.5 * dt);
+    const double u = st.f[F_ENEP][i] + st.f[F_DENE][i] * (0.5 * dt);
+    st.f[F_ENE][i] = u;
+    st.f[F_SOUND][i] = sqrt(c_sound * u);
+}
+
+__global__ void init_fields_kernel(State st, int n, double alpha, double c_sound)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    st.f[F_ALPHA][i] = alpha;
+    st.f[F_BALSARA][i] = 1.0;
+    st.f[F_SOUND][i] = sqrt(c_sound * st.f[F_ENE][i]);
+}
+
+__global__ void update_time_kernel(int R, double* time, const double* dt)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < R) time[r] += dt[r];
+}
+
+// Energy and momentum of every run: one block per (run, chunk) slice writes partial sums, a
+// second pass adds the partials of a run in a fixed order (deterministic).
+constexpr int ESUM = 7;   // kinetic, thermal, potential, (unused), p_x, p_y, p_z
+constexpr int ECHUNK = 8192;
+
+template <int D>
+__global__ void energy_partial_kernel(State st, const int* run_begin, int R, int chunks_per_run_max,
+                                      double* partial)
+{
+    const int r = blockIdx.y;
+    const int b0 = run_begin[r], e0 = run_begin[r + 1];
+    const int chunk = blockIdx.x;
+    const int b = b0 + chunk * ECHUNK, e = min(e0, b + ECHUNK);
+    double s[ESUM] = {0, 0, 0, 0, 0, 0, 0};
+    for (int i = b + threadIdx.x; i < e; i += blockDim.x) {
+        const double m = st.f[F_MASS][i];
+        double v2 = 0.0;
+#pragma unroll
+        for (int k = 0; k < D; ++k) { const double v = st.f[F_VEL + k][i]; v2 += v * v; s[4 + k] += m * v; }
+        s[0] += 0.5 * m * v2;
+        s[1] += m * st.f[F_ENE][i];
+        s[2] += 0.5 * m * st.f[F_PHI][i];
+    }
+    __shared__ double red[ESUM][THREADS / 32];
+#pragma unroll
+    for (int q = 0; q < ESUM; ++q) {
+        double v = s[q];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+        if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < ESUM) {
+        double v = 0.0;
+        for (int w = 0; w < THREADS / 32; ++w) v += red[threadIdx.x][w];
+        partial[((size_t)r * chunks_per_run_max + chunk) * ESUM + threadIdx.x] = v;
+    }
+}
+
+__global__ void energy_final_kernel(const int* run_begin, int R, int chunks_per_run_max,
+                                    const double* partial, double* out)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    const int nch = (run_begin[r + 1] - run_begin[r] + ECHUNK - 1) / ECHUNK;
+    double s[ESUM] = {0, 0, 0, 0, 0, 0, 0};
+    for (int c = 0; c < nch; ++c)
+        for (int q = 0; q < ESUM; ++q) s[q] += partial[((size_t)r * chunks_per_run_max + c) * ESUM + q];
+    out[r * ESUM + 0] = s[0];
+    out[r * ESUM + 1] = s[1];
+    out[r * ESUM + 2] = s[2];
+    out[r * ESUM + 3] = s[0] + s[1] + s[2];
+    out[r * ESUM + 4] = s[4];
+    out[r * ESUM + 5] = s[5];
+    out[r * ESUM + 6] = s[6];
+}
+
+}  // namespace
+
+void launch_timestep(Ctx& c)
+{
+    const int g = ceil_div(c.n, THREADS);
+    if (c.dim == 1) timestep_min_kernel<1><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.p.cfl_force, c.d_dtmin);
+    else if (c.dim == 2) timestep_min_kernel<2><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.p.cfl_force, c.d_dtmin);
+    else timestep_min_kernel<3><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.p.cfl_force, c.d_dtmin);
+    timestep_final_kernel<<<ceil_div(c.R, 128), 128, 0, c.stream>>>(c.R, c.p.cfl_sound, c.d_hvs, c.d_dtmin, c.d_dt);
+}
+
+void launch_predict(Ctx& c)
+{
+    const int g = ceil_div(c.n, THREADS);
+    const double cs = c.p.gamma * (c.p.gamma - 1.0);
+    if (c.dim == 1) predict_kernel<1><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.d_dt, cs, c.pb);
+    else if (c.dim == 2) predict_kernel<2><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.d_dt, cs, c.pb);
+    else predict_kernel<3><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.d_dt, cs, c.pb);
+}
+
+void launch_correct(Ctx& c)
+{
+    const int g = ceil_div(c.n, THREADS);
+    const double cs = c.p.gamma * (c.p.gamma - 1.0);
+    if (c.dim == 1) correct_kernel<1><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.d_dt, cs);
+    else if (c.dim == 2) correct_kernel<2><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.d_dt, cs);
+    else correct_kernel<3><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.d_dt, cs);
+}
+
+void launch_init_fields(Ctx& c)
+{
+    init_fields_kernel<<<ceil_div(c.n, THREADS), THREADS, 0, c.stream>>>(
+        c.st, c.n, c.p.av_alpha, c.p.gamma * (c.p.gamma - 1.0));
+}
+
+void launch_update_time(Ctx& c)
+{
+    update_time_kernel<<<ceil_div(c.R, 128), 128, 0, c.stream>>>(c.R, c.d_time, c.d_dt);
+}
+
+void launch_energy(Ctx& c, double* d_out)
+{
+    int maxc = 1;
+    for (int r = 0; r < c.R; ++r) maxc = std::max(maxc, ceil_div(c.run_begin[r + 1] - c.run_begin[r], ECHUNK));
+    dim3 grid(maxc, c.R);
+    // partial buffer: reuse the stage buffer (sized at create for >= R * maxc * ESUM doubles)
+    double* partial = c.d_sums;
+    if (c.dim == 1) energy_partial_kernel<1><<<grid, THREADS, 0, c.stream>>>(c.st, c.d_run_begin, c.R, maxc, partial);
+    else if (c.dim == 2) energy_partial_kernel<2><<<grid, THREADS, 0, c.stream>>>(c.st, c.d_run_begin, c.R, maxc, partial);
+    else energy_partial_kernel<3><<<grid, THREADS, 0, c.stream>>>(c.st, c.d_run_begin, c.R, maxc, partial);
+    energy_final_kernel<<<ceil_div(c.R, 128), 128, 0, c.stream>>>(c.d_run_begin, c.R, maxc, partial, d_out);
+}
+
+}  // namespace sphgpu

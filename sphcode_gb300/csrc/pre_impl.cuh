@@ -1,0 +1,466 @@
+// PreInteraction on the device: smoothing length by Newton iteration, density, pressure, grad-h
+// term, signal velocity, Balsara switch and time-dependent viscosity (ssph:
+// src/pre_interaction.cpp:39-169,227-283; disph: src/disph/d_pre_interaction.cpp:21-230) or the
+// MUSCL gradients (gsph: src/gsph/g_pre_interaction.cpp:27-144), and the first-call
+// initial_smoothing (src/pre_interaction.cpp:171-215).
+//
+// One CTA per target group (group.cuh).  The candidate set of a target is the reference's:
+// {j : r_ij^2 < h_s^2} with h_s = 1.2 h_guess (the search radius of src/pre_interaction.cpp:64,70),
+// decided exactly.  Newton iterations and the density loop run over the candidate bitmask with
+// the pair terms in T; the reference's `r >= h -> break` over the distance-sorted list is the
+// set {r < h}; at the final h that set is decided exactly (it defines the neighbour count).
+// The Newton update and its convergence test |dh| < 1e-4 (h + h_prev) are FP64.
+#pragma once
+
+#include "context.cuh"
+#include "group.cuh"
+
+namespace sphgpu {
+
+template <typename T>
+struct PreArgs {
+    State st;
+    TreeView tv;
+    Periodic pb;
+    SmemLayout L;
+    GroupWork work;
+    const typename Vec4<T>::type* mvel;   // {vx, vy, vz, c}
+    const T* mu;                          // u
+    int nn;
+    double ratio;
+    double gamma;
+    int iterative;
+    int initial;
+    int use_balsara, use_tdav;
+    int gsph_2nd;
+    double alpha_min, alpha_max, eps_av;
+    const double* dt_run;
+    long long* hvs;
+    int* newton_fail;
+};
+
+template <int D>
+__device__ __forceinline__ double h_guess(double nn, double m, double rho)
+{
+    const double x = nn * m / (rho * volume_const<D>());
+    if (D == 1) return x;
+    if (D == 2) return sqrt(x);          // = pow(x, 0.5), both correctly rounded
+    return pow(x, 1.0 / 3.0);
+}
+
+template <int D, typename T, int TYPE, int K>
+__global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
+{
+    using V4 = typename Vec4<T>::type;
+    using KF = Kern<D, K, T>;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const SmemLayout L = a.L;
+    GroupMisc* gm = reinterpret_cast<GroupMisc*>(smem + L.off_misc);
+    const Tile<T> tile = tile_of<T>(smem, L);
+    const State& st = a.st;
+    const int t = threadIdx.x;
+    const int GT = blockDim.x;
+    constexpr double A = volume_const<D>();
+
+    for (;;) {
+        const int g = next_group(gm, a.work);
+        if (g < 0) break;
+        const int gb = a.work.g_begin[g], gn = a.work.g_count[g];
+        const bool active = t < gn;
+        const int i = gb + (active ? t : 0);
+        double xi[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) xi[k] = st.f[F_POS + k][i];
+        const double mi = st.f[F_MASS][i];
+        const double hg = h_guess<D>((double)a.nn, mi, st.f[F_DENS][i]);
+        const double hs = a.initial ? hg : hg * a.ratio;
+        group_box<D>(gm, xi, active, hs, a.pb);
+        const int run = st.run[gb];
+        if (!group_walk<D>(smem, L, gm, a.tv, run, false, a.pb)) { report_overflow(a.work, g); continue; }
+        {
+            const double R = gm->R;
+            double lim[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) lim[k] = (gm->he[k] + R) * (1.0 + 1e-12);
+            const int ntile = stage_sources<D, T>(smem, L, gm, st, a.pb, tile, [&](int, const double* off) {
+#pragma unroll
+                for (int k = 0; k < D; ++k)
+                    if (fabs(off[k]) > lim[k]) return false;
+                return true;
+            }, [&](int j) { return (T)st.f[F_MASS][j]; });
+            if (ntile < 0) { report_overflow(a.work, g); continue; }
+            gm->ntile = ntile;   // every thread writes the same value
+        }
+        const int ntile = gm->ntile;
+        const int nw = (ntile + 31) >> 5;
+        T xo[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) xo[k] = (T)min_image(xi[k] - gm->gc[k], a.pb, k);
+
+        // ---- candidates: r^2 < h_s^2, exactly (src/bhtree.cpp:256) ----
+        {
+            const double hs2 = __dmul_rn(hs, hs);
+            const double band = r2_band<T, D>(gm, hs);
+            const T lo_t = to_T_down<T>(hs2 - band), hi_t = to_T_up<T>(hs2 + band);
+            for (int w = 0; w < nw; ++w) {
+                unsigned bits = 0;
+                const int smax = min(32, ntile - w * 32);
+                for (int b = 0; b < smax; ++b) {
+                    const int s = w * 32 + b;
+                    T r[D];
+                    const T r2 = tile_r2<D, T>(xo, tile.pm[s], r);
+                    bool in = r2 < lo_t;
+                    if (!in && r2 <= hi_t) in = exact_r2<D>(st, xi, tile.idx[s], a.pb) < hs2;
+                    if (in) bits |= 1u << b;
+                }
+                tile.mask[w * GT + t] = active ? bits : 0u;
+            }
+        }
+
+        // ---- smoothing length: Newton-Raphson on rho h^D = b (or n h^D = b for disph) ----
+        double h = hg;
+        if (!a.initial && a.iterative) {
+            const double bconst = (TYPE == 1) ? a.nn / A : mi * a.nn / A;
+            bool done = !active, conv = false;
+            for (int it = 0; it < 10; ++it) {
+                if (!__any_sync(FULL, !done)) break;
+                if (!done) {
+                    const T hT = (T)h;
+                    Sum<T> s0, s1;
+                    s0.zero();
+                    s1.zero();
+                    for (int w = 0; w < nw; ++w) {
+                        unsigned bits = tile.mask[w * GT + t];
+                        while (bits) {
+                            const int b = __ffs(bits) - 1;
+                            bits &= bits - 1;
+                            const V4 p = tile.pm[w * 32 + b];
+                            T r[D];
+                            const T rr = sqrt(tile_r2<D, T>(xo, p, r));
+                            if (rr < hT) {
+                                const T W = KF::w(rr, hT), dW = KF::dhw(rr, hT);
+                                if (TYPE == 1) { s0.add(W); s1.add(dW); }
+                                else { s0.add(p.w * W); s1.add(p.w * dW); }
+                            }
+                        }
+                    }
+                    const double dens = (double)s0.get(), ddens = (double)s1.get();
+                    const double hd = powD<D>(h);
+                    const double hd1 = D == 1 ? 1.0 : D == 2 ? h : h * h;
+                    const double f = dens * hd - bconst;
+                    const double df = ddens * hd + D * dens * hd1;
+                    const double hn = h - f / df;
+                    if (fabs(hn - h) < (hn + h) * 1e-4) { done = true; conv = true; }
+                    h = hn;
+                }
+            }
+            if (active && !conv) {
+                h = hg;   // PreInteraction::newton_raphson falls back to the unscaled guess
+                atomicAdd(a.newton_fail, 1);
+            }
+        }
+        const double hf = a.initial ? hg : (a.iterative ? h : hs);
+
+        // ---- density, pressure, grad-h, signal velocity over {r < h} ----
+        const T hT = (T)hf;
+        const double ci = st.f[F_SOUND][i];
+        const double ui = st.f[F_ENE][i];
+        T vi[3] = {T(0), T(0), T(0)};
+#pragma unroll
+        for (int k = 0; k < D; ++k) vi[k] = (T)st.f[F_VEL + k][i];
+        Sum<T> sd, sdh, sn, sp, sdp, sdn;
+        sd.zero(); sdh.zero(); sn.zero(); sp.zero(); sdp.zero(); sdn.zero();
+        T vsig = (T)(ci * 2.0);
+        int nnb = 0;
+        {
+            const double hf2 = __dmul_rn(hf, hf);
+            const double band = r2_band<T, D>(gm, hf);
+            const T lo_t = to_T_down<T>(hf2 - band), hi_t = to_T_up<T>(hf2 + band);
+            const T ciT = (T)ci;
+            for (int w = 0; w < nw; ++w) {
+                const unsigned bits0 = tile.mask[w * GT + t];
+                unsigned bits = bits0, keep = 0;
+                while (bits) {
+                    const int b = __ffs(bits) - 1;
+                    bits &= bits - 1;
+                    const int s = w * 32 + b;
+                    const V4 p = tile.pm[s];
+                    T r[D];
+                    const T r2 = tile_r2<D, T>(xo, p, r);
+                    bool in = r2 < lo_t;
+                    if (!in && r2 <= hi_t) in = __dsqrt_rn(exact_r2<D>(st, xi, tile.idx[s], a.pb)) < hf;
+                    if (!in) continue;
+                    keep |= 1u << b;
+                    ++nnb;
+                    const int j = tile.idx[s];
+                    const T rr = sqrt(r2);
+                    const T W = KF::w(rr, hT);
+                    sd.add(p.w * W);
+                    if (TYPE == 0) {
+                        if (!a.initial) sdh.add(p.w * KF::dhw(rr, hT));
+                    } else if (TYPE == 1) {
+                        if (!a.initial) {
+                            const T dW = KF::dhw(rr, hT);
+                            const T muj = p.w * a.mu[j];
+                            sn.add(W);
+                            sp.add(muj * W);
+                            sdp.add(muj * dW);
+                            sdn.add(dW);
+                        }
+                    }
+                    if (!a.initial && j != i) {
+                        const V4 vj = a.mvel[j];
+                        T rv = r[0] * (vi[0] - vj.x);
+                        if (D > 1) rv += r[D > 1 ? 1 : 0] * (vi[1] - vj.y);
+                        if (D > 2) rv += r[D > 2 ? 2 : 0] * (vi[2] - vj.z);
+                        const T vs = ciT + vj.w - T(3) * rv / rr;
+                        vsig = vs > vsig ? vs : vsig;
+                    }
+                }
+                tile.mask[w * GT + t] = active ? keep : 0u;
+            }
+        }
+        if (a.initial) {
+            if (active) {
+                st.f[F_SML][i] = hf;
+                st.f[F_DENS][i] = (double)sd.get();
+            }
+            continue;
+        }
+        const double dens = (double)sd.get();
+        double pres, gradh = 0.0;
+        if (TYPE == 0) {
+            pres = (a.gamma - 1.0) * dens * ui;
+            gradh = 1.0 / (1.0 + hf / (D * dens) * (double)sdh.get());
+        } else if (TYPE == 1) {
+            const double n_i = (double)sn.get();
+            pres = (a.gamma - 1.0) * (double)sp.get();
+            gradh = hf / (D * n_i) * (double)sdp.get() / (1.0 + hf / (D * n_i) * (double)sdn.get());
+        } else {
+            pres = (a.gamma - 1.0) * dens * ui;
+        }
+        // h / v_sig minimum of the group -> run minimum (TimeStep input)
+        {
+            double hv = active ? hf / (double)vsig : 1.7976931348623157e308;
+            for (int o = 16; o > 0; o >>= 1) hv = fmin(hv, __shfl_xor_sync(FULL, hv, o));
+            if ((t & 31) == 0) atomicMin(&a.hvs[run], dbl_to_ord(hv));
+        }
+
+        if (TYPE == 2) {
+            // ---- MUSCL gradients (src/gsph/g_pre_interaction.cpp:112-136) ----
+            if (active) {
+                st.f[F_SML][i] = hf;
+                st.f[F_DENS][i] = dens;
+                st.f[F_PRES][i] = pres;
+                st.neighbor[i] = nnb;
+            }
+            if (!a.gsph_2nd) continue;
+            Sum<T> dd[D], du[D], dv[D][D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+                dd[k].zero(); du[k].zero();
+#pragma unroll
+                for (int q = 0; q < D; ++q) dv[k][q].zero();
+            }
+            const T uiT = (T)ui;
+            for (int w = 0; w < nw; ++w) {
+                unsigned bits = tile.mask[w * GT + t];
+                while (bits) {
+                    const int b = __ffs(bits) - 1;
+                    bits &= bits - 1;
+                    const int s = w * 32 + b;
+                    const V4 p = tile.pm[s];
+                    const int j = tile.idx[s];
+                    T r[D];
+                    const T rr = sqrt(tile_r2<D, T>(xo, p, r));
+                    const T cf = KF::dw_coef(rr, hT);
+                    const V4 vj = a.mvel[j];
+                    const T vjv[3] = {vj.x, vj.y, vj.z};
+                    const T mdu = p.w * (a.mu[j] - uiT);
+#pragma unroll
+                    for (int k = 0; k < D; ++k) {
+                        const T dw = r[k] * cf;
+                        dd[k].add(dw * p.w);
+                        du[k].add(dw * mdu);
+                    }
+#pragma unroll
+                    for (int q = 0; q < D; ++q) {
+                        const T mv = p.w * (vjv[q] - vi[q]);
+#pragma unroll
+                        for (int k = 0; k < D; ++k) dv[q][k].add(r[k] * cf * mv);
+                    }
+                }
+            }
+            if (active) {
+                const double rho_inv = 1.0 / dens;
+#pragma unroll
+                for (int k = 0; k < D; ++k) {
+                    const double ddk = (double)dd[k].get();
+                    st.f[F_GRADD + k][i] = ddk;
+                    st.f[F_GRADP + k][i] = (ddk * ui + (double)du[k].get()) * (a.gamma - 1.0);
+                }
+#pragma unroll
+                for (int q = 0; q < D; ++q)
+#pragma unroll
+                    for (int k = 0; k < D; ++k) st.f[F_GRADV + q * 3 + k][i] = (double)dv[q][k].get() * rho_inv;
+            }
+            continue;
+        }
+
+        // ---- Balsara switch and time-dependent alpha (src/pre_interaction.cpp:115-161) ----
+        double alpha = st.f[F_ALPHA][i];
+        double balsara = st.f[F_BALSARA][i];
+        const double dt = a.dt_run[run];
+        const bool bal = a.use_balsara && D != 1;
+        if (bal || a.use_tdav) {
+            Sum<T> sdiv, srot[3];
+            sdiv.zero(); srot[0].zero(); srot[1].zero(); srot[2].zero();
+            for (int w = 0; w < nw; ++w) {
+                unsigned bits = tile.mask[w * GT + t];
+                while (bits) {
+                    const int b = __ffs(bits) - 1;
+                    bits &= bits - 1;
+                    const int s = w * 32 + b;
+                    const V4 p = tile.pm[s];
+                    const int j = tile.idx[s];
+                    T r[D];
+                    const T rr = sqrt(tile_r2<D, T>(xo, p, r));
+                    const T cf = KF::dw_coef(rr, hT);
+                    const V4 vj = a.mvel[j];
+                    const T wj = (TYPE == 1) ? p.w * a.mu[j] : p.w;
+                    T dw[3] = {T(0), T(0), T(0)}, vij[3] = {T(0), T(0), T(0)};
+#pragma unroll
+                    for (int k = 0; k < D; ++k) dw[k] = r[k] * cf;
+                    vij[0] = vi[0] - vj.x;
+                    if (D > 1) vij[1] = vi[1] - vj.y;
+                    if (D > 2) vij[2] = vi[2] - vj.z;
+                    T vd = vij[0] * dw[0];
+                    if (D > 1) vd += vij[1] * dw[1];
+                    if (D > 2) vd += vij[2] * dw[2];
+                    sdiv.add(-wj * vd);
+                    if (bal) {
+                        if (D == 2) {
+                            srot[0].add((vij[0] * dw[1] - vij[1] * dw[0]) * wj);
+                        } else if (D == 3) {
+                            srot[0].add((vij[1] * dw[2] - vij[2] * dw[1]) * wj);
+                            srot[1].add((vij[2] * dw[0] - vij[0] * dw[2]) * wj);
+                            srot[2].add((vij[0] * dw[1] - vij[1] * dw[0]) * wj);
+                        }
+                    }
+                }
+            }
+            double div = (double)sdiv.get();
+            double rot[3] = {(double)srot[0].get(), (double)srot[1].get(), (double)srot[2].get()};
+            if (TYPE == 1) {
+                const double p_inv = (a.gamma - 1.0) / pres;
+                div *= p_inv;
+                for (int k = 0; k < 3; ++k) rot[k] *= p_inv;
+            } else {
+                div /= dens;
+                for (int k = 0; k < 3; ++k) rot[k] /= dens;
+            }
+            if (bal) {
+                const double rot_abs = D == 2 ? fabs(rot[0]) : sqrt(rot[0] * rot[0] + rot[1] * rot[1] + rot[2] * rot[2]);
+                balsara = fabs(div) / (fabs(div) + rot_abs + 1e-4 * ci / hf);
+                if (a.use_tdav) {
+                    const double tau_inv = a.eps_av * ci / hf;
+                    const double sdv = -div > 0.0 ? -div : 0.0;
+                    alpha += (-(alpha - a.alpha_min) * tau_inv + sdv * (a.alpha_max - alpha)) * dt;
+                }
+            } else {
+                const double tau_inv = a.eps_av * ci / hf;
+                const double s_i = -div > 0.0 ? -div : 0.0;
+                alpha = (alpha + dt * tau_inv * a.alpha_min + s_i * dt * a.alpha_max) / (1.0 + dt * tau_inv + s_i * dt);
+            }
+        }
+        if (active) {
+            st.f[F_SML][i] = hf;
+            st.f[F_DENS][i] = dens;
+            st.f[F_PRES][i] = pres;
+            st.f[F_GRADH][i] = gradh;
+            st.f[F_BALSARA][i] = balsara;
+            st.f[F_ALPHA][i] = alpha;
+            st.neighbor[i] = nnb;
+        }
+    }
+}
+
+// Key-ordered T mirrors of the source fields Pre reads per pair.
+template <int D, typename T>
+__global__ void pre_mirror_kernel(State st, int n, typename Vec4<T>::type* mvel, T* mu)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    typename Vec4<T>::type v;
+    v.x = (T)st.f[F_VEL][i];
+    v.y = D > 1 ? (T)st.f[F_VEL + (D > 1 ? 1 : 0)][i] : T(0);
+    v.z = D > 2 ? (T)st.f[F_VEL + (D > 2 ? 2 : 0)][i] : T(0);
+    v.w = (T)st.f[F_SOUND][i];
+    mvel[i] = v;
+    mu[i] = (T)st.f[F_ENE][i];
+}
+
+static __global__ void pre_reset_kernel(int R, long long* hvs, int* counters, int ncounters)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < R) hvs[r] = dbl_to_ord(1.7976931348623157e308);
+    if (r < ncounters) counters[r] = 0;
+}
+
+}  // namespace sphgpu
+
+// ---------------------------------------------------------------------------------------------
+// Launcher (host).
+namespace sphgpu {
+
+template <int D>
+constexpr int default_tile_cap() { return D == 1 ? 128 : D == 2 ? 512 : 1024; }
+
+template <int D, typename T, int TYPE, int K>
+void run_pre(Ctx& c, bool initial)
+{
+    using V4 = typename Vec4<T>::type;
+    auto kern = pre_kernel<D, T, TYPE, K>;
+    cudaStream_t s = c.stream;
+    pre_mirror_kernel<D, T><<<ceil_div(c.n, 256), 256, 0, s>>>(c.st, c.n, (V4*)c.mir[0], (T*)c.mir[1]);
+    // counters: [0] main work, [1] overflow count, [2] overflow work; plus h/v_sig and Newton
+    if (!initial) pre_reset_kernel<<<ceil_div(std::max(c.R, 4), 128), 128, 0, s>>>(c.R, c.d_hvs, c.d_work, 4);
+    else pre_reset_kernel<<<1, 32, 0, s>>>(0, c.d_hvs, c.d_work, 4);
+    cudaMemsetAsync(c.d_newton_fail, 0, sizeof(int), s);
+    PreArgs<T> a{};
+    a.st = c.st;
+    a.tv = tree_view(c);
+    a.pb = c.pb;
+    a.mvel = (const V4*)c.mir[0];
+    a.mu = (const T*)c.mir[1];
+    a.nn = c.p.neighbor_number;
+    a.ratio = c.p.iterative_sml ? 1.2 : 1.0;
+    a.gamma = c.p.gamma;
+    a.iterative = c.p.iterative_sml;
+    a.initial = initial ? 1 : 0;
+    a.use_balsara = c.p.use_balsara;
+    a.use_tdav = c.p.use_tdav;
+    a.gsph_2nd = c.p.gsph_2nd_order;
+    a.alpha_min = c.p.alpha_min;
+    a.alpha_max = c.p.alpha_max;
+    a.eps_av = c.p.epsilon_av;
+    a.dt_run = c.d_dt;
+    a.hvs = c.d_hvs;
+    a.newton_fail = c.d_newton_fail;
+    const int gt = c.group_threads;
+    const int tcap = c.tile_cap ? c.tile_cap : default_tile_cap<D>();
+    a.L = make_layout(gt, tcap, sizeof(V4), 256, 256);
+    a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 0, nullptr, nullptr,
+                       c.d_ovf_list, c.d_work + 1, c.d_err};
+    cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, max_optin_smem(c));
+    const int nb = std::max(1, kernel_occupancy((const void*)kern, gt, a.L.total));
+    kern<<<nb * c.num_sms, gt, a.L.total, s>>>(a);
+    // overflow pass: groups that did not fit, with the largest capacities
+    const int big = big_tile_cap(c, gt, sizeof(V4), 1024, 2048);
+    a.L = make_layout(gt, big, sizeof(V4), 1024, 2048);
+    a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 2, c.d_ovf_list, c.d_work + 1,
+                       nullptr, nullptr, c.d_err};
+    kern<<<c.num_sms, gt, a.L.total, s>>>(a);
+}
+
+}  // namespace sphgpu

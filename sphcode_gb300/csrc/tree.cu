@@ -1,0 +1,731 @@
+// Octree construction on the device (replaces BHTree::make / create_tree / assign,
+// src/bhtree.cpp:55-107,136-204, and BHTree::set_kernel, :109-112,206-232).
+//
+// The reference splits a node at its geometric center with `pos > center` per axis and builds
+// children's centers as center +/- edge/4 (src/bhtree.cpp:170-175,190-196).  Every particle's
+// path through that recursion is its key: per level, the D comparison bits against the FP64
+// center sequence the reference would compute.  Sorting by those keys (radix sort) puts each
+// node's particles in one contiguous range, so nodes are built level by level as ranges, with
+// the reference's split rule (num > leafParticleNumber and level <= maxTreeLevel; the root always
+// splits) and its node-pool capacity of 5 N.  Node mass, centre of mass and kernel size are
+// reduced bottom-up.  The roots' mass and centre of mass stay zero, as in the reference, whose
+// root never receives them (include/bhtree.hpp:46-53, src/bhtree.cpp:57).
+#include "context.cuh"
+
+namespace sphgpu {
+
+namespace {
+
+constexpr int RADIX_THREADS = 256;
+constexpr int RADIX_ITEMS = 16;
+constexpr int RADIX_TILE = RADIX_THREADS * RADIX_ITEMS;
+constexpr int LEVEL_CHUNK = 1024;
+
+// ---- root boxes ---------------------------------------------------------------------------
+
+__global__ void bbox_init_kernel(long long* bbox, int R, int D)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= R * D) return;
+    const int r = i / D, k = i % D;
+    bbox[r * 2 * D + k] = dbl_to_ord(1.7976931348623157e308);
+    bbox[r * 2 * D + D + k] = dbl_to_ord(-1.7976931348623157e308);
+}
+
+template <int D>
+__global__ void bbox_kernel(State st, int n, long long* bbox)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool ok = i < n;
+    const int r = ok ? st.run[i] : -1;
+    const unsigned same = __match_any_sync(FULL, r);
+    const bool whole_warp = same == FULL;
+    if (whole_warp && r < 0) return;   // a warp entirely past the end
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        double lo = ok ? st.f[F_POS + k][i] : 1.7976931348623157e308;
+        double hi = ok ? st.f[F_POS + k][i] : -1.7976931348623157e308;
+        if (whole_warp) {
+            for (int o = 16; o > 0; o >>= 1) {
+                lo = fmin(lo, __shfl_xor_sync(FULL, lo, o));
+                hi = fmax(hi, __shfl_xor_sync(FULL, hi, o));
+            }
+            if ((threadIdx.x & 31) == 0) {
+                atomicMin(&bbox[r * 2 * D + k], dbl_to_ord(lo));
+                atomicMax(&bbox[r * 2 * D + D + k], dbl_to_ord(hi));
+            }
+        } else if (ok) {
+            atomicMin(&bbox[r * 2 * D + k], dbl_to_ord(lo));
+            atomicMax(&bbox[r * 2 * D + D + k], dbl_to_ord(hi));
+        }
+    }
+}
+
+// Root node of every run (BHTree::initialize / BHTree::make, src/bhtree.cpp:12-40,59-95):
+// periodic -> center of the range, edge = largest range; else the bounding box of the run.
+template <int D>
+__global__ void roots_kernel(TreeView tv, double* center0, double* center1, double* center2,
+                             double* edge, int* begin, int* count, int* first, int* nchild,
+                             int* level, int* parent, int* arrive, double* mass, double* com0,
+                             double* com1, double* com2, const long long* bbox,
+                             const int* run_begin, int R, Periodic pb, int* lvl_start)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r == 0) { lvl_start[0] = 0; lvl_start[1] = 0; lvl_start[2] = R; }
+    if (r >= R) return;
+    double* cen[3] = {center0, center1, center2};
+    double l = 0.0;
+    for (int k = 0; k < D; ++k) {
+        double lo, hi;
+        if (pb.on) { lo = pb.lo[k]; hi = pb.hi[k]; }
+        else { lo = ord_to_dbl(bbox[r * 2 * D + k]); hi = ord_to_dbl(bbox[r * 2 * D + D + k]); }
+        cen[k][r] = (hi + lo) * 0.5;
+        const double range = hi - lo;
+        if (l < range) l = range;
+    }
+    edge[r] = l;
+    begin[r] = run_begin[r];
+    count[r] = run_begin[r + 1] - run_begin[r];
+    first[r] = -1;
+    nchild[r] = 0;
+    level[r] = 1;
+    parent[r] = -1;
+    arrive[r] = 0;
+    mass[r] = 0.0;
+    com0[r] = 0.0;
+    if (com1) com1[r] = 0.0;
+    if (com2) com2[r] = 0.0;
+}
+
+// ---- keys -------------------------------------------------------------------------------
+
+// The path of a particle through the reference's recursive split, one D-bit digit per level,
+// most significant first, with the run index above the digits.
+template <int D>
+__global__ void keys_kernel(State st, int n, TreeView tv, int levels, int run_shift,
+                            unsigned long long* keys, int* perm)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int r = st.run[i];
+    double x[D], c[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) { x[k] = st.f[F_POS + k][i]; c[k] = tv.center[k][r]; }
+    double e = tv.edge[r];
+    unsigned long long key = 0;
+    for (int l = 0; l < levels; ++l) {
+        unsigned digit = 0;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            const bool up = x[k] > c[k];
+            digit |= (up ? 1u : 0u) << k;
+            // child center: center + (+/-1 * edge) * 0.25, one rounding (src/bhtree.cpp:190-196)
+            c[k] = __dadd_rn(c[k], (up ? e : -e) * 0.25);
+        }
+        key = (key << D) | digit;
+        e = e * 0.5;
+    }
+    if (run_shift < 64) key |= (unsigned long long)r << run_shift;
+    keys[i] = key;
+    perm[i] = i;
+}
+
+// ---- radix sort (LSD, 8-bit digits, stable) ---------------------------------------------
+
+__global__ void radix_hist_kernel(const unsigned long long* keys, int n, int shift, int* hist,
+                                  int nblocks)
+{
+    __shared__ int h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const int base = blockIdx.x * RADIX_TILE;
+    for (int i = threadIdx.x; i < RADIX_TILE; i += RADIX_THREADS) {
+        const int idx = base + i;
+        if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 255], 1);
+    }
+    __syncthreads();
+    hist[threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+}
+
+// Exclusive scan of m ints in one block of 1024 threads.
+__global__ void scan_single_block_kernel(int* data, int m)
+{
+    __shared__ int part[1024];
+    const int t = threadIdx.x;
+    const int per = (m + 1023) / 1024;
+    const int b = t * per, e = min(m, b + per);
+    int s = 0;
+    for (int i = b; i < e; ++i) s += data[i];
+    part[t] = s;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const int v = t >= o ? part[t - o] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    int run = t > 0 ? part[t - 1] : 0;
+    for (int i = b; i < e; ++i) {
+        const int v = data[i];
+        data[i] = run;
+        run += v;
+    }
+}
+
+__global__ void radix_scatter_kernel(const unsigned long long* kin, const int* vin,
+                                     unsigned long long* kout, int* vout, int n, int shift,
+                                     const int* hist, int nblocks)
+{
+    __shared__ int base[256];
+    __shared__ int wcnt[RADIX_THREADS / 32][256];
+    const int t = threadIdx.x, w = t >> 5, lane = t & 31;
+    base[t] = hist[t * nblocks + blockIdx.x];
+    for (int round = 0; round < RADIX_ITEMS; ++round) {
+        const int idx = blockIdx.x * RADIX_TILE + round * RADIX_THREADS + t;
+        const bool valid = idx < n;
+        const unsigned long long k = valid ? kin[idx] : 0ull;
+        const int d = valid ? (int)((k >> shift) & 255) : 256;
+#pragma unroll
+        for (int ww = 0; ww < RADIX_THREADS / 32; ++ww) wcnt[ww][t] = 0;
+        __syncthreads();
+        const unsigned peers = __match_any_sync(FULL, d);
+        const int rank = __popc(peers & lanemask_lt());
+        if (valid && (__ffs(peers) - 1) == lane) wcnt[w][d] = __popc(peers);
+        __syncthreads();
+        int s = 0;
+#pragma unroll
+        for (int ww = 0; ww < RADIX_THREADS / 32; ++ww) {
+            const int c = wcnt[ww][t];
+            wcnt[ww][t] = s;
+            s += c;
+        }
+        __syncthreads();
+        if (valid) {
+            const int pos = base[d] + wcnt[w][d] + rank;
+            kout[pos] = k;
+            vout[pos] = vin[idx];
+        }
+        __syncthreads();
+        base[t] += s;
+    }
+}
+
+// ---- reorder ----------------------------------------------------------------------------
+
+struct FieldMove {
+    const double* src[F_COUNT];
+    double* dst[F_COUNT];
+    int nf;
+    const int* isrc[2];
+    int* idst[2];
+    int ni;
+};
+
+__global__ void reorder_kernel(FieldMove fm, const int* perm, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int j = perm[i];
+    for (int f = 0; f < fm.nf; ++f) fm.dst[f][i] = fm.src[f][j];
+    for (int f = 0; f < fm.ni; ++f) fm.idst[f][i] = fm.isrc[f][j];
+}
+
+__global__ void copy_fields_kernel(FieldMove fm, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int f = 0; f < fm.nf; ++f) fm.dst[f][i] = fm.src[f][i];
+    for (int f = 0; f < fm.ni; ++f) fm.idst[f][i] = fm.isrc[f][i];
+}
+
+// ---- level-by-level node construction ---------------------------------------------------
+
+struct NodeArrays {
+    int *begin, *count, *first, *nchild, *parent, *level, *arrive;
+    double *center[3], *edge;
+};
+
+template <int D>
+__device__ __forceinline__ void child_bounds(const unsigned long long* keys, int b, int cnt,
+                                             int shift, int* bnd)
+{
+    constexpr int NC = 1 << D;
+    bnd[0] = b;
+    bnd[NC] = b + cnt;
+    for (int c = 1; c < NC; ++c) {
+        int lo = bnd[c - 1], hi = b + cnt;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            const int dg = (int)((keys[mid] >> shift) & (NC - 1));
+            if (dg < c) lo = mid + 1; else hi = mid;
+        }
+        bnd[c] = lo;
+    }
+}
+
+template <int D>
+__global__ void level_count_kernel(NodeArrays na, const unsigned long long* keys,
+                                   const int* lvl_start, int l, int levels, int leaf_num,
+                                   int* lvl_tmp, int* chunk_sum)
+{
+    constexpr int NC = 1 << D;
+    __shared__ int red[32];
+    const int s = lvl_start[l], e = lvl_start[l + 1];
+    const int nchunks = (e - s + LEVEL_CHUNK - 1) / LEVEL_CHUNK;
+    for (int chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
+        const int node = s + chunk * LEVEL_CHUNK + threadIdx.x;
+        int nc = 0;
+        if (node < e) {
+            const int cnt = na.count[node];
+            const bool split = (l == 1) || (cnt > leaf_num && l <= levels);
+            if (split && cnt > 0) {
+                int bnd[NC + 1];
+                child_bounds<D>(keys, na.begin[node], cnt, D * (levels - l), bnd);
+                for (int c = 0; c < NC; ++c) nc += bnd[c + 1] > bnd[c];
+            }
+            if (!split) { na.first[node] = -1; na.nchild[node] = 0; }
+            lvl_tmp[node - s] = nc;
+        }
+        // block sum
+        int v = nc;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            int u = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0;
+            for (int o = 16; o > 0; o >>= 1) u += __shfl_xor_sync(FULL, u, o);
+            if (threadIdx.x == 0) chunk_sum[chunk] = u;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void level_scan_kernel(int* lvl_start, int l, int* chunk_sum, int node_cap,
+                                  unsigned* err)
+{
+    __shared__ int part[1024];
+    const int s = lvl_start[l], e = lvl_start[l + 1];
+    const int m = (e - s + LEVEL_CHUNK - 1) / LEVEL_CHUNK;
+    const int t = threadIdx.x;
+    const int per = (m + 1023) / 1024;
+    const int b = t * per, en = min(m, b + per);
+    int sum = 0;
+    for (int i = b; i < en; ++i) sum += chunk_sum[i];
+    part[t] = sum;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const int v = t >= o ? part[t - o] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    int run = t > 0 ? part[t - 1] : 0;
+    for (int i = b; i < en; ++i) {
+        const int v = chunk_sum[i];
+        chunk_sum[i] = run;
+        run += v;
+    }
+    if (t == 1023) {
+        int next = lvl_start[l + 1] + part[1023];
+        if (next > node_cap) { atomicOr(err, (unsigned)ERR_NODE_POOL); next = node_cap; }
+        lvl_start[l + 2] = next;
+    }
+}
+
+template <int D>
+__global__ void level_emit_kernel(NodeArrays na, const unsigned long long* keys,
+                                  const int* lvl_start, int l, int levels, int leaf_num,
+                                  const int* lvl_tmp, const int* chunk_off, int node_cap,
+                                  unsigned* err)
+{
+    constexpr int NC = 1 << D;
+    __shared__ int sc[LEVEL_CHUNK];
+    const int s = lvl_start[l], e = lvl_start[l + 1];
+    const int cbase = lvl_start[l + 1];
+    const int nchunks = (e - s + LEVEL_CHUNK - 1) / LEVEL_CHUNK;
+    for (int chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
+        const int node = s + chunk * LEVEL_CHUNK + threadIdx.x;
+        const int nc = node < e ? lvl_tmp[node - s] : 0;
+        sc[threadIdx.x] = nc;
+        __syncthreads();
+        for (int o = 1; o < LEVEL_CHUNK; o <<= 1) {
+            const int v = (int)threadIdx.x >= o ? sc[threadIdx.x - o] : 0;
+            __syncthreads();
+            sc[threadIdx.x] += v;
+            __syncthreads();
+        }
+        const int off = sc[threadIdx.x] - nc + chunk_off[chunk];
+        __syncthreads();
+        if (node < e && nc > 0) {
+            const int b = na.begin[node], cnt = na.count[node];
+            int bnd[NC + 1];
+            child_bounds<D>(keys, b, cnt, D * (levels - l), bnd);
+            const int fc = cbase + off;
+            if (fc + nc > node_cap) {
+                atomicOr(err, (unsigned)ERR_NODE_POOL);
+                na.first[node] = -1;
+                na.nchild[node] = 0;
+            } else {
+                na.first[node] = fc;
+                na.nchild[node] = nc;
+                const double edge = na.edge[node];
+                double cen[D];
+#pragma unroll
+                for (int k = 0; k < D; ++k) cen[k] = na.center[k][node];
+                int ci = fc;
+                for (int c = 0; c < NC; ++c) {
+                    if (bnd[c + 1] <= bnd[c]) continue;
+                    na.begin[ci] = bnd[c];
+                    na.count[ci] = bnd[c + 1] - bnd[c];
+                    na.level[ci] = l + 1;
+                    na.parent[ci] = node;
+                    na.first[ci] = -1;
+                    na.nchild[ci] = 0;
+                    na.arrive[ci] = 0;
+                    na.edge[ci] = edge * 0.5;
+#pragma unroll
+                    for (int k = 0; k < D; ++k)
+                        na.center[k][ci] = __dadd_rn(cen[k], ((c >> k) & 1 ? edge : -edge) * 0.25);
+                    ++ci;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---- bottom-up reductions ---------------------------------------------------------------
+
+// Mass and sum of m x per node: leaves sum their particles; the last child to finish sums its
+// parent's children (in child order, so the result does not depend on scheduling).
+template <int D>
+__global__ void moments_kernel(State st, const int* node_total_p, int R, int* begin, int* count,
+                               int* first, int* nchild, int* parent, int* arrive, double* mass,
+                               double* mx0, double* mx1, double* mx2)
+{
+    double* mx[3] = {mx0, mx1, mx2};
+    const int total = *node_total_p;
+    for (int i = R + blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        if (first[i] >= 0) continue;
+        double m = 0.0, s[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) s[k] = 0.0;
+        const int b = begin[i], e = b + count[i];
+        for (int j = b; j < e; ++j) {
+            const double mj = st.f[F_MASS][j];
+            m += mj;
+#pragma unroll
+            for (int k = 0; k < D; ++k) s[k] += st.f[F_POS + k][j] * mj;
+        }
+        mass[i] = m;
+#pragma unroll
+        for (int k = 0; k < D; ++k) mx[k][i] = s[k];
+        int node = i;
+        while (true) {
+            const int p = parent[node];
+            if (p < R) break;   // roots keep zero mass and centre (reference quirk)
+            __threadfence();
+            const int old = atomicAdd(&arrive[p], 1);
+            if (old != nchild[p] - 1) break;
+            __threadfence();
+            const int fc = first[p], nc = nchild[p];
+            double pm = 0.0, ps[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) ps[k] = 0.0;
+            for (int c = 0; c < nc; ++c) {
+                pm += __ldcg(&mass[fc + c]);
+#pragma unroll
+                for (int k = 0; k < D; ++k) ps[k] += __ldcg(&mx[k][fc + c]);
+            }
+            mass[p] = pm;
+#pragma unroll
+            for (int k = 0; k < D; ++k) mx[k][p] = ps[k];
+            node = p;
+        }
+    }
+}
+
+// centre of mass = (sum m x) / m for every non-root node (src/bhtree.cpp:152).
+template <int D>
+__global__ void com_finalize_kernel(const int* node_total_p, int R, const double* mass,
+                                    double* mx0, double* mx1, double* mx2)
+{
+    double* mx[3] = {mx0, mx1, mx2};
+    const int total = *node_total_p;
+    for (int i = R + blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const double m = mass[i];
+#pragma unroll
+        for (int k = 0; k < D; ++k) mx[k][i] = mx[k][i] / m;
+    }
+}
+
+// Per-node maximum smoothing length (BHNode::set_kernel, src/bhtree.cpp:206-232), bottom-up.
+__global__ void ksize_kernel(const double* sml, const int* node_total_p, int* begin, int* count,
+                             int* first, int* nchild, int* parent, int* arrive, double* ksize)
+{
+    const int total = *node_total_p;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        if (first[i] >= 0) continue;
+        double h = 0.0;
+        const int b = begin[i], e = b + count[i];
+        for (int j = b; j < e; ++j) h = fmax(h, sml[j]);
+        ksize[i] = h;
+        int node = i;
+        while (true) {
+            const int p = parent[node];
+            if (p < 0) break;
+            __threadfence();
+            const int old = atomicAdd(&arrive[p], 1);
+            if (old != nchild[p] - 1) break;
+            __threadfence();
+            const int fc = first[p], nc = nchild[p];
+            double hm = 0.0;
+            for (int c = 0; c < nc; ++c) hm = fmax(hm, __ldcg(&ksize[fc + c]));
+            ksize[p] = hm;
+            node = p;
+        }
+    }
+}
+
+// ---- target groups -------------------------------------------------------------------------
+
+// Partition the particles into groups of at most G consecutive (key-ordered) particles that are
+// spatially compact: maximal nodes with <= G particles, with consecutive such siblings merged
+// while the merged count stays <= G; a leaf with more than G particles is cut into chunks.
+__global__ void groups_kernel(const int* node_total_p, int R, const int* begin, const int* count,
+                              const int* first, const int* nchild, int G, int* g_begin,
+                              int* g_count, int* n_groups, int max_groups, unsigned* err)
+{
+    const int total = *node_total_p;
+    auto emit = [&](int b, int c) {
+        const int slot = atomicAdd(n_groups, 1);
+        if (slot < max_groups) { g_begin[slot] = b; g_count[slot] = c; }
+        else atomicOr(err, (unsigned)ERR_TILE);
+    };
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int cnt = count[i];
+        if (i < R) {
+            if (cnt == 0) continue;
+            if (cnt <= G) { emit(begin[i], cnt); continue; }
+        } else if (cnt <= G || first[i] < 0) {
+            continue;
+        }
+        const int fc = first[i], nc = nchild[i];
+        if (fc < 0) {
+            // a root with > G particles that was not split (cannot happen: roots always split)
+            for (int b = begin[i]; b < begin[i] + cnt; b += G) emit(b, min(G, begin[i] + cnt - b));
+            continue;
+        }
+        int ab = -1, an = 0;
+        for (int c = 0; c < nc; ++c) {
+            const int ch = fc + c, cc = count[ch];
+            if (cc <= G) {
+                if (an + cc > G) { emit(ab, an); an = 0; }
+                if (an == 0) ab = begin[ch];
+                an += cc;
+            } else {
+                if (an > 0) { emit(ab, an); an = 0; }
+                if (first[ch] < 0)
+                    for (int b = begin[ch]; b < begin[ch] + cc; b += G) emit(b, min(G, begin[ch] + cc - b));
+            }
+        }
+        if (an > 0) emit(ab, an);
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------
+
+TreeView tree_view(const Ctx& c)
+{
+    TreeView t;
+    t.begin = c.nd_begin;
+    t.count = c.nd_count;
+    t.first_child = c.nd_first;
+    t.nchild = c.nd_nchild;
+    for (int k = 0; k < 3; ++k) { t.center[k] = c.nd_center[k]; t.com[k] = c.nd_com[k]; }
+    t.edge = c.nd_edge;
+    t.mass = c.nd_mass;
+    t.ksize = c.nd_ksize;
+    return t;
+}
+
+int tree_alloc(Ctx& c)
+{
+    const int n = c.n;
+    c.node_cap = 5 * n + c.R;   // BHTree::resize: particle_num * 5 (src/bhtree.cpp:42-53)
+    const size_t nc = (size_t)c.node_cap;
+    cudaError_t e = cudaSuccess;
+    auto A = [&](void** p, size_t bytes) { if (e == cudaSuccess) e = cudaMalloc(p, bytes ? bytes : 8); };
+    A((void**)&c.keys, sizeof(unsigned long long) * n);
+    A((void**)&c.keys_alt, sizeof(unsigned long long) * n);
+    A((void**)&c.perm, sizeof(int) * n);
+    A((void**)&c.perm_alt, sizeof(int) * n);
+    c.radix_blocks = ceil_div(n, RADIX_TILE);
+    A((void**)&c.radix_hist, sizeof(int) * 256 * c.radix_blocks);
+    A((void**)&c.nd_begin, sizeof(int) * nc);
+    A((void**)&c.nd_count, sizeof(int) * nc);
+    A((void**)&c.nd_first, sizeof(int) * nc);
+    A((void**)&c.nd_nchild, sizeof(int) * nc);
+    A((void**)&c.nd_parent, sizeof(int) * nc);
+    A((void**)&c.nd_level, sizeof(int) * nc);
+    A((void**)&c.nd_arrive, sizeof(int) * nc);
+    for (int k = 0; k < c.dim; ++k) {
+        A((void**)&c.nd_center[k], sizeof(double) * nc);
+        A((void**)&c.nd_com[k], sizeof(double) * nc);
+    }
+    A((void**)&c.nd_edge, sizeof(double) * nc);
+    A((void**)&c.nd_mass, sizeof(double) * nc);
+    A((void**)&c.nd_ksize, sizeof(double) * nc);
+    A((void**)&c.lvl_start, sizeof(int) * (MAX_LEVELS + 2));
+    A((void**)&c.lvl_tmp, sizeof(int) * nc);
+    A((void**)&c.chunk_sum, sizeof(int) * (ceil_div(nc, LEVEL_CHUNK) + 1));
+    A((void**)&c.bbox, sizeof(long long) * 2 * 3 * c.R);
+    A((void**)&c.node_total, sizeof(int));
+    c.max_groups = n + c.R;
+    A((void**)&c.g_begin, sizeof(int) * c.max_groups);
+    A((void**)&c.g_count, sizeof(int) * c.max_groups);
+    A((void**)&c.n_groups, sizeof(int));
+    if (e != cudaSuccess) {
+        c.last_error = std::string("tree allocation: ") + cudaGetErrorString(e);
+        return SPHGPU_ERR_CUDA;
+    }
+    cudaMemset(c.lvl_start, 0, sizeof(int) * (MAX_LEVELS + 2));
+    return SPHGPU_OK;
+}
+
+void tree_free(Ctx& c)
+{
+    void* ptrs[] = {c.keys, c.keys_alt, c.perm, c.perm_alt, c.radix_hist, c.nd_begin, c.nd_count,
+                    c.nd_first, c.nd_nchild, c.nd_parent, c.nd_level, c.nd_arrive, c.nd_center[0],
+                    c.nd_center[1], c.nd_center[2], c.nd_com[0], c.nd_com[1], c.nd_com[2],
+                    c.nd_edge, c.nd_mass, c.nd_ksize, c.lvl_start, c.lvl_tmp, c.chunk_sum, c.bbox,
+                    c.node_total, c.g_begin, c.g_count, c.n_groups};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+}
+
+void launch_reorder_fields(Ctx& c, bool all)
+{
+    // Inside a step, fields that the stages after the rebuild recompute before reading them need
+    // no move: PRES, SML, ACC, DENE always; GRADH for ssph/disph; PHI with gravity; the gsph
+    // gradients with the second-order scheme.
+    FieldMove fm{};
+    for (int f = 0; f < F_COUNT; ++f) {
+        if (!c.st.f[f]) continue;
+        if (!all) {
+            bool recomputed = (f >= F_ACC && f < F_ACC + 3) || f == F_PRES || f == F_DENE || f == F_SML;
+            if (f == F_GRADH && c.p.sph_type != 2) recomputed = true;
+            if (f == F_PHI && c.p.use_gravity) recomputed = true;
+            if (f >= F_GRADD && c.p.sph_type == 2 && c.p.gsph_2nd_order) recomputed = true;
+            if (recomputed) continue;
+        }
+        fm.src[fm.nf] = c.st.f[f];
+        fm.dst[fm.nf] = c.alt.f[f];
+        ++fm.nf;
+    }
+    fm.isrc[0] = c.st.id; fm.idst[0] = c.alt.id;
+    fm.ni = 1;
+    if (all) { fm.isrc[1] = c.st.neighbor; fm.idst[1] = c.alt.neighbor; fm.ni = 2; }
+    reorder_kernel<<<ceil_div(c.n, 256), 256, 0, c.stream>>>(fm, c.perm, c.n);
+    // copy back, so the state keeps its buffers (the step graph replays fixed pointers)
+    FieldMove back{};
+    back.nf = fm.nf;
+    back.ni = fm.ni;
+    for (int q = 0; q < fm.nf; ++q) { back.src[q] = fm.dst[q]; back.dst[q] = const_cast<double*>(fm.src[q]); }
+    for (int q = 0; q < fm.ni; ++q) { back.isrc[q] = fm.idst[q]; back.idst[q] = const_cast<int*>(fm.isrc[q]); }
+    copy_fields_kernel<<<ceil_div(c.n, 256), 256, 0, c.stream>>>(back, c.n);
+}
+
+template <int D>
+static void make_tree_d(Ctx& c, bool reorder_all)
+{
+    const int n = c.n, R = c.R;
+    cudaStream_t s = c.stream;
+    TreeView tv = tree_view(c);
+    if (!c.pb.on) {
+        bbox_init_kernel<<<ceil_div(R * D, 128), 128, 0, s>>>(c.bbox, R, D);
+        bbox_kernel<D><<<ceil_div(n, 256), 256, 0, s>>>(c.st, n, c.bbox);
+    }
+    roots_kernel<D><<<ceil_div(R, 128), 128, 0, s>>>(
+        tv, c.nd_center[0], c.nd_center[1], c.nd_center[2], c.nd_edge, c.nd_begin, c.nd_count,
+        c.nd_first, c.nd_nchild, c.nd_level, c.nd_parent, c.nd_arrive, c.nd_mass, c.nd_com[0],
+        c.nd_com[1], c.nd_com[2], c.bbox, c.d_run_begin, R, c.pb, c.lvl_start);
+    const int levels = c.key_levels;
+    const int run_shift = D * levels;
+    keys_kernel<D><<<ceil_div(n, 256), 256, 0, s>>>(c.st, n, tv, levels, run_shift, c.keys, c.perm);
+    // radix sort on the significant bits
+    const int bits = D * levels + c.run_bits;
+    const int passes = (bits + 7) / 8;
+    for (int p = 0; p < passes; ++p) {
+        const int shift = 8 * p;
+        radix_hist_kernel<<<c.radix_blocks, RADIX_THREADS, 0, s>>>(c.keys, n, shift, c.radix_hist, c.radix_blocks);
+        scan_single_block_kernel<<<1, 1024, 0, s>>>(c.radix_hist, 256 * c.radix_blocks);
+        radix_scatter_kernel<<<c.radix_blocks, RADIX_THREADS, 0, s>>>(
+            c.keys, c.perm, c.keys_alt, c.perm_alt, n, shift, c.radix_hist, c.radix_blocks);
+        std::swap(c.keys, c.keys_alt);
+        std::swap(c.perm, c.perm_alt);
+    }
+    launch_reorder_fields(c, reorder_all);
+    // nodes, level by level
+    NodeArrays na;
+    na.begin = c.nd_begin; na.count = c.nd_count; na.first = c.nd_first; na.nchild = c.nd_nchild;
+    na.parent = c.nd_parent; na.level = c.nd_level; na.arrive = c.nd_arrive;
+    for (int k = 0; k < 3; ++k) na.center[k] = c.nd_center[k];
+    na.edge = c.nd_edge;
+    const int grid = std::max(1, std::min(c.num_sms * 4, ceil_div(c.node_cap, LEVEL_CHUNK)));
+    for (int l = 1; l <= levels + 1; ++l) {
+        level_count_kernel<D><<<grid, LEVEL_CHUNK, 0, s>>>(na, c.keys, c.lvl_start, l, levels,
+                                                         c.p.leaf_num, c.lvl_tmp, c.chunk_sum);
+        level_scan_kernel<<<1, 1024, 0, s>>>(c.lvl_start, l, c.chunk_sum, c.node_cap, c.d_err);
+        level_emit_kernel<D><<<grid, LEVEL_CHUNK, 0, s>>>(na, c.keys, c.lvl_start, l, levels,
+                                                        c.p.leaf_num, c.lvl_tmp, c.chunk_sum,
+                                                        c.node_cap, c.d_err);
+    }
+    cudaMemcpyAsync(c.node_total, c.lvl_start + levels + 2, sizeof(int), cudaMemcpyDeviceToDevice, s);
+    launch_node_moments(c);
+    // target groups for the three pair kernels (one list; group size = 32 * max warps)
+    cudaMemsetAsync(c.n_groups, 0, sizeof(int), s);
+    const int G = 32 * c.gw_pre;
+    c.group_threads = G;
+    groups_kernel<<<c.num_sms * 4, 256, 0, s>>>(c.node_total, R, c.nd_begin, c.nd_count, c.nd_first,
+                                                c.nd_nchild, G, c.g_begin, c.g_count, c.n_groups,
+                                                c.max_groups, c.d_err);
+    c.tree_valid = true;
+    c.kernel_size_valid = false;
+}
+
+void launch_make_tree(Ctx& c, bool reorder_all)
+{
+    if (c.dim == 1) make_tree_d<1>(c, reorder_all);
+    else if (c.dim == 2) make_tree_d<2>(c, reorder_all);
+    else make_tree_d<3>(c, reorder_all);
+}
+
+void launch_node_moments(Ctx& c)
+{
+    const int grid = c.num_sms * 4;
+    if (c.dim == 1) {
+        moments_kernel<1><<<grid, 256, 0, c.stream>>>(c.st, c.node_total, c.R, c.nd_begin, c.nd_count, c.nd_first, c.nd_nchild, c.nd_parent, c.nd_arrive, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
+        com_finalize_kernel<1><<<grid, 256, 0, c.stream>>>(c.node_total, c.R, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
+    } else if (c.dim == 2) {
+        moments_kernel<2><<<grid, 256, 0, c.stream>>>(c.st, c.node_total, c.R, c.nd_begin, c.nd_count, c.nd_first, c.nd_nchild, c.nd_parent, c.nd_arrive, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
+        com_finalize_kernel<2><<<grid, 256, 0, c.stream>>>(c.node_total, c.R, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
+    } else {
+        moments_kernel<3><<<grid, 256, 0, c.stream>>>(c.st, c.node_total, c.R, c.nd_begin, c.nd_count, c.nd_first, c.nd_nchild, c.nd_parent, c.nd_arrive, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
+        com_finalize_kernel<3><<<grid, 256, 0, c.stream>>>(c.node_total, c.R, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
+    }
+}
+
+void launch_set_kernel_size(Ctx& c)
+{
+    // counters reset: the moments pass left arrive[p] = nchild[p]
+    cudaMemsetAsync(c.nd_arrive, 0, sizeof(int) * c.node_cap, c.stream);
+    ksize_kernel<<<c.num_sms * 4, 256, 0, c.stream>>>(c.st.f[F_SML], c.node_total, c.nd_begin,
+                                                      c.nd_count, c.nd_first, c.nd_nchild,
+                                                      c.nd_parent, c.nd_arrive, c.nd_ksize);
+    c.kernel_size_valid = true;
+}
+
+}  // namespace sphgpu
