@@ -380,7 +380,7 @@ int create_impl(const sphgpu_params* params, int dim, int n_runs, const int* run
         A(&c.mir[5], c.p.sph_type == 2 ? sizeof(double) * 16 * n : 16);   // gsph gradients
         A(&c.mir[6], c.p.use_gravity ? sizeof(double4_32a) * n : 16);          // gravity leaf offsets
         A(&c.mir[7], c.p.use_gravity ? sizeof(double) * n : 16);           // gravity h
-        for (int q = 0; q < 6 && e == cudaSuccess; ++q) e = cudaEventCreate(&c.ev[q]);
+        for (int q = 0; q < 7 && e == cudaSuccess; ++q) e = cudaEventCreate(&c.ev[q]);
         if (e != cudaSuccess) rc = cuda_status(c, e, "create");
     }
     if (rc == SPHGPU_OK) {

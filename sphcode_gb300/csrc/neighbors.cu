@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(256) neighbors_kernel(NbArgs a)
             }
         }
         a.counts[id_i] = cnt;
-        if (cnt > a.cap) atomicOr(a.work.err, (unsigned)ERR_LIST);
+        if (a.list && cnt > a.cap) atomicOr(a.work.err, (unsigned)ERR_LIST);
     }
 }
 
