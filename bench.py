@@ -192,9 +192,25 @@ def main():
     ap.add_argument("--ref-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--profile-run", action="store_true",
+                    help="initialize + --steps eager steps and exit (a short, fixed launch sequence "
+                         "for ncu: no timing, graphs, CPU baseline or e2e)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference_arm(args)
+        return
+    if args.profile_run:
+        import __graft_entry__ as g
+        g.build()
+        from sphcode_gb300 import sphgpu
+        p, f, desc = workload(args.workload)
+        with sphgpu.GpuSimulation(p, f, precision=args.precision) as sim:
+            sim.set_tuning("graph", 0)
+            sim.initialize()
+            sim.step(args.steps)
+            print(json.dumps({"profile_run": desc, "n": sim.n, "steps": args.steps,
+                              "precision": args.precision, "time": sim.scalar("time")}))
         return
     if args.warmup < 3:
         raise SystemExit("at least 3 warm-up steps")
