@@ -211,6 +211,29 @@ int sphgpu_bench_steps(sphgpu_ctx* ctx, int n_steps, int flush_l2, double* ms);
  * device in TFLOP/s, the denominators of the pair kernels' compute rooflines. */
 int sphgpu_measure_peaks(double* fp32_tflops, double* fp64_tflops);
 
+/* ---- allocation-free entry point ---------------------------------------------------------- */
+
+/* Energy and momentum sums of sphgpu_energy over caller-owned device arrays, with no device
+ * allocation at all.  No counterpart in the reference.  It is meant for callers that cannot
+ * call cudaMalloc where they need the sums: code inside another library's CUDA stream capture
+ * (allocation is not allowed while a stream is captured) and host programs that own every byte
+ * of device memory through a pool they reserved at start-up.
+ *
+ * Inputs are device pointers in the caller's particle order: mass[n], vel[n * dim] (interleaved
+ * x0 y0 z0 x1 ...), ene[n] and phi[n] (phi may be NULL: potential 0).  out is a device pointer
+ * to 4 + dim doubles {kinetic, thermal, potential, total, p_0 .. p_{dim-1}}, written on `stream`
+ * (a cudaStream_t; NULL = the legacy default stream); the call returns once the work is queued.
+ *
+ * Scratch: a fixed file-scope device array of 4096 x 7 doubles (229,376 bytes) that every GPU
+ * loading the library keeps until the process exits; hence n <= 33,554,432 (4096 chunks of 8192
+ * particles), larger n returns SPHGPU_ERR_CAPACITY with the text in sphgpu_last_error(NULL).
+ * The first call on a device looks up the array's device address (cudaGetSymbolAddress) with
+ * that device current; make that first call before any stream capture.  All calls share the one
+ * array: calls that may overlap on the GPU (different streams, or different host threads on the
+ * same device) race on it and must be serialised by the caller. */
+int sphgpu_energy_noalloc(int dim, int n, const double* mass, const double* vel, const double* ene,
+                          const double* phi, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

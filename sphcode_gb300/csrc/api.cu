@@ -474,6 +474,12 @@ int kernel_occupancy(const void* kern, int threads, size_t smem)
 
 void reset_work_counters(Ctx& c) { cudaMemsetAsync(c.d_work, 0, sizeof(int) * 16, c.stream); }
 
+void set_global_error(const std::string& text)
+{
+    std::lock_guard<std::mutex> lk(g_err_mutex);
+    g_create_error = text;
+}
+
 void launch_pre(Ctx& c, bool initial)
 {
     if (c.dim == 1) launch_pre_dim<1>(c, initial);

@@ -137,6 +137,7 @@ inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 int max_optin_smem(const Ctx& c);
 int kernel_occupancy(const void* kern, int threads, size_t smem);
 void reset_work_counters(Ctx& c);
+void set_global_error(const std::string& text);   // text of sphgpu_last_error(NULL)
 
 // The largest source tile that fits the opt-in shared memory next to the walk capacities of the
 // overflow pass.

@@ -83,6 +83,7 @@ _SIGS = {
     "sphgpu_stage_times": (ctypes.c_int, [_P, _P]),
     "sphgpu_bench_steps": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "sphgpu_measure_peaks": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    "sphgpu_energy_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _P, _P, _P, _P, _P, _P]),
 }
 
 
