@@ -193,6 +193,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--group-warps", type=int, default=0,
+                    help="target-group size in warps (0 = the library's default)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--tile-pre", type=int, default=0)
+    ap.add_argument("--tile-fluid", type=int, default=0)
     ap.add_argument("--profile-run", action="store_true",
                     help="initialize + --steps eager steps and exit (a short, fixed launch sequence "
                          "for ncu: no timing, graphs, CPU baseline or e2e)")
@@ -249,7 +254,17 @@ def main():
         return float(t.item())
 
     # ---- FP32-pair form: device-resident throughput --------------------------------------
-    sim = sphgpu.GpuSimulation(p, f, precision="fp32")
+    def make(prec):
+        s_ = sphgpu.GpuSimulation(p, f, precision=prec)
+        if args.group_warps:
+            s_.set_tuning("group_warps", args.group_warps)
+        if args.tile_pre:
+            s_.set_tuning("tile_cap_pre", args.tile_pre)
+        if args.tile_fluid:
+            s_.set_tuning("tile_cap", args.tile_fluid)
+        return s_
+
+    sim = make("fp32")
     sim.initialize()
     sim.step(args.warmup)
     launches_per_step = sim.get_tuning("graph_kernels")
@@ -271,6 +286,10 @@ def main():
         sim.step(1)
         for k, v in sim.stage_times().items():
             stages[k] += v / reps
+    overflow = {"pre": sim.get_tuning("overflow_pre"), "fluid": sim.get_tuning("overflow_fluid")}
+    schedule = {"group_warps": sim.get_tuning("group_warps"), "tile_pre": sim.get_tuning("tile_cap_pre"),
+                "tile_fluid": sim.get_tuning("tile_cap"), "autotuned": bool(sim.get_tuning("autotune")),
+                "rejected_candidate_status_bits": sim.get_tuning("tune_rejects")}
     sim.set_tuning("timing", 0)
     pairs = sim.neighbor_counts(True).astype(np.int64) - 1   # r = 0 (self) is skipped
     mean_pairs = float(pairs.mean())
@@ -281,8 +300,8 @@ def main():
     fp64 = None
     errs = {}
     if not args.no_fp64:
-        s64 = sphgpu.GpuSimulation(p, f, precision="fp64")
-        s32 = sphgpu.GpuSimulation(p, f, precision="fp32")
+        s64 = make("fp64")
+        s32 = make("fp32")
         s64.initialize()
         s32.initialize()
         s64.step(1)
@@ -299,38 +318,40 @@ def main():
         s64.close()
 
     # ---- end to end through the reference-facing AoS boundary, host buffers ------------------
-    dt = aos_dtype(D)
-    holder, raw = pinned_array(n * dt.itemsize)
-    aos = raw.view(dt)
-    aos[:] = 0
-    aos["pos"] = f["pos"].reshape(n, D)
-    aos["vel"] = f["vel"].reshape(n, D)
-    aos["mass"] = f["mass"]
-    aos["dens"] = f["dens"]
-    aos["pres"] = f["pres"]
-    aos["ene"] = f["ene"]
-    aos["id"] = np.arange(n)
-    lay = aos_layout(dt)
-    import ctypes
-    e2e_sim = sphgpu.GpuSimulation(p, f, precision="fp32")
-    e2e_sim.initialize()
-    e2e_sim.lib.sphgpu_download_aos(e2e_sim._h, ctypes.c_void_p(raw.ctypes.data), ctypes.byref(lay))
-    e2e_sim.step(args.warmup)
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        rc = e2e_sim.lib.sphgpu_upload_aos(e2e_sim._h, ctypes.c_void_p(raw.ctypes.data), ctypes.byref(lay))
-        rc |= e2e_sim.lib.sphgpu_step(e2e_sim._h, 1)
-        rc |= e2e_sim.lib.sphgpu_download_aos(e2e_sim._h, ctypes.c_void_p(raw.ctypes.data), ctypes.byref(lay))
-        if rc:
-            raise RuntimeError(e2e_sim.lib.sphgpu_last_error(e2e_sim._h))
-    barrier()
-    e2e_s = max_over_ranks(time.perf_counter() - t0)
-    e2e_sim.close()
-    e2e = {"value": world * n * args.steps / e2e_s, "unit": "particle-steps/s",
-           "h2d_bytes_per_step": 2 * n * dt.itemsize, "d2h_bytes_per_step": n * dt.itemsize,
-           "path": "sphgpu_upload_aos + sphgpu_step(1) + sphgpu_download_aos on a pinned "
-                   "std::vector<SPHParticle>-layout buffer"}
+    e2e = None
+    if not args.no_e2e:
+        dt = aos_dtype(D)
+        holder, raw = pinned_array(n * dt.itemsize)
+        aos = raw.view(dt)
+        aos[:] = 0
+        aos["pos"] = f["pos"].reshape(n, D)
+        aos["vel"] = f["vel"].reshape(n, D)
+        aos["mass"] = f["mass"]
+        aos["dens"] = f["dens"]
+        aos["pres"] = f["pres"]
+        aos["ene"] = f["ene"]
+        aos["id"] = np.arange(n)
+        lay = aos_layout(dt)
+        import ctypes
+        e2e_sim = make("fp32")
+        e2e_sim.initialize()
+        e2e_sim.lib.sphgpu_download_aos(e2e_sim._h, ctypes.c_void_p(raw.ctypes.data), ctypes.byref(lay))
+        e2e_sim.step(args.warmup)
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            rc = e2e_sim.lib.sphgpu_upload_aos(e2e_sim._h, ctypes.c_void_p(raw.ctypes.data), ctypes.byref(lay))
+            rc |= e2e_sim.lib.sphgpu_step(e2e_sim._h, 1)
+            rc |= e2e_sim.lib.sphgpu_download_aos(e2e_sim._h, ctypes.c_void_p(raw.ctypes.data), ctypes.byref(lay))
+            if rc:
+                raise RuntimeError(e2e_sim.lib.sphgpu_last_error(e2e_sim._h))
+        barrier()
+        e2e_s = max_over_ranks(time.perf_counter() - t0)
+        e2e_sim.close()
+        e2e = {"value": world * n * args.steps / e2e_s, "unit": "particle-steps/s",
+               "h2d_bytes_per_step": 2 * n * dt.itemsize, "d2h_bytes_per_step": n * dt.itemsize,
+               "path": "sphgpu_upload_aos + sphgpu_step(1) + sphgpu_download_aos on a pinned "
+                       "std::vector<SPHParticle>-layout buffer"}
 
     # ---- roofline of the dominant kernel ----------------------------------------------------
     fp32_peak, fp64_peak = sphgpu.measure_peaks()
@@ -378,7 +399,8 @@ def main():
                 "fp64_form": fp64,
                 "fp32_over_fp64": (value / fp64["value"]) if fp64 else None,
                 "fp32_rel_err_vs_fp64_after_1_step": errs,
-                "stage_ms": stages, "newton_failures": newton_fail,
+                "stage_ms": stages, "overflow_groups": overflow, "newton_failures": newton_fail,
+                "schedule": schedule,
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
                 "gpu_launches": launches_per_step * args.steps,
                 "peaks": {"fp32_tflops": fp32_peak, "fp64_tflops": fp64_peak}}

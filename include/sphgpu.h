@@ -189,11 +189,17 @@ int sphgpu_newton_failures(sphgpu_ctx* ctx, int* count);
 /* Text of the last error on this context (or of the last failed create if ctx is NULL). */
 const char* sphgpu_last_error(const sphgpu_ctx* ctx);
 
-/* Kernel schedule knobs (chosen by the autotuner; exposed for tests and the tuner):
+/* Kernel schedule knobs.  With autotune on (the default), sphgpu_initialize times
+ * PreInteraction and FluidForce for candidate target-group sizes and tile capacities on the
+ * initial state and keeps the fastest; setting 0, 3 or 10 explicitly turns the tuner off. */
+/* Knobs:
  * which = 0 target-group size in warps, 1 FluidForce warps, 2 GravityForce warps,
  * 3 source-tile capacity (0 = automatic), 4 autotune on/off, 5 per-stage event timing on/off
  * (steps then run eagerly), 6 CUDA-graph replay of steps on/off; 7 (read only) kernel launches
- * in one captured step. */
+ * in one captured step; 8, 9 (read only) target groups that overflowed into the large-capacity
+ * pass in the last timed PreInteraction / FluidForce; 10 PreInteraction source-tile capacity
+ * (0 = automatic; 3 then applies to FluidForce); 11 (read only) status bits raised by tuning
+ * candidates that the tuner rejected. */
 int sphgpu_set_tuning(sphgpu_ctx* ctx, int which, int value);
 int sphgpu_get_tuning(sphgpu_ctx* ctx, int which, int* value);
 

@@ -27,6 +27,11 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 # The integrator and the tree keys restate FP64 arithmetic of the reference operation by
 # operation; without contraction into FMAs their results are bit-identical to it.
 NO_FMA = {"integrate.cu", "tree.cu"}
+# The pair kernels take FP32 division and square root from the fast hardware approximations:
+# every membership decision is made on products and sums only (and re-decided in FP64 inside its
+# guard band), so only the FP32 pair terms see the approximation.  FP64 arithmetic is unaffected.
+FAST_F32 = {"pre_d1.cu", "pre_d2.cu", "pre_d3.cu", "fluid_d1.cu", "fluid_d2.cu", "fluid_d3.cu",
+            "gravity.cu", "neighbors.cu"}
 
 
 def nvcc() -> str:
@@ -62,6 +67,8 @@ def build_library(force: bool = False, jobs: int = 0, verbose: bool = False) -> 
             flags = list(COMMON)
             if os.path.basename(s) in NO_FMA:
                 flags.append("--fmad=false")
+            if os.path.basename(s) in FAST_F32:
+                flags += ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"]
             todo.append([exe, *ARCH, *flags, "-c", s, "-o", o])
 
     def run(cmd):

@@ -209,7 +209,8 @@ int finish(Ctx& c, const char* what)
     e = cudaMemcpy(&bits, c.d_err, sizeof(unsigned), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_status(c, e, what);
     if (bits) {
-        cudaMemset(c.d_err, 0, sizeof(unsigned));
+        cudaMemsetAsync(c.d_err, 0, sizeof(unsigned), c.stream);
+        cudaStreamSynchronize(c.stream);
         c.last_error = std::string(what) + ": " + err_bits_text(bits);
         return (int)err_bits_to_status(bits);
     }
@@ -262,7 +263,7 @@ void free_ctx(Ctx& c)
     c.alt.run = nullptr;
     free_state(c.alt, false);
     void* ptrs[] = {c.d_run_begin, c.d_time, c.d_dt, c.d_hvs, c.d_dtmin, c.d_sums, c.d_err,
-                    c.d_newton_fail, c.d_work, c.d_ovf_list, c.d_stage, c.d_aos, c.d_flush};
+                    c.d_newton_fail, c.d_work, c.d_ovf_list, c.d_ovf_list2, c.d_stage, c.d_aos, c.d_flush};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (void* p : c.mir)
@@ -342,6 +343,7 @@ int create_impl(const sphgpu_params* params, int dim, int n_runs, const int* run
         c.pb.lo[k] = params->range_min[k];
         c.pb.hi[k] = params->range_max[k];
         c.pb.len[k] = params->range_max[k] - params->range_min[k];
+        c.pb.lenf[k] = (float)c.pb.len[k];
     }
     c.run_begin.assign(n_runs + 1, 0);
     for (int r = 0; r < n_runs; ++r) c.run_begin[r + 1] = c.run_begin[r] + run_sizes[r];
@@ -369,6 +371,7 @@ int create_impl(const sphgpu_params* params, int dim, int n_runs, const int* run
         A((void**)&c.d_newton_fail, sizeof(int));
         A((void**)&c.d_work, sizeof(int) * 16);
         A((void**)&c.d_ovf_list, sizeof(int) * c.max_groups);
+        A((void**)&c.d_ovf_list2, sizeof(int) * c.max_groups);
         c.stage_bytes = sizeof(double) * n * (size_t)std::max(9, dim * dim);
         A((void**)&c.d_stage, c.stage_bytes);
         // key-ordered mirrors in the pair type, sized for FP64
@@ -378,11 +381,12 @@ int create_impl(const sphgpu_params* params, int dim, int n_runs, const int* run
         A(&c.mir[3], sizeof(double4_32a) * n);                       // Fluid rec1
         A(&c.mir[4], sizeof(double4_32a) * n);                       // Fluid rec2
         A(&c.mir[5], c.p.sph_type == 2 ? sizeof(double) * 16 * n : 16);   // gsph gradients
-        A(&c.mir[6], c.p.use_gravity ? sizeof(double4_32a) * n : 16);          // gravity leaf offsets
-        A(&c.mir[7], c.p.use_gravity ? sizeof(double) * n : 16);           // gravity h
+        A(&c.mir[6], sizeof(double4_32a) * n);                        // {x - leaf centre, m}
+        A(&c.mir[7], sizeof(double) * n);                             // h
         for (int q = 0; q < 7 && e == cudaSuccess; ++q) e = cudaEventCreate(&c.ev[q]);
         if (e != cudaSuccess) rc = cuda_status(c, e, "create");
     }
+    if (rc == SPHGPU_OK) rc = build_groups(c);
     if (rc == SPHGPU_OK) {
         cudaMemcpy(c.d_run_begin, c.run_begin.data(), sizeof(int) * (c.R + 1), cudaMemcpyHostToDevice);
         cudaMemset(c.d_time, 0, sizeof(double) * c.R);
@@ -424,6 +428,113 @@ void run_pre_stage(Ctx& c)
     launch_set_kernel_size(c);   // BHTree::set_kernel at the end of PreInteraction::calculation
 }
 
+// ---- autotuner ------------------------------------------------------------------------------
+// Times PreInteraction and FluidForce on the live state for candidate schedules — target-group
+// size (32 or 64 particles, i.e. 1 or 2 warps per CTA) and the source-tile capacity of each
+// stage — and keeps the fastest.  Runs inside sphgpu_initialize after the initial smoothing pass,
+// so every Pre trial starts from the same inputs: the fields PreInteraction reads and overwrites
+// (density for the smoothing-length guess, alpha, Balsara) are saved once and restored before
+// every trial and before the final Pre that the caller's results come from.
+__global__ void copy3_kernel(const double* a, const double* b, const double* c3, double* dst, int n, int dir)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (dir == 0) { dst[i] = a[i]; dst[n + i] = b[i]; dst[2 * (size_t)n + i] = c3[i]; }
+    else {
+        const_cast<double*>(a)[i] = dst[i];
+        const_cast<double*>(b)[i] = dst[n + i];
+        const_cast<double*>(c3)[i] = dst[2 * (size_t)n + i];
+    }
+}
+
+void pre_inputs(Ctx& c, int dir)   // 0 save, 1 restore (into the staging buffer)
+{
+    copy3_kernel<<<ceil_div(c.n, 256), 256, 0, c.stream>>>(c.st.f[F_DENS], c.st.f[F_ALPHA], c.st.f[F_BALSARA],
+                                                            c.d_stage, c.n, dir);
+}
+
+// Device status bits raised since the last check (cleared); used to reject a tuning candidate.
+unsigned take_err_bits(Ctx& c)
+{
+    unsigned bits = 0;
+    cudaStreamSynchronize(c.stream);
+    cudaMemcpy(&bits, c.d_err, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    if (bits) {
+        cudaMemsetAsync(c.d_err, 0, sizeof(unsigned), c.stream);
+        cudaStreamSynchronize(c.stream);
+    }
+    return bits;
+}
+
+template <class F>
+float time_ms(Ctx& c, F fn, int reps)
+{
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int r = 0; r < reps; ++r) {
+        cudaEventRecord(e0, c.stream);
+        fn();
+        cudaEventRecord(e1, c.stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        best = std::min(best, ms);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return best;
+}
+
+int autotune_impl(Ctx& c)
+{
+    const int base_pre = c.dim == 1 ? 128 : c.dim == 2 ? 512 : 1024;
+    const int base_fluid = c.dim == 1 ? 128 : c.dim == 2 ? 384 : 1024;
+    const double fr[4] = {0.5, 0.75, 1.0, 1.5};
+    pre_inputs(c, 0);
+    float best_total = 1e30f;
+    int best_gw = c.gw_pre, best_tp = base_pre, best_tf = base_fluid;
+    for (int gw = 1; gw <= 2; ++gw) {
+        if (32 * gw > 32 * 8) break;
+        c.gw_pre = gw;
+        if (build_groups(c) != SPHGPU_OK) break;
+        launch_make_tree(c, true);   // same positions: an identity reorder, new group split
+        float bp = 1e30f, bf = 1e30f;
+        int tp = base_pre, tf = base_fluid;
+        for (double f : fr) {
+            const int cap = std::max(32, (int)(base_pre * f) / 32 * 32);
+            c.tile_cap_pre = cap;
+            const float ms = time_ms(c, [&] { pre_inputs(c, 1); launch_pre(c, false); }, 2);
+            const unsigned bad = take_err_bits(c);
+            if (bad) c.tune_rejects |= bad;
+            else if (ms < bp) { bp = ms; tp = cap; }
+        }
+        c.tile_cap_pre = tp;
+        pre_inputs(c, 1);
+        launch_pre(c, false);
+        launch_set_kernel_size(c);
+        for (double f : fr) {
+            const int cap = std::max(32, (int)(base_fluid * f) / 32 * 32);
+            c.tile_cap = cap;
+            const float ms = time_ms(c, [&] { launch_fluid(c); }, 2);
+            const unsigned bad = take_err_bits(c);
+            if (bad) c.tune_rejects |= bad;
+            else if (ms < bf) { bf = ms; tf = cap; }
+        }
+        if (bp + bf < best_total) { best_total = bp + bf; best_gw = gw; best_tp = tp; best_tf = tf; }
+    }
+    c.gw_pre = best_gw;
+    c.tile_cap_pre = best_tp;
+    c.tile_cap = best_tf;
+    int rc = build_groups(c);
+    if (rc != SPHGPU_OK) return rc;
+    launch_make_tree(c, true);
+    pre_inputs(c, 1);
+    c.tuned = true;
+    return SPHGPU_OK;
+}
+
 void run_step(Ctx& c, bool timed)
 {
     cudaStream_t s = c.stream;
@@ -434,9 +545,15 @@ void run_step(Ctx& c, bool timed)
     launch_make_tree(c, false);
     if (timed) cudaEventRecord(c.ev[2], s);
     run_pre_stage(c);
-    if (timed) cudaEventRecord(c.ev[3], s);
+    if (timed) {
+        cudaEventRecord(c.ev[3], s);
+        cudaMemcpyAsync(&c.stage_ovf[0], c.d_work + 1, sizeof(int), cudaMemcpyDeviceToHost, s);
+    }
     launch_fluid(c);
-    if (timed) cudaEventRecord(c.ev[4], s);
+    if (timed) {
+        cudaEventRecord(c.ev[4], s);
+        cudaMemcpyAsync(&c.stage_ovf[1], c.d_work + 1, sizeof(int), cudaMemcpyDeviceToHost, s);
+    }
     if (c.p.use_gravity) launch_gravity(c);
     if (timed) cudaEventRecord(c.ev[5], s);
     launch_correct(c);
@@ -548,7 +665,6 @@ int sphgpu_set_field(sphgpu_ctx* h, int field, const double* host)
         sphgpu::field_map(c.st, slot, width, c.dim), c.st.id, c.n, c.d_stage);
     if (field == SPHGPU_POS || field == SPHGPU_MASS) c.tree_valid = false;   // node boxes and moments
     if (field == SPHGPU_SML) c.kernel_size_valid = false;                    // node kernel sizes
-    c.graph_valid = false;
     return sphgpu::finish(c, "set_field");
 }
 
@@ -604,7 +720,6 @@ int sphgpu_upload_aos(sphgpu_ctx* h, const void* base, const sphgpu_aos_layout* 
     sphgpu::aos_upload_kernel<<<sphgpu::ceil_div(c.n, 256), 256, 0, c.stream>>>(c.st, m, c.d_aos, c.n);
     c.tree_valid = false;
     c.kernel_size_valid = false;
-    c.graph_valid = false;
     return sphgpu::finish(c, "upload_aos");
 }
 
@@ -651,12 +766,14 @@ int sphgpu_set_scalar(sphgpu_ctx* h, int which, int run, double value)
     CTX_OR_FAIL(h);
     if (run < 0 || run >= c.R) return SPHGPU_ERR_ARG;
     cudaError_t e = cudaSuccess;
-    if (which == SPHGPU_TIME) e = cudaMemcpy(c.d_time + run, &value, sizeof(double), cudaMemcpyHostToDevice);
-    else if (which == SPHGPU_DT) e = cudaMemcpy(c.d_dt + run, &value, sizeof(double), cudaMemcpyHostToDevice);
+    // stream-ordered (the library's stream does not synchronise with the legacy default stream)
+    if (which == SPHGPU_TIME) e = cudaMemcpyAsync(c.d_time + run, &value, sizeof(double), cudaMemcpyHostToDevice, c.stream);
+    else if (which == SPHGPU_DT) e = cudaMemcpyAsync(c.d_dt + run, &value, sizeof(double), cudaMemcpyHostToDevice, c.stream);
     else if (which == SPHGPU_H_PER_V_SIG) {
         const long long o = sphgpu::host_dbl_to_ord(value);
-        e = cudaMemcpy(c.d_hvs + run, &o, sizeof(long long), cudaMemcpyHostToDevice);
+        e = cudaMemcpyAsync(c.d_hvs + run, &o, sizeof(long long), cudaMemcpyHostToDevice, c.stream);
     } else return SPHGPU_ERR_ARG;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
     return sphgpu::cuda_status(c, e, "set_scalar");
 }
 
@@ -706,6 +823,7 @@ int sphgpu_gravity_force(sphgpu_ctx* h)
     CTX_OR_FAIL(h);
     if (!c.p.use_gravity) return SPHGPU_OK;   // GravityForce::calculation returns at once
     if (!c.tree_valid) { c.last_error = "gravity_force before make_tree"; return SPHGPU_ERR_STATE; }
+    if (!c.kernel_size_valid) sphgpu::launch_set_kernel_size(c);
     sphgpu::launch_gravity(c);
     return sphgpu::finish(c, "gravity_force");
 }
@@ -738,6 +856,12 @@ int sphgpu_initialize(sphgpu_ctx* h)
     sphgpu::launch_init_fields(c);
     sphgpu::launch_make_tree(c, true);
     c.first_pre = true;
+    if (c.autotune && !c.tuned) {
+        sphgpu::launch_pre(c, true);   // initial smoothing once; the tuner's trials start after it
+        c.first_pre = false;
+        const int rc = sphgpu::autotune_impl(c);
+        if (rc != SPHGPU_OK) return rc;
+    }
     sphgpu::run_pre_stage(c);
     sphgpu::launch_fluid(c);
     if (c.p.use_gravity) sphgpu::launch_gravity(c);
@@ -817,7 +941,7 @@ int sphgpu_neighbors(sphgpu_ctx* h, int is_ij, int* counts, int* list, int cap)
     CTX_OR_FAIL(h);
     if (!counts || (list && cap < 1) || (!list && cap != 0)) return SPHGPU_ERR_ARG;
     if (!c.tree_valid) sphgpu::launch_make_tree(c, true);
-    if (is_ij && !c.kernel_size_valid) sphgpu::launch_set_kernel_size(c);
+    if (!c.kernel_size_valid) sphgpu::launch_set_kernel_size(c);
     int *dc = nullptr, *dl = nullptr;
     cudaError_t e = cudaMalloc((void**)&dc, sizeof(int) * c.n);
     if (e == cudaSuccess && list) e = cudaMalloc((void**)&dl, sizeof(int) * (size_t)c.n * cap);
@@ -895,12 +1019,15 @@ int sphgpu_set_tuning(sphgpu_ctx* h, int which, int value)
 {
     CTX_OR_FAIL(h);
     switch (which) {
-    case 0:
+    case 0: {
         if (value < 1 || value > 8) return SPHGPU_ERR_ARG;
+        cudaStreamSynchronize(c.stream);
         c.gw_pre = value;
-        c.tree_valid = false;
-        c.kernel_size_valid = false;
+        c.autotune = 0;   // an explicit schedule replaces the tuner's choice
+        const int rc = sphgpu::build_groups(c);
+        if (rc != SPHGPU_OK) return rc;
         break;
+    }
     case 1: case 2:
         if (value < 1 || value > 8) return SPHGPU_ERR_ARG;
         if (which == 1) c.gw_fluid = value; else c.gw_grav = value;
@@ -908,6 +1035,12 @@ int sphgpu_set_tuning(sphgpu_ctx* h, int which, int value)
     case 3:
         if (value < 0 || (value % 32) != 0 || value > 16384) return SPHGPU_ERR_ARG;
         c.tile_cap = value;
+        c.autotune = 0;
+        break;
+    case 10:
+        if (value < 0 || (value % 32) != 0 || value > 16384) return SPHGPU_ERR_ARG;
+        c.tile_cap_pre = value;
+        c.autotune = 0;
         break;
     case 4: c.autotune = value != 0; break;
     case 5: c.timing = value != 0; break;
@@ -932,6 +1065,10 @@ int sphgpu_get_tuning(sphgpu_ctx* h, int which, int* value)
     case 5: *value = c.timing; break;
     case 6: *value = c.use_graph; break;
     case 7: *value = c.graph_kernels; break;
+    case 8: *value = c.stage_ovf[0]; break;
+    case 9: *value = c.stage_ovf[1]; break;
+    case 10: *value = c.tile_cap_pre; break;
+    case 11: *value = (int)c.tune_rejects; break;
     default: return SPHGPU_ERR_ARG;
     }
     return SPHGPU_OK;

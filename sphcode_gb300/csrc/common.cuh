@@ -71,11 +71,17 @@ struct TreeView {
     const double* mass;
     const double* com[3];
     const double* ksize;
+    // FP32 copies for the superset walk of the pair kernels: centres rounded to nearest, edge
+    // and kernel size rounded up
+    const float* cf[3];
+    const float* ef;
+    const float* kf;
 };
 
 struct Periodic {
     int on;
     double lo[3], hi[3], len[3];
+    float lenf[3];
 };
 
 // ------------------------------------------------------------------------------------------
@@ -114,6 +120,14 @@ __device__ __forceinline__ double min_image(double d, const Periodic& pb, int k)
     const double half = 0.5 * pb.len[k];
     if (d > half) d -= pb.len[k];
     else if (d < -half) d += pb.len[k];
+    return d;
+}
+__device__ __forceinline__ float min_image_f(float d, const Periodic& pb, int k)
+{
+    if (!pb.on) return d;
+    const float half = 0.5f * pb.lenf[k];
+    if (d > half) d -= pb.lenf[k];
+    else if (d < -half) d += pb.lenf[k];
     return d;
 }
 
@@ -163,55 +177,60 @@ __device__ __forceinline__ T powD(T h)
 template <typename T>
 __device__ __forceinline__ T pos_part(T x) { return x > T(0) ? x : T(0); }
 
-// W(r, h), dW/dh and the scalar c of grad W = r_ij * c.
+// W(r, h), dW/dh and the scalar c of grad W = r_ij * c, given hinv = 1/h (and rinv = 1/r for
+// the gradient), so that a pair costs multiplications only.
 template <int D, int K, typename T>
 struct Kern {
-    static __device__ __forceinline__ T w(T r, T h)
+    static __device__ __forceinline__ T w(T r, T hinv)
     {
         if (K == 0) {
-            const T hh = h * T(0.5);
-            const T q = r / hh;
+            const T hh = T(2) * hinv;                 // 1 / (h / 2)
+            const T q = r * hh;
             const T a = pos_part(T(2) - q), b = pos_part(T(1) - q);
-            return T(Sigma<D>::cubic) / powD<D>(hh) * (T(0.25) * (a * a * a) - b * b * b);
+            return T(Sigma<D>::cubic) * powD<D>(hh) * (T(0.25) * (a * a * a) - b * b * b);
         } else {
-            const T q = r / h;
+            const T q = r * hinv;
             const T a = pos_part(T(1) - q);
             const T a2 = a * a;
-            return T(Sigma<D>::c4) / powD<D>(h) * (a2 * a2 * a2) * (T(1) + T(6) * q + T(35.0 / 3.0) * q * q);
+            return T(Sigma<D>::c4) * powD<D>(hinv) * (a2 * a2 * a2) * (T(1) + T(6) * q + T(35.0 / 3.0) * q * q);
         }
     }
-    static __device__ __forceinline__ T dhw(T r, T h)
+    static __device__ __forceinline__ T dhw(T r, T hinv)
     {
         if (K == 0) {
-            const T hh = h * T(0.5);
-            const T q = r / hh;
+            const T hh = T(2) * hinv;
+            const T q = r * hh;
             const T a = pos_part(T(2) - q), b = pos_part(T(1) - q);
-            return T(0.5 * Sigma<D>::cubic) / (powD<D>(hh) * hh)
+            return T(0.5 * Sigma<D>::cubic) * (powD<D>(hh) * hh)
                  * (a * a * (T((3.0 + D) * 0.25) * q - T(0.5 * D)) + b * b * (T(-3.0 - D) * q + T(D)));
         } else {
-            const T q = r / h;
+            const T q = r * hinv;
             const T a = pos_part(T(1) - q);
             const T a2 = a * a;
-            return T(-Sigma<D>::c4 / 3.0) / (powD<D>(h) * h) * (a2 * a2 * a)
+            return T(-Sigma<D>::c4 / 3.0) * (powD<D>(hinv) * hinv) * (a2 * a2 * a)
                  * (T(3.0 * D) + T(15.0 * D) * q + T(-56.0 + 17.0 * D) * q * q - T(35.0 * (8.0 + D)) * (q * q * q));
         }
     }
-    static __device__ __forceinline__ T dw_coef(T r, T h)
+    static __device__ __forceinline__ T dw_coef(T r, T rinv, T hinv)
     {
         if (K == 0) {
-            if (r == T(0)) return T(0);
-            const T hh = h * T(0.5);
-            const T q = r / hh;
+            if (r == T(0)) return T(0);             // the cubic spline's dw returns 0 at r = 0
+            const T hh = T(2) * hinv;
+            const T q = r * hh;
             const T a = pos_part(T(2) - q), b = pos_part(T(1) - q);
-            return T(-Sigma<D>::cubic) / (powD<D>(hh) * hh * r) * (T(0.75) * a * a - T(3) * b * b);
+            return T(-Sigma<D>::cubic) * (powD<D>(hh) * hh) * rinv * (T(0.75) * a * a - T(3) * b * b);
         } else {
-            const T q = r / h;
+            const T q = r * hinv;
             const T a = pos_part(T(1) - q);
             const T a2 = a * a;
-            return T(-56.0 / 3.0 * Sigma<D>::c4) / (powD<D>(h) * h * h) * (a2 * a2 * a) * (T(1) + T(5) * q);
+            return T(-56.0 / 3.0 * Sigma<D>::c4) * (powD<D>(hinv) * hinv * hinv) * (a2 * a2 * a) * (T(1) + T(5) * q);
         }
     }
 };
+
+// 1/sqrt in T (the FP32 pair kernels are compiled with approximate division and square root).
+__device__ __forceinline__ float rsqrt_t(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double rsqrt_t(double x) { return 1.0 / sqrt(x); }
 
 // Dimension constant A_D (src/pre_interaction.cpp:61-63).
 template <int D>

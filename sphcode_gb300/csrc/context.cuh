@@ -42,18 +42,23 @@ struct Ctx {
     int *nd_parent = nullptr, *nd_level = nullptr, *nd_arrive = nullptr;
     double *nd_center[3] = {nullptr, nullptr, nullptr}, *nd_edge = nullptr, *nd_mass = nullptr;
     double *nd_com[3] = {nullptr, nullptr, nullptr}, *nd_ksize = nullptr;
+    float *nd_cf[3] = {nullptr, nullptr, nullptr}, *nd_ef = nullptr, *nd_kf = nullptr;
     int* lvl_start = nullptr;       // device, MAX_LEVELS + 2 entries
     int* lvl_tmp = nullptr;         // per-node child counts of the frontier
     int* chunk_sum = nullptr;       // per-1024-node chunk sums
     long long* bbox = nullptr;      // per run: D mins then D maxs (ordered-int images)
     int* node_total = nullptr;      // device: number of nodes built
 
-    // target groups
-    int group_threads = 32;         // group size used to build the current group list
+    // target groups: fixed chunks of group_threads key-consecutive particles of one run
+    int group_threads = 32;         // group size of the current group list
     int* g_begin = nullptr;
     int* g_count = nullptr;
-    int* n_groups = nullptr;        // device counter
+    int* n_groups = nullptr;        // device copy of the group count (2 per chunk)
     int max_groups = 0;
+    int num_groups = 0;
+    int* ck_begin = nullptr;        // fixed chunks of group_threads particles per run
+    int* ck_count = nullptr;
+    int num_chunks = 0;
 
     // per-run scalars on the device
     double* d_time = nullptr;
@@ -64,11 +69,14 @@ struct Ctx {
     unsigned* d_err = nullptr;      // status bits
     int* d_newton_fail = nullptr;
 
-    // key-ordered mirrors of source fields in the pair type (sized for FP64)
+    // key-ordered mirrors of source fields in the pair type (sized for FP64):
+    // 0 Pre {v, c}, 1 Pre u, 2-4 Fluid records, 5 gsph gradients,
+    // 6 {x - leaf centre, m} (tree build), 7 h (end of PreInteraction)
     void* mir[16] = {nullptr};
     // persistent-kernel work counters and the overflow group list
-    int* d_work = nullptr;          // 16 counters
-    int* d_ovf_list = nullptr;      // max_groups entries
+    int* d_work = nullptr;          // 16 counters (pair-kernel passes: [0] [2] [4] work, [1] [3] overflow)
+    int* d_ovf_list = nullptr;      // max_groups entries: groups left by the first pass
+    int* d_ovf_list2 = nullptr;     // max_groups entries: groups left by the second pass
 
     // staging buffer for field transfers
     double* d_stage = nullptr;
@@ -88,6 +96,7 @@ struct Ctx {
     int tile_cap = 0;               // 0 = automatic
     int autotune = 1;
     bool tuned = false;
+    unsigned tune_rejects = 0;      // status bits of tuning candidates that were rejected
 
     // CUDA graph of one integrate() step
     cudaGraphExec_t graph = nullptr;
@@ -100,6 +109,8 @@ struct Ctx {
     cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     bool timing = false;
     double stage_ms[5] = {0, 0, 0, 0, 0};
+    int stage_ovf[2] = {0, 0};      // groups sent to the overflow pass by Pre / Fluid (timing mode)
+    int tile_cap_pre = 0;           // per-stage source tile capacities (0 = automatic)
 
     std::string last_error;
 };
@@ -112,6 +123,7 @@ void launch_set_kernel_size(Ctx& c);
 void launch_node_moments(Ctx& c);
 TreeView tree_view(const Ctx& c);
 void launch_reorder_fields(Ctx& c, bool all);
+int build_groups(Ctx& c);          // host: fixed chunks per run, uploaded to the device
 
 // ---- pre_dD.cu / fluid_dD.cu / gravity.cu
 template <int D>
@@ -139,16 +151,49 @@ int kernel_occupancy(const void* kern, int threads, size_t smem);
 void reset_work_counters(Ctx& c);
 void set_global_error(const std::string& text);   // text of sphgpu_last_error(NULL)
 
+// Three passes of a CTA-per-group pair kernel over the group list.  Pass 1 runs every group with
+// the tuned capacities at full occupancy and lists those that do not fit; pass 2 runs that list
+// with 4x the tile and larger walk capacities, still at full occupancy; pass 3 runs what is left
+// with the largest tile the shared memory holds, one CTA per SM; a group that fits nowhere sets
+// the capacity error bit.  Args must carry `L` (SmemLayout) and `work` (GroupWork).
+template <class Args>
+void launch_three_pass(Ctx& c, const void* kern, Args& a, int tcap, int elt4, int eltT,
+                       void (*launch)(const void*, int, int, size_t, cudaStream_t, Args&));
+
 // The largest source tile that fits the opt-in shared memory next to the walk capacities of the
 // overflow pass.
-inline int big_tile_cap(const Ctx& c, int gt, int elt4, int stack_cap, int leaf_cap)
+inline int big_tile_cap(const Ctx& c, int gt, int elt4, int eltT, int stack_cap, int leaf_cap)
 {
-    const SmemLayout L0 = make_layout(gt, 0, elt4, stack_cap, leaf_cap);
-    const size_t per = (size_t)elt4 + sizeof(int) + (size_t)gt / 8;
+    const SmemLayout L0 = make_layout(gt, 0, elt4, eltT, stack_cap, leaf_cap);
+    const size_t per = (size_t)elt4 + (size_t)eltT + sizeof(int) + (size_t)gt / 8;
     size_t cap = ((size_t)max_optin_smem(c) - L0.total - 64) / per;
     cap = cap / 32 * 32;
     if (cap > 16384) cap = 16384;
     return (int)cap;
+}
+
+template <class Args>
+void launch_three_pass(Ctx& c, const void* kern, Args& a, int tcap, int elt4, int eltT,
+                       void (*launch)(const void*, int, int, size_t, cudaStream_t, Args&))
+{
+    const int gt = c.group_threads;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, max_optin_smem(c));
+    const int big = big_tile_cap(c, gt, elt4, eltT, 1024, 1024);
+    // pass 1
+    a.L = make_layout(gt, std::min(tcap, big), elt4, eltT, 128, 96);
+    a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 0, nullptr, nullptr,
+                       c.d_ovf_list, c.d_work + 1, c.d_err};
+    launch(kern, std::max(1, kernel_occupancy(kern, gt, a.L.total)) * c.num_sms, gt, a.L.total, c.stream, a);
+    // pass 2
+    a.L = make_layout(gt, std::min(4 * tcap, big), elt4, eltT, 512, 512);
+    a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 2, c.d_ovf_list, c.d_work + 1,
+                       c.d_ovf_list2, c.d_work + 3, c.d_err};
+    launch(kern, std::max(1, kernel_occupancy(kern, gt, a.L.total)) * c.num_sms, gt, a.L.total, c.stream, a);
+    // pass 3
+    a.L = make_layout(gt, big, elt4, eltT, 1024, 1024);
+    a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 4, c.d_ovf_list2, c.d_work + 3,
+                       nullptr, nullptr, c.d_err};
+    launch(kern, c.num_sms, gt, a.L.total, c.stream, a);
 }
 
 }  // namespace sphgpu

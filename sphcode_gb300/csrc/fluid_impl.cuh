@@ -24,7 +24,9 @@ struct FluidArgs {
     Periodic pb;
     SmemLayout L;
     GroupWork work;
-    const V4* rec0;   // {vx, vy, vz, h}
+    const V4* xrel;   // {x - leaf centre, m}
+    const T* hmir;    // h
+    const V4* rec0;   // {vx, vy, vz, 1/h}
     const V4* rec1;   // {rho, P, c, X}   X: ssph P/rho^2 gradh, disph gradh, gsph 0
     const V4* rec2;   // {alpha, balsara, u, Y}   Y: disph u/P
     const T* grad;    // gsph: 16 per particle, grad rho [0,D), grad P [3,3+D), grad v [6 + 3k + d]
@@ -75,11 +77,13 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
     const Tile<T> tile = tile_of<T>(smem, L);
     const State& st = a.st;
     const int t = threadIdx.x;
+    const int GT = blockDim.x;
 
     for (;;) {
         const int g = next_group(gm, a.work);
         if (g < 0) break;
         const int gb = a.work.g_begin[g], gn = a.work.g_count[g];
+        if (gn == 0) continue;   // the unused half of an unsplit chunk
         const bool active = t < gn;
         const int i = gb + (active ? t : 0);
         double xi[D];
@@ -88,36 +92,38 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
         const double hi = st.f[F_SML][i];
         group_box<D>(gm, xi, active, hi, a.pb);
         const int run = st.run[gb];
-        if (!group_walk<D>(smem, L, gm, a.tv, run, true, a.pb)) { report_overflow(a.work, g); continue; }
+        if (!group_walk<D, T>(smem, L, gm, a.tv, run, true, a.pb)) { report_overflow(a.work, g); continue; }
         {
-            const double R = gm->R;
-            double he[D];
+            // keep sources within max(R, h_j) of the group box per axis
+            const double u = Unit<T>::u;
+            const T Rt = to_T_up<T>(gm->R);
+            const T rel = (T)(1.0 + 8.0 * u), slack = to_T_up<T>(4.0 * u * gm->bmax + 1e-300);
+            T he[D];
 #pragma unroll
-            for (int k = 0; k < D; ++k) he[k] = gm->he[k];
-            const int ntile = stage_sources<D, T>(smem, L, gm, st, a.pb, tile, [&](int j, const double* off) {
-                const double r = fmax(R, st.f[F_SML][j]);
+            for (int k = 0; k < D; ++k) he[k] = to_T_up<T>(gm->he[k]);
+            const T* hmir = a.hmir;
+            const int ntile = stage_sources<D, T>(smem, L, gm, a.xrel, tile, [&](int j, const T* off) {
+                const T hj = hmir[j];
+                const T r = Rt > hj ? Rt : hj;
 #pragma unroll
                 for (int k = 0; k < D; ++k)
-                    if (fabs(off[k]) > (he[k] + r) * (1.0 + 1e-12)) return false;
+                    if (fabs(off[k]) > (he[k] + r) * rel + slack) return false;
                 return true;
-            }, [&](int j) { return (T)st.f[F_MASS][j]; });
+            }, [&](int j) { return a.rec0[j].w; });
             if (ntile < 0) { report_overflow(a.work, g); continue; }
             gm->ntile = ntile;
         }
         const int ntile = gm->ntile;
+        const int nw = (ntile + 31) >> 5;
 
-        // Relative guard band of the T-precision test r^2 < H^2 for H >= h_min of the group:
-        // |r2_T - r2| <= 2 r E + D E^2 + 2u r^2 with E <= u (2 he + 3 H) + FP64 rounding of the
-        // offsets; at r ~ H this is below delta * H^2.
+        // Relative guard band of the T-precision test r^2 < H^2 for H = max(h_i, h_j) >= h_min
+        // of the group: the component error E (comp_err) at separations ~H is below e_rel H, so
+        // |r2_T - r2| < delta H^2 there.
         double delta;
         {
-            double hem = 0.0;
-#pragma unroll
-            for (int k = 0; k < D; ++k) hem = fmax(hem, gm->he[k]);
-            const double u = Unit<T>::u, u64 = Unit<double>::u;
             const double hm = gm->rmin;
-            const double e_rel = u * (2.0 * hem / hm + 3.0) * 1.5 + 8.0 * u64 * (gm->scale / hm + 1.0);
-            delta = 2.0 * (2.0 * 1.7320508075688772 * e_rel + D * e_rel * e_rel + 8.0 * u);
+            const double e_rel = comp_err<T>(gm, hm) / hm + Unit<T>::u * 3.0;
+            delta = 2.0 * (2.0 * 1.7320508075688772 * e_rel + D * e_rel * e_rel + 8.0 * Unit<T>::u);
         }
         const T dlo = (T)(1.0 - delta), dhi = (T)(1.0 + delta);
 
@@ -126,7 +132,23 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
         for (int k = 0; k < D; ++k) xo[k] = (T)min_image(xi[k] - gm->gc[k], a.pb, k);
         const V4 r0i = a.rec0[i], r1i = a.rec1[i], r2i = a.rec2[i];
         const T vi[3] = {r0i.x, r0i.y, r0i.z};
-        const T hiT = r0i.w;
+        const T hinv_i = r0i.w;
+
+        // ---- pair candidates: r^2 < max(h_i, h_j)^2 (1 + delta), j != i ----
+        for (int w = 0; w < nw; ++w) {
+            unsigned bits = 0;
+            const int smax = min(32, ntile - w * 32);
+            for (int b = 0; b < smax; ++b) {
+                const int s = w * 32 + b;
+                T r[D];
+                const T r2 = tile_r2<D, T>(xo, tile.pm[s], r);
+                const T hinv_j = tile.aux[s];
+                const T Hinv = hinv_i < hinv_j ? hinv_i : hinv_j;   // 1 / max(h_i, h_j)
+                if (r2 * (Hinv * Hinv) < dhi) bits |= 1u << b;
+            }
+            tile.mask[w * GT + t] = active ? bits : 0u;
+        }
+
         const T rho_i = r1i.x, p_i = r1i.y, c_i = r1i.z, X_i = r1i.w;
         const T al_i = r2i.x, b_i = r2i.y, u_i = r2i.z;
         const T m_i = (T)st.f[F_MASS][i];
@@ -150,33 +172,34 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
         for (int k = 0; k < D; ++k) acc[k].zero();
         dene.zero();
 
-        if (active) {
-            for (int s = 0; s < ntile; ++s) {
+        MaskIter it(tile.mask, GT, t, nw);
+        int s;
+        while (it.next(s)) {
+            {
                 const V4 p = tile.pm[s];
                 T rv[D];
                 const T r2 = tile_r2<D, T>(xo, p, rv);
                 const int j = tile.idx[s];
-                const V4 r0j = a.rec0[j];
-                const T hj = r0j.w;
-                const T H = hiT > hj ? hiT : hj;
-                const T H2 = H * H;
-                if (r2 >= H2 * dhi) continue;
                 if (j == i) continue;
-                if (!(r2 < H2 * dlo) || r2 == T(0)) {
+                const T hinv_j = tile.aux[s];
+                const T Hinv = hinv_i < hinv_j ? hinv_i : hinv_j;
+                if (!(r2 * (Hinv * Hinv) < dlo) || r2 == T(0)) {
                     const double r2x = exact_r2<D>(st, xi, j, a.pb);
                     const double rx = __dsqrt_rn(r2x);
                     if (rx >= fmax(hi, st.f[F_SML][j]) || rx == 0.0) continue;
                     if (r2 == T(0)) continue;   // unresolvable in T (coincident offsets)
                 }
-                const T r = sqrt(r2);
-                const T cfi = KF::dw_coef(r, hiT);
-                const T cfj = KF::dw_coef(r, hj);
+                const V4 r0j = a.rec0[j];
+                const T rinv = rsqrt_t(r2);
+                const T r = r2 * rinv;
+                const T cfi = KF::dw_coef(r, rinv, hinv_i);
+                const T cfj = KF::dw_coef(r, rinv, hinv_j);
                 const V4 r1j = a.rec1[j];
                 const T mj = p.w;
                 if (TYPE == 2) {
                     // ---- Godunov SPH pair (src/gsph/g_fluid_force.cpp:79-163) ----
                     const T rho_j = r1j.x, p_j = r1j.y, c_j = r1j.z;
-                    const T r_inv = T(1) / r;
+                    const T r_inv = rinv;
                     T e[D];
 #pragma unroll
                     for (int k = 0; k < D; ++k) e[k] = rv[k] * r_inv;
@@ -246,7 +269,7 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
                     if (vr < T(0)) {
                         const T alpha = T(0.5) * (al_i + r2j.x);
                         const T bal = T(0.5) * (b_i + r2j.y);
-                        const T w = vr / r;
+                        const T w = vr * rinv;
                         const T vsig = c_i + c_j - T(3) * w;
                         const T rho_ij_inv = T(2) / (rho_i + rho_j);
                         pi_ij = T(-0.5) * bal * alpha * vsig * w * rho_ij_inv;
@@ -255,8 +278,8 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
                     T ac = T(0);
                     if (a.use_ac) {
                         // Wadsley et al. (2008) / Price (2008) (src/fluid_force.cpp:108-116)
-                        const T vs = a.ac_gravity ? fabs(vr / r) : sqrt(T(2) * fabs(p_i - p_j) / (rho_i + rho_j));
-                        ac = alpha_ac * mj * vs * (u_i - r2j.z) * (cfij * r2) / r;
+                        const T vs = a.ac_gravity ? fabs(vr * rinv) : sqrt(T(2) * fabs(p_i - p_j) / (rho_i + rho_j));
+                        ac = alpha_ac * mj * vs * (u_i - r2j.z) * (cfij * r);
                     }
                     T ai, aj, de_p;
                     if (TYPE == 0) {
@@ -299,7 +322,7 @@ __global__ void fluid_mirror_kernel(State st, int n, typename Vec4<T>::type* rec
     v.x = (T)st.f[F_VEL][i];
     v.y = D > 1 ? (T)st.f[F_VEL + (D > 1 ? 1 : 0)][i] : T(0);
     v.z = D > 2 ? (T)st.f[F_VEL + (D > 2 ? 2 : 0)][i] : T(0);
-    v.w = (T)st.f[F_SML][i];
+    v.w = (T)(1.0 / st.f[F_SML][i]);
     rec0[i] = v;
     const double rho = st.f[F_DENS][i], p = st.f[F_PRES][i];
     typename Vec4<T>::type b;
@@ -335,7 +358,7 @@ __global__ void fluid_mirror_kernel(State st, int n, typename Vec4<T>::type* rec
 namespace sphgpu {
 
 template <int D>
-constexpr int fluid_default_tile_cap() { return D == 1 ? 128 : D == 2 ? 512 : 1024; }
+constexpr int fluid_default_tile_cap() { return D == 1 ? 128 : D == 2 ? 384 : 1024; }
 
 template <int D, typename T, int TYPE, int K>
 void run_fluid(Ctx& c)
@@ -353,6 +376,8 @@ void run_fluid(Ctx& c)
     a.st = c.st;
     a.tv = tree_view(c);
     a.pb = c.pb;
+    a.xrel = (const V4*)c.mir[6];
+    a.hmir = (const T*)c.mir[7];
     a.rec0 = rec0;
     a.rec1 = rec1;
     a.rec2 = rec2;
@@ -363,19 +388,11 @@ void run_fluid(Ctx& c)
     a.alpha_ac = c.p.alpha_ac;
     a.gsph_2nd = c.p.gsph_2nd_order;
     a.dt_run = c.d_dt;
-    const int gt = c.group_threads;
     const int tcap = c.tile_cap ? c.tile_cap : fluid_default_tile_cap<D>();
-    a.L = make_layout(gt, tcap, sizeof(V4), 256, 256);
-    a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 0, nullptr, nullptr,
-                       c.d_ovf_list, c.d_work + 1, c.d_err};
-    cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, max_optin_smem(c));
-    const int nb = std::max(1, kernel_occupancy((const void*)kern, gt, a.L.total));
-    kern<<<nb * c.num_sms, gt, a.L.total, s>>>(a);
-    const int big = big_tile_cap(c, gt, sizeof(V4), 1024, 2048);
-    a.L = make_layout(gt, big, sizeof(V4), 1024, 2048);
-    a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 2, c.d_ovf_list, c.d_work + 1,
-                       nullptr, nullptr, c.d_err};
-    kern<<<c.num_sms, gt, a.L.total, s>>>(a);
+    launch_three_pass<FluidArgs<T>>(c, (const void*)kern, a, tcap, sizeof(V4), sizeof(T),
+        [](const void* k, int grid, int block, size_t smem, cudaStream_t st, FluidArgs<T>& args) {
+            reinterpret_cast<void (*)(FluidArgs<T>)>(const_cast<void*>(k))<<<grid, block, smem, st>>>(args);
+        });
 }
 
 }  // namespace sphgpu

@@ -28,8 +28,8 @@ struct GravArgs {
     TreeView tv;
     Periodic pb;
     GroupWork work;
-    const V4* grel;   // {x_j - centre of j's leaf (T), m_j}
-    const T* gh;      // h_j
+    const V4* grel;   // {x_j - centre of j's leaf (T), m_j}: built with the tree
+    const T* gh;      // h_j in T: built at the end of PreInteraction
     double G;
     double theta2;
     int stack_cap;
@@ -196,30 +196,6 @@ __global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
     }
 }
 
-// Leaf-relative offsets and softening lengths of every particle, in T.
-template <int D, typename T>
-__global__ void gravity_mirror_kernel(State st, const int* node_total_p, TreeView tv,
-                                      typename Vec4<T>::type* grel, T* gh)
-{
-    const int total = *node_total_p;
-    for (int nd = blockIdx.x * blockDim.x + threadIdx.x; nd < total; nd += gridDim.x * blockDim.x) {
-        if (tv.first_child[nd] >= 0) continue;
-        const int b = tv.begin[nd], e = b + tv.count[nd];
-        double c[D];
-#pragma unroll
-        for (int k = 0; k < D; ++k) c[k] = tv.center[k][nd];
-        for (int j = b; j < e; ++j) {
-            typename Vec4<T>::type q;
-            q.x = (T)(st.f[F_POS][j] - c[0]);
-            q.y = D > 1 ? (T)(st.f[F_POS + (D > 1 ? 1 : 0)][j] - c[D > 1 ? 1 : 0]) : T(0);
-            q.z = D > 2 ? (T)(st.f[F_POS + (D > 2 ? 2 : 0)][j] - c[D > 2 ? 2 : 0]) : T(0);
-            q.w = (T)st.f[F_MASS][j];
-            grel[j] = q;
-            gh[j] = (T)st.f[F_SML][j];
-        }
-    }
-}
-
 template <int D, typename T>
 void run_gravity(Ctx& c)
 {
@@ -228,8 +204,6 @@ void run_gravity(Ctx& c)
     V4* grel = (V4*)c.mir[6];
     T* gh = (T*)c.mir[7];
     TreeView tv = tree_view(c);
-    if (sizeof(T) == 4)
-        gravity_mirror_kernel<D, T><<<c.num_sms * 8, 256, 0, s>>>(c.st, c.node_total, tv, grel, gh);
     reset_work_counters(c);
     GravArgs<T> a{};
     a.st = c.st;

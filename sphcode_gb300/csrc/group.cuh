@@ -1,19 +1,22 @@
 // Group machinery shared by the pair kernels (PreInteraction, FluidForce, neighbour export).
 //
-// A CTA owns one target group at a time: up to blockDim.x consecutive key-ordered particles
-// that the tree keeps spatially compact.  For each group the CTA
-//   1. reduces the group's bounding box in FP64 (centre gc, half extent he),
-//   2. walks the octree once with one warp, keeping every leaf whose box intersects the box
-//      grown by the search radius (a superset of the reference's per-particle walks,
-//      src/bhtree.cpp:234-270),
+// A CTA owns one target group at a time: G key-consecutive particles of one run (a fixed chunk
+// of the key order, which the octree keeps spatially compact).  For each group the CTA
+//   1. reduces the group's bounding box in FP64 (centre gc, half extent he) and the search
+//      radius R = max over targets,
+//   2. walks the octree once with one warp in FP32 with conservative margins, keeping every
+//      leaf whose box can intersect the box grown by the search radius (a superset of the
+//      reference's per-particle walks, src/bhtree.cpp:234-270); for each kept leaf it forms the
+//      offset of the leaf centre from gc once in FP64,
 //   3. stages the particles of those leaves that can be in reach into a shared-memory source
-//      tile: position offsets from gc computed in FP64 and stored in the pair type T, with the
-//      mass in the fourth lane, plus the source's slot index, in a deterministic order,
-//   4. marks per target a bitmask over the tile with the candidate predicate.
+//      tile: offset from gc = (leaf centre - gc) + (x_j - leaf centre), the second term read from
+//      a per-particle mirror in T, so no FP64 arithmetic is done per source; mass and one
+//      auxiliary value per source go along, plus the source's key-order slot,
+//   4. marks per target a bitmask over the tile with a candidate predicate.
 // Other per-source fields are read from key-ordered T mirror records by slot index.
 // Membership predicates that decide integer results (who is a neighbour) are exact: the
-// T-precision distance decides outside a guard band, and pairs inside the band are re-decided
-// with the reference's own FP64 arithmetic (common.cuh: ref_r2).
+// T-precision distance decides outside a guard band that bounds its rounding error, and pairs
+// inside the band are re-decided with the reference's own FP64 arithmetic (common.cuh: ref_r2).
 //
 // CTAs are persistent: each takes the next group from a device work counter until none are
 // left.  A group whose walk or tile does not fit the launch's capacities is appended to an
@@ -58,7 +61,8 @@ struct SmemLayout {
     int gt;         // threads of the CTA (= targets of a group)
     int stack_cap;  // walk stack entries
     int leaf_cap;   // leaf ranges
-    size_t off_stack, off_leaves, off_lpre, off_misc, off_tpos, off_tidx, off_mask, total;
+    size_t off_stack, off_leaves, off_loff, off_lpre, off_misc, off_tpos, off_taux, off_tidx,
+        off_mask, total;
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -70,6 +74,10 @@ struct GroupMisc {
     double rmin;        // min over targets of the search radius
     double span;        // max_k he_k + R : bound on |offset| of staged sources
     double scale;       // max_k |gc_k| + max periodic length (FP64 rounding scale)
+    double bmax;        // max half-diagonal of the walked leaves (bound on |x_j - leaf centre|)
+    float gcf[3];       // gc in FP32
+    float hef[3];       // he rounded up
+    float Rf;           // R rounded up
     int group;          // current group index
     int nleaves;
     int ntile;
@@ -77,16 +85,20 @@ struct GroupMisc {
     double wred[8][8];  // per-warp reduction scratch (at most 8 warps per CTA)
 };
 
-__host__ __device__ inline SmemLayout make_layout(int gt, int tcap, int elt4, int stack_cap, int leaf_cap)
+// elt4 = sizeof(Vec4<T>), eltT = sizeof(T)
+__host__ __device__ inline SmemLayout make_layout(int gt, int tcap, int elt4, int eltT, int stack_cap,
+                                                  int leaf_cap)
 {
     SmemLayout L;
     L.tcap = tcap; L.gt = gt; L.stack_cap = stack_cap; L.leaf_cap = leaf_cap;
     size_t o = 0;
     L.off_stack = o; o = align16(o + sizeof(int) * stack_cap);
     L.off_leaves = o; o = align16(o + sizeof(int2) * leaf_cap);
+    L.off_loff = o; o = align16(o + (size_t)elt4 * leaf_cap);
     L.off_lpre = o; o = align16(o + sizeof(int) * (leaf_cap + 1));
     L.off_misc = o; o = align16(o + sizeof(GroupMisc));
     L.off_tpos = o; o = align16(o + (size_t)elt4 * tcap);
+    L.off_taux = o; o = align16(o + (size_t)eltT * tcap);
     L.off_tidx = o; o = align16(o + sizeof(int) * tcap);
     L.off_mask = o; o = align16(o + sizeof(unsigned) * (size_t)(tcap / 32) * gt);
     L.total = o;
@@ -96,6 +108,7 @@ __host__ __device__ inline SmemLayout make_layout(int gt, int tcap, int elt4, in
 template <typename T>
 struct Tile {
     typename Vec4<T>::type* pm;   // offset x, y, z from gc and mass
+    T* aux;                       // one auxiliary value per source (stage-defined)
     int* idx;                     // key-order slot of each staged source
     unsigned* mask;               // word w of target t at mask[w * gt + t]
     int gt;
@@ -106,11 +119,35 @@ __device__ __forceinline__ Tile<T> tile_of(unsigned char* smem, const SmemLayout
 {
     Tile<T> v;
     v.pm = reinterpret_cast<typename Vec4<T>::type*>(smem + L.off_tpos);
+    v.aux = reinterpret_cast<T*>(smem + L.off_taux);
     v.idx = reinterpret_cast<int*>(smem + L.off_tidx);
     v.mask = reinterpret_cast<unsigned*>(smem + L.off_mask);
     v.gt = L.gt;
     return v;
 }
+
+// The set bits of one target's candidate mask, visited across all words in one loop, so that a
+// warp runs max-over-lanes of the candidate counts (not the sum over words of per-word maxima).
+struct MaskIter {
+    unsigned* mask;
+    int gt, t, nw, w, b;
+    unsigned bits;
+    __device__ __forceinline__ MaskIter(unsigned* m, int gt_, int t_, int nw_)
+        : mask(m), gt(gt_), t(t_), nw(nw_), w(0), b(0), bits(nw_ > 0 ? m[t_] : 0u) {}
+    __device__ __forceinline__ bool next(int& s)
+    {
+        while (bits == 0) {
+            if (++w >= nw) return false;
+            bits = mask[w * gt + t];
+        }
+        b = __ffs(bits) - 1;
+        bits &= bits - 1;
+        s = w * 32 + b;
+        return true;
+    }
+    // drop the source last returned by next() from the stored mask
+    __device__ __forceinline__ void clear_current() { mask[w * gt + t] &= ~(1u << b); }
+};
 
 // Work distribution: next group for this CTA (block-uniform), or -1 when done.
 struct GroupWork {
@@ -189,35 +226,46 @@ __device__ void group_box(GroupMisc* gm, const double* xi, bool active, double r
             double a = gm->wred[0][k], b = gm->wred[0][3 + k];
             for (int ww = 1; ww < nw; ++ww) { a = fmin(a, gm->wred[ww][k]); b = fmax(b, gm->wred[ww][3 + k]); }
             gm->gc[k] = 0.5 * (a + b);
-            gm->he[k] = 0.5 * (b - a);
+            // half extent, rounded so that every target lies within gc +/- he
+            gm->he[k] = fmax(b - gm->gc[k], gm->gc[k] - a);
             span = fmax(span, gm->he[k]);
             sc = fmax(sc, fabs(gm->gc[k]) + (pb.on ? pb.len[k] : 0.0));
+            gm->gcf[k] = (float)gm->gc[k];
+            gm->hef[k] = __double2float_ru(gm->he[k]);
         }
         gm->R = R;
+        gm->Rf = __double2float_ru(R);
         gm->span = span + R;
         gm->scale = sc;
+        gm->bmax = 0.0;
         gm->ntile = 0;
         gm->overflow = 0;
     }
     __syncthreads();
 }
 
-// ---- 2. tree walk by one warp -----------------------------------------------------------------
-// Leaves whose box intersects [gc - he - r, gc + he + r] per axis, r = R or max(R, node kernel
-// size).  Returns the number of leaves, or -1 on overflow of the stack or the leaf list.
-template <int D>
-__device__ int walk_group(const TreeView& tv, int root, const GroupMisc* gm, bool use_ksize,
-                          const Periodic& pb, int* stack, int stack_cap, int2* leaves, int leaf_cap)
+// ---- 2. tree walk by one warp, in FP32 -----------------------------------------------------------
+// Leaves whose box can intersect [gc - he - r, gc + he + r] per axis, r = R or max(R, node
+// kernel size).  The FP32 test keeps a node whenever the exact test might: the rounding of
+// centre, gc and their difference is below 3u (|gc| + d), covered by the relative margin and the
+// absolute slack.  For each kept leaf the offset of its centre from gc is formed in FP64 and
+// stored in T.  Returns the number of leaves, or -1 on overflow of the stack or the leaf list.
+template <int D, typename T>
+__device__ int walk_group(const TreeView& tv, int root, GroupMisc* gm, bool use_ksize,
+                          const Periodic& pb, int* stack, int stack_cap, int2* leaves,
+                          typename Vec4<T>::type* loff, int leaf_cap)
 {
     const int lane = threadIdx.x & 31;
     const unsigned lt = lanemask_lt();
-    double gc[D], he[D];
+    float gcf[D], hef[D];
 #pragma unroll
-    for (int k = 0; k < D; ++k) { gc[k] = gm->gc[k]; he[k] = gm->he[k]; }
-    const double R = gm->R;
+    for (int k = 0; k < D; ++k) { gcf[k] = gm->gcf[k]; hef[k] = gm->hef[k]; }
+    const float Rf = gm->Rf;
+    const float slack = (float)(4.0 * 5.9604644775390625e-08 * gm->scale) + 1e-30f;
     if (lane == 0) stack[0] = root;
     int sp = 1, nl = 0;
     bool overflow = false;
+    float bmax = 0.f;
     __syncwarp();
     while (sp > 0) {
         const int take = sp < 32 ? sp : 32;
@@ -227,14 +275,14 @@ __device__ int walk_group(const TreeView& tv, int root, const GroupMisc* gm, boo
         bool hit = false, leaf = false;
         int nc = 0, fc = -1;
         if (node >= 0) {
-            const double e2 = 0.5 * tv.edge[node];
-            const double r = use_ksize ? fmax(R, tv.ksize[node]) : R;
+            const float e2 = 0.5f * tv.ef[node];
+            const float r = use_ksize ? fmaxf(Rf, tv.kf[node]) : Rf;
             hit = tv.count[node] > 0;
 #pragma unroll
             for (int k = 0; k < D; ++k) {
-                const double d = fabs(min_image(tv.center[k][node] - gc[k], pb, k));
-                const double lim = e2 + he[k] + r;
-                if (d > lim * (1.0 + 1e-12)) hit = false;
+                const float d = fabsf(min_image_f(tv.cf[k][node] - gcf[k], pb, k));
+                const float lim = e2 + hef[k] + r;
+                if (d > lim * 1.00001f + slack) hit = false;
             }
             fc = tv.first_child[node];
             leaf = fc < 0;
@@ -243,7 +291,16 @@ __device__ int walk_group(const TreeView& tv, int root, const GroupMisc* gm, boo
         const unsigned lm = __ballot_sync(FULL, hit && leaf);
         if (hit && leaf) {
             const int pos = nl + __popc(lm & lt);
-            if (pos < leaf_cap) leaves[pos] = make_int2(tv.begin[node], tv.count[node]);
+            if (pos < leaf_cap) {
+                leaves[pos] = make_int2(tv.begin[node], tv.count[node]);
+                typename Vec4<T>::type o;
+                o.x = (T)min_image(tv.center[0][node] - gm->gc[0], pb, 0);
+                o.y = D > 1 ? (T)min_image(tv.center[D > 1 ? 1 : 0][node] - gm->gc[D > 1 ? 1 : 0], pb, D > 1 ? 1 : 0) : T(0);
+                o.z = D > 2 ? (T)min_image(tv.center[D > 2 ? 2 : 0][node] - gm->gc[D > 2 ? 2 : 0], pb, D > 2 ? 2 : 0) : T(0);
+                o.w = T(0);
+                loff[pos] = o;
+            }
+            bmax = fmaxf(bmax, tv.ef[node]);
         }
         nl += __popc(lm);
         int incl = nc;
@@ -261,19 +318,23 @@ __device__ int walk_group(const TreeView& tv, int root, const GroupMisc* gm, boo
         sp += total;
         __syncwarp();
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) bmax = fmaxf(bmax, __shfl_xor_sync(FULL, bmax, o));
+    if (lane == 0) gm->bmax = 0.5 * (double)bmax * 1.7320508075688772 * (1.0 + 1e-6);
     if (nl > leaf_cap) overflow = true;
     return overflow ? -1 : nl;
 }
 
 // Walk + publish the leaf count; returns false (block-uniform) on overflow.
-template <int D>
+template <int D, typename T>
 __device__ bool group_walk(unsigned char* smem, const SmemLayout& L, GroupMisc* gm,
                            const TreeView& tv, int root, bool use_ksize, const Periodic& pb)
 {
     if (threadIdx.x < 32) {
         int* stack = reinterpret_cast<int*>(smem + L.off_stack);
         int2* leaves = reinterpret_cast<int2*>(smem + L.off_leaves);
-        const int nl = walk_group<D>(tv, root, gm, use_ksize, pb, stack, L.stack_cap, leaves, L.leaf_cap);
+        auto* loff = reinterpret_cast<typename Vec4<T>::type*>(smem + L.off_loff);
+        const int nl = walk_group<D, T>(tv, root, gm, use_ksize, pb, stack, L.stack_cap, leaves, loff, L.leaf_cap);
         if (threadIdx.x == 0) {
             gm->nleaves = nl < 0 ? 0 : nl;
             if (nl < 0) gm->overflow = 1;
@@ -283,16 +344,28 @@ __device__ bool group_walk(unsigned char* smem, const SmemLayout& L, GroupMisc* 
     return gm->overflow == 0;
 }
 
+// Per-axis acceptance limit in T for staged offsets: |off_k| <= lim_k keeps every source whose
+// exact offset is within ext_k, given the rounding of off (below u (2 |off| + 2 bmax)).
+template <typename T>
+__device__ __forceinline__ T accept_limit(double ext, const GroupMisc* gm)
+{
+    const double u = Unit<T>::u;
+    return to_T_up<T>(ext * (1.0 + 8.0 * u) + 4.0 * u * gm->bmax + 1e-300);
+}
+
 // ---- 3. staging -------------------------------------------------------------------------------
 // Flattens the leaf ranges and calls, for each particle j (key slot) in deterministic order,
-// accept(j, off) where off[k] = min-image (x_j - gc) in FP64; accepted sources get consecutive
-// tile slots (offsets and wval(j) stored in T).  Returns the tile count, or -1 on overflow.
-template <int D, typename T, class Accept, class WVal>
+// accept(j, off) with off[k] = (leaf centre - gc) + (x_j - leaf centre) in T; accepted sources
+// get consecutive tile slots with their offsets, mass (xrel[j].w) and aux(j).  Returns the tile
+// count, or -1 on overflow.
+template <int D, typename T, class Accept, class Aux>
 __device__ int stage_sources(unsigned char* smem, const SmemLayout& L, GroupMisc* gm,
-                             const State& st, const Periodic& pb, const Tile<T>& tile, Accept accept,
-                             WVal wval)
+                             const typename Vec4<T>::type* xrel, const Tile<T>& tile,
+                             Accept accept, Aux aux)
 {
+    using V4 = typename Vec4<T>::type;
     int2* leaves = reinterpret_cast<int2*>(smem + L.off_leaves);
+    const V4* loff = reinterpret_cast<const V4*>(smem + L.off_loff);
     int* lpre = reinterpret_cast<int*>(smem + L.off_lpre);
     const int nl = gm->nleaves;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -314,15 +387,13 @@ __device__ int stage_sources(unsigned char* smem, const SmemLayout& L, GroupMisc
     __syncthreads();
     const int total = lpre[nl];
     int* wcnt = reinterpret_cast<int*>(&gm->wred[0][0]);
-    double gc[D];
-#pragma unroll
-    for (int k = 0; k < D; ++k) gc[k] = gm->gc[k];
     int base = 0;
     for (int f0 = 0; f0 < total; f0 += blockDim.x) {
         const int f = f0 + threadIdx.x;
         bool ok = false;
         int j = -1;
-        double off[D];
+        T off[D];
+        T m = T(0);
         if (f < total) {
             int lo = 0, hi = nl;   // last r with lpre[r] <= f
             while (hi - lo > 1) {
@@ -330,8 +401,12 @@ __device__ int stage_sources(unsigned char* smem, const SmemLayout& L, GroupMisc
                 if (lpre[mid] <= f) lo = mid; else hi = mid;
             }
             j = leaves[lo].x + (f - lpre[lo]);
-#pragma unroll
-            for (int k = 0; k < D; ++k) off[k] = min_image(st.f[F_POS + k][j] - gc[k], pb, k);
+            const V4 a = loff[lo];
+            const V4 q = xrel[j];
+            off[0] = a.x + q.x;
+            if (D > 1) off[D > 1 ? 1 : 0] = a.y + q.y;
+            if (D > 2) off[D > 2 ? 2 : 0] = a.z + q.z;
+            m = q.w;
             ok = accept(j, off);
         }
         const unsigned bal = __ballot_sync(FULL, ok);
@@ -347,12 +422,13 @@ __device__ int stage_sources(unsigned char* smem, const SmemLayout& L, GroupMisc
         if (ok) {
             const int slot = base + woff + __popc(bal & lanemask_lt());
             if (slot < L.tcap) {
-                typename Vec4<T>::type v;
-                v.x = (T)off[0];
-                v.y = D > 1 ? (T)off[D > 1 ? 1 : 0] : T(0);
-                v.z = D > 2 ? (T)off[D > 2 ? 2 : 0] : T(0);
-                v.w = wval(j);
+                V4 v;
+                v.x = off[0];
+                v.y = D > 1 ? off[D > 1 ? 1 : 0] : T(0);
+                v.z = D > 2 ? off[D > 2 ? 2 : 0] : T(0);
+                v.w = m;
                 tile.pm[slot] = v;
+                tile.aux[slot] = aux(j);
                 tile.idx[slot] = j;
             }
         }
@@ -372,13 +448,24 @@ __device__ __forceinline__ double exact_r2(const State& st, const double* xi, in
     return ref_r2<D>(xi, xj, pb);
 }
 
-// Guard band of |r2_T - r2_exact| for pairs with |offsets| <= span and r <= h.
+// Bound on the rounding error of each component of a T-precision separation between a target
+// (|xo| <= he) and a staged source (|p| <= span), for separations up to h:
+// E = u (he + 2 |p| + 2 bmax + |r|) <= u (3 span + 2 bmax + h), plus the FP64 rounding of the
+// offsets against the coordinate scale.
+template <typename T>
+__device__ __forceinline__ double comp_err(const GroupMisc* gm, double h)
+{
+    const double u = Unit<T>::u;
+    return u * (3.0 * gm->span + 2.0 * gm->bmax + h) * 1.25 + 8.0 * Unit<double>::u * (gm->span + h + gm->scale);
+}
+
+// Guard band of |r2_T - r2_exact| for pairs with separation <= h.
 template <typename T, int D>
 __device__ __forceinline__ double r2_band(const GroupMisc* gm, double h)
 {
     const double u = Unit<T>::u;
-    const double E = u * (2.0 * gm->span + h) * 1.5 + 8.0 * Unit<double>::u * (gm->span + h + gm->scale);
-    return 2.0 * 1.7320508075688772 * E * h + D * E * E + 4.0 * u * h * h;
+    const double E = comp_err<T>(gm, h);
+    return 2.0 * 1.7320508075688772 * E * h + D * E * E + (D + 2) * u * h * h;
 }
 
 // Squared distance in T between a target offset and tile source s; also returns the vector.

@@ -8,8 +8,11 @@ namespace sphgpu {
 
 namespace {
 
+template <typename T>
 struct NbArgs {
     State st;
+    const typename Vec4<T>::type* xrel;
+    const T* hmir;
     TreeView tv;
     Periodic pb;
     SmemLayout L;
@@ -20,19 +23,20 @@ struct NbArgs {
     int cap;
 };
 
-template <int D>
-__global__ void __launch_bounds__(256) neighbors_kernel(NbArgs a)
+template <int D, typename T>
+__global__ void __launch_bounds__(256) neighbors_kernel(NbArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const SmemLayout L = a.L;
     GroupMisc* gm = reinterpret_cast<GroupMisc*>(smem + L.off_misc);
-    const Tile<double> tile = tile_of<double>(smem, L);
+    const Tile<T> tile = tile_of<T>(smem, L);
     const State& st = a.st;
     const int t = threadIdx.x;
     for (;;) {
         const int g = next_group(gm, a.work);
         if (g < 0) break;
         const int gb = a.work.g_begin[g], gn = a.work.g_count[g];
+        if (gn == 0) continue;   // the unused half of an unsplit chunk
         const bool active = t < gn;
         const int i = gb + (active ? t : 0);
         double xi[D];
@@ -41,20 +45,24 @@ __global__ void __launch_bounds__(256) neighbors_kernel(NbArgs a)
         const double hi = st.f[F_SML][i];
         group_box<D>(gm, xi, active, hi, a.pb);
         const int run = st.run[gb];
-        if (!group_walk<D>(smem, L, gm, a.tv, run, a.is_ij != 0, a.pb)) { report_overflow(a.work, g); continue; }
+        if (!group_walk<D, T>(smem, L, gm, a.tv, run, a.is_ij != 0, a.pb)) { report_overflow(a.work, g); continue; }
         {
-            const double R = gm->R;
+            const double u = Unit<T>::u;
+            const T Rt = to_T_up<T>(gm->R);
+            const T rel = (T)(1.0 + 8.0 * u), slack = to_T_up<T>(4.0 * u * gm->bmax + 1e-300);
             const int is_ij = a.is_ij;
-            double he[D];
+            const T* hmir = a.hmir;
+            T he[D];
 #pragma unroll
-            for (int k = 0; k < D; ++k) he[k] = gm->he[k];
-            const int ntile = stage_sources<D, double>(smem, L, gm, st, a.pb, tile, [&](int j, const double* off) {
-                const double r = is_ij ? fmax(R, st.f[F_SML][j]) : R;
+            for (int k = 0; k < D; ++k) he[k] = to_T_up<T>(gm->he[k]);
+            const int ntile = stage_sources<D, T>(smem, L, gm, a.xrel, tile, [&](int j, const T* off) {
+                T r = Rt;
+                if (is_ij) { const T hj = hmir[j]; r = r > hj ? r : hj; }
 #pragma unroll
                 for (int k = 0; k < D; ++k)
-                    if (fabs(off[k]) > (he[k] + r) * (1.0 + 1e-12)) return false;
+                    if (fabs(off[k]) > (he[k] + r) * rel + slack) return false;
                 return true;
-            }, [&](int) { return 0.0; });
+            }, [&](int) { return T(0); });
             if (ntile < 0) { report_overflow(a.work, g); continue; }
             gm->ntile = ntile;
         }
@@ -81,39 +89,36 @@ __global__ void __launch_bounds__(256) neighbors_kernel(NbArgs a)
     }
 }
 
-template <int D>
+template <int D, typename T>
 void run_neighbors(Ctx& c, int is_ij, int* d_counts, int* d_list, int cap)
 {
+    using V4 = typename Vec4<T>::type;
     reset_work_counters(c);
-    NbArgs a{};
+    NbArgs<T> a{};
     a.st = c.st;
+    a.xrel = (const V4*)c.mir[6];
+    a.hmir = (const T*)c.mir[7];
     a.tv = tree_view(c);
     a.pb = c.pb;
     a.is_ij = is_ij;
     a.counts = d_counts;
     a.list = d_list;
     a.cap = cap;
-    const int gt = c.group_threads;
-    auto kern = neighbors_kernel<D>;
-    cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, max_optin_smem(c));
-    a.L = make_layout(gt, D == 1 ? 128 : 1024, sizeof(double4_32a), 256, 256);
-    a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 0, nullptr, nullptr,
-                       c.d_ovf_list, c.d_work + 1, c.d_err};
-    kern<<<c.num_sms * 2, gt, a.L.total, c.stream>>>(a);
-    const int big = big_tile_cap(c, gt, sizeof(double4_32a), 1024, 2048);
-    a.L = make_layout(gt, big, sizeof(double4_32a), 1024, 2048);
-    a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 2, c.d_ovf_list, c.d_work + 1,
-                       nullptr, nullptr, c.d_err};
-    kern<<<c.num_sms, gt, a.L.total, c.stream>>>(a);
+    auto kern = neighbors_kernel<D, T>;
+    launch_three_pass<NbArgs<T>>(c, (const void*)kern, a, D == 1 ? 128 : 1024, sizeof(V4), sizeof(T),
+        [](const void* k, int grid, int block, size_t smem, cudaStream_t st, NbArgs<T>& args) {
+            reinterpret_cast<void (*)(NbArgs<T>)>(const_cast<void*>(k))<<<grid, block, smem, st>>>(args);
+        });
 }
 
 }  // namespace
 
 void launch_neighbors(Ctx& c, int is_ij, int* d_counts, int* d_list, int cap)
 {
-    if (c.dim == 1) run_neighbors<1>(c, is_ij, d_counts, d_list, cap);
-    else if (c.dim == 2) run_neighbors<2>(c, is_ij, d_counts, d_list, cap);
-    else run_neighbors<3>(c, is_ij, d_counts, d_list, cap);
+    const bool f32 = c.precision == SPHGPU_FP32_PAIR;
+    if (c.dim == 1) { if (f32) run_neighbors<1, float>(c, is_ij, d_counts, d_list, cap); else run_neighbors<1, double>(c, is_ij, d_counts, d_list, cap); }
+    else if (c.dim == 2) { if (f32) run_neighbors<2, float>(c, is_ij, d_counts, d_list, cap); else run_neighbors<2, double>(c, is_ij, d_counts, d_list, cap); }
+    else { if (f32) run_neighbors<3, float>(c, is_ij, d_counts, d_list, cap); else run_neighbors<3, double>(c, is_ij, d_counts, d_list, cap); }
 }
 
 }  // namespace sphgpu

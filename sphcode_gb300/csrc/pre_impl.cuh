@@ -9,7 +9,8 @@
 // decided exactly.  Newton iterations and the density loop run over the candidate bitmask with
 // the pair terms in T; the reference's `r >= h -> break` over the distance-sorted list is the
 // set {r < h}; at the final h that set is decided exactly (it defines the neighbour count).
-// The Newton update and its convergence test |dh| < 1e-4 (h + h_prev) are FP64.
+// The Newton step f / f' is formed from the T sums; h itself and the convergence test
+// |dh| < 1e-4 (h + h_prev) stay FP64.
 #pragma once
 
 #include "context.cuh"
@@ -19,12 +20,14 @@ namespace sphgpu {
 
 template <typename T>
 struct PreArgs {
+    using V4 = typename Vec4<T>::type;
     State st;
     TreeView tv;
     Periodic pb;
     SmemLayout L;
     GroupWork work;
-    const typename Vec4<T>::type* mvel;   // {vx, vy, vz, c}
+    const V4* xrel;                       // {x - leaf centre, m}
+    const V4* mvel;                       // {vx, vy, vz, c}
     const T* mu;                          // u
     int nn;
     double ratio;
@@ -66,6 +69,7 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
         const int g = next_group(gm, a.work);
         if (g < 0) break;
         const int gb = a.work.g_begin[g], gn = a.work.g_count[g];
+        if (gn == 0) continue;   // the unused half of an unsplit chunk
         const bool active = t < gn;
         const int i = gb + (active ? t : 0);
         double xi[D];
@@ -76,18 +80,18 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
         const double hs = a.initial ? hg : hg * a.ratio;
         group_box<D>(gm, xi, active, hs, a.pb);
         const int run = st.run[gb];
-        if (!group_walk<D>(smem, L, gm, a.tv, run, false, a.pb)) { report_overflow(a.work, g); continue; }
+        if (!group_walk<D, T>(smem, L, gm, a.tv, run, false, a.pb)) { report_overflow(a.work, g); continue; }
         {
-            const double R = gm->R;
-            double lim[D];
+            T lim[D];
 #pragma unroll
-            for (int k = 0; k < D; ++k) lim[k] = (gm->he[k] + R) * (1.0 + 1e-12);
-            const int ntile = stage_sources<D, T>(smem, L, gm, st, a.pb, tile, [&](int, const double* off) {
+            for (int k = 0; k < D; ++k) lim[k] = accept_limit<T>(gm->he[k] + gm->R, gm);
+            const T* mu = a.mu;
+            const int ntile = stage_sources<D, T>(smem, L, gm, a.xrel, tile, [&](int, const T* off) {
 #pragma unroll
                 for (int k = 0; k < D; ++k)
                     if (fabs(off[k]) > lim[k]) return false;
                 return true;
-            }, [&](int j) { return (T)st.f[F_MASS][j]; });
+            }, [&](int j) { return mu[j]; });
             if (ntile < 0) { report_overflow(a.work, g); continue; }
             gm->ntile = ntile;   // every thread writes the same value
         }
@@ -120,36 +124,34 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
         // ---- smoothing length: Newton-Raphson on rho h^D = b (or n h^D = b for disph) ----
         double h = hg;
         if (!a.initial && a.iterative) {
-            const double bconst = (TYPE == 1) ? a.nn / A : mi * a.nn / A;
+            const T bconst = (T)((TYPE == 1) ? a.nn / A : mi * a.nn / A);
             bool done = !active, conv = false;
             for (int it = 0; it < 10; ++it) {
                 if (!__any_sync(FULL, !done)) break;
                 if (!done) {
                     const T hT = (T)h;
+                    const T hinvT = T(1) / hT;
                     Sum<T> s0, s1;
                     s0.zero();
                     s1.zero();
-                    for (int w = 0; w < nw; ++w) {
-                        unsigned bits = tile.mask[w * GT + t];
-                        while (bits) {
-                            const int b = __ffs(bits) - 1;
-                            bits &= bits - 1;
-                            const V4 p = tile.pm[w * 32 + b];
-                            T r[D];
-                            const T rr = sqrt(tile_r2<D, T>(xo, p, r));
-                            if (rr < hT) {
-                                const T W = KF::w(rr, hT), dW = KF::dhw(rr, hT);
-                                if (TYPE == 1) { s0.add(W); s1.add(dW); }
-                                else { s0.add(p.w * W); s1.add(p.w * dW); }
-                            }
+                    MaskIter it(tile.mask, GT, t, nw);
+                    int s;
+                    while (it.next(s)) {
+                        const V4 p = tile.pm[s];
+                        T r[D];
+                        const T rr = sqrt(tile_r2<D, T>(xo, p, r));
+                        if (rr < hT) {
+                            const T W = KF::w(rr, hinvT), dW = KF::dhw(rr, hinvT);
+                            if (TYPE == 1) { s0.add(W); s1.add(dW); }
+                            else { s0.add(p.w * W); s1.add(p.w * dW); }
                         }
                     }
-                    const double dens = (double)s0.get(), ddens = (double)s1.get();
-                    const double hd = powD<D>(h);
-                    const double hd1 = D == 1 ? 1.0 : D == 2 ? h : h * h;
-                    const double f = dens * hd - bconst;
-                    const double df = ddens * hd + D * dens * hd1;
-                    const double hn = h - f / df;
+                    const T dens = (T)s0.get(), ddens = (T)s1.get();
+                    const T hd = powD<D>(hT);
+                    const T hd1 = D == 1 ? T(1) : D == 2 ? hT : hT * hT;
+                    const T f = dens * hd - bconst;
+                    const T df = ddens * hd + T(D) * dens * hd1;
+                    const double hn = h - (double)(f / df);
                     if (fabs(hn - h) < (hn + h) * 1e-4) { done = true; conv = true; }
                     h = hn;
                 }
@@ -163,61 +165,56 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
 
         // ---- density, pressure, grad-h, signal velocity over {r < h} ----
         const T hT = (T)hf;
-        const double ci = st.f[F_SOUND][i];
-        const double ui = st.f[F_ENE][i];
+        const T hinvT = (T)(1.0 / hf);
+        const T ciT = a.mvel[i].w;
+        const T uiT = a.mu[i];
         T vi[3] = {T(0), T(0), T(0)};
-#pragma unroll
-        for (int k = 0; k < D; ++k) vi[k] = (T)st.f[F_VEL + k][i];
+        {
+            const V4 v = a.mvel[i];
+            vi[0] = v.x; vi[1] = v.y; vi[2] = v.z;
+        }
         Sum<T> sd, sdh, sn, sp, sdp, sdn;
         sd.zero(); sdh.zero(); sn.zero(); sp.zero(); sdp.zero(); sdn.zero();
-        T vsig = (T)(ci * 2.0);
+        T vsig = T(2) * ciT;
         int nnb = 0;
         {
             const double hf2 = __dmul_rn(hf, hf);
             const double band = r2_band<T, D>(gm, hf);
             const T lo_t = to_T_down<T>(hf2 - band), hi_t = to_T_up<T>(hf2 + band);
-            const T ciT = (T)ci;
-            for (int w = 0; w < nw; ++w) {
-                const unsigned bits0 = tile.mask[w * GT + t];
-                unsigned bits = bits0, keep = 0;
-                while (bits) {
-                    const int b = __ffs(bits) - 1;
-                    bits &= bits - 1;
-                    const int s = w * 32 + b;
-                    const V4 p = tile.pm[s];
-                    T r[D];
-                    const T r2 = tile_r2<D, T>(xo, p, r);
-                    bool in = r2 < lo_t;
-                    if (!in && r2 <= hi_t) in = __dsqrt_rn(exact_r2<D>(st, xi, tile.idx[s], a.pb)) < hf;
-                    if (!in) continue;
-                    keep |= 1u << b;
-                    ++nnb;
-                    const int j = tile.idx[s];
-                    const T rr = sqrt(r2);
-                    const T W = KF::w(rr, hT);
-                    sd.add(p.w * W);
-                    if (TYPE == 0) {
-                        if (!a.initial) sdh.add(p.w * KF::dhw(rr, hT));
-                    } else if (TYPE == 1) {
-                        if (!a.initial) {
-                            const T dW = KF::dhw(rr, hT);
-                            const T muj = p.w * a.mu[j];
-                            sn.add(W);
-                            sp.add(muj * W);
-                            sdp.add(muj * dW);
-                            sdn.add(dW);
-                        }
-                    }
-                    if (!a.initial && j != i) {
-                        const V4 vj = a.mvel[j];
-                        T rv = r[0] * (vi[0] - vj.x);
-                        if (D > 1) rv += r[D > 1 ? 1 : 0] * (vi[1] - vj.y);
-                        if (D > 2) rv += r[D > 2 ? 2 : 0] * (vi[2] - vj.z);
-                        const T vs = ciT + vj.w - T(3) * rv / rr;
-                        vsig = vs > vsig ? vs : vsig;
+            MaskIter it(tile.mask, GT, t, nw);
+            int s;
+            while (it.next(s)) {
+                const V4 p = tile.pm[s];
+                T r[D];
+                const T r2 = tile_r2<D, T>(xo, p, r);
+                bool in = r2 < lo_t;
+                if (!in && r2 <= hi_t) in = __dsqrt_rn(exact_r2<D>(st, xi, tile.idx[s], a.pb)) < hf;
+                if (!in) { it.clear_current(); continue; }
+                ++nnb;
+                const int j = tile.idx[s];
+                const T rr = sqrt(r2);
+                const T W = KF::w(rr, hinvT);
+                sd.add(p.w * W);
+                if (TYPE == 0) {
+                    if (!a.initial) sdh.add(p.w * KF::dhw(rr, hinvT));
+                } else if (TYPE == 1) {
+                    if (!a.initial) {
+                        const T dW = KF::dhw(rr, hinvT);
+                        const T muj = p.w * tile.aux[s];
+                        sn.add(W);
+                        sp.add(muj * W);
+                        sdp.add(muj * dW);
+                        sdn.add(dW);
                     }
                 }
-                tile.mask[w * GT + t] = active ? keep : 0u;
+                if (!a.initial && j != i) {
+                    const V4 vj = a.mvel[j];
+                    T rv = r[0] * (vi[0] - vj.x);
+                    if (D > 1) rv += r[D > 1 ? 1 : 0] * (vi[1] - vj.y);
+                    if (D > 2) rv += r[D > 2 ? 2 : 0] * (vi[2] - vj.z);
+                    const T vs = ciT + vj.w - T(3) * rv * (T(1) / rr);
+                    vsig = vs > vsig ? vs : vsig;
+                }
             }
         }
         if (a.initial) {
@@ -228,20 +225,23 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
             continue;
         }
         const double dens = (double)sd.get();
-        double pres, gradh = 0.0;
+        const T densT = (T)dens;
+        double pres;
+        T gradh = T(0);
         if (TYPE == 0) {
-            pres = (a.gamma - 1.0) * dens * ui;
-            gradh = 1.0 / (1.0 + hf / (D * dens) * (double)sdh.get());
+            pres = (a.gamma - 1.0) * dens * (double)st.f[F_ENE][i];
+            gradh = T(1) / (T(1) + hT / (T(D) * densT) * (T)sdh.get());
         } else if (TYPE == 1) {
-            const double n_i = (double)sn.get();
+            const T n_i = (T)sn.get();
             pres = (a.gamma - 1.0) * (double)sp.get();
-            gradh = hf / (D * n_i) * (double)sdp.get() / (1.0 + hf / (D * n_i) * (double)sdn.get());
+            const T c = hT / (T(D) * n_i);
+            gradh = c * (T)sdp.get() / (T(1) + c * (T)sdn.get());
         } else {
-            pres = (a.gamma - 1.0) * dens * ui;
+            pres = (a.gamma - 1.0) * dens * (double)st.f[F_ENE][i];
         }
         // h / v_sig minimum of the group -> run minimum (TimeStep input)
         {
-            double hv = active ? hf / (double)vsig : 1.7976931348623157e308;
+            double hv = active ? (double)(hT / vsig) : 1.7976931348623157e308;
             for (int o = 16; o > 0; o >>= 1) hv = fmin(hv, __shfl_xor_sync(FULL, hv, o));
             if ((t & 31) == 0) atomicMin(&a.hvs[run], dbl_to_ord(hv));
         }
@@ -262,21 +262,18 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
 #pragma unroll
                 for (int q = 0; q < D; ++q) dv[k][q].zero();
             }
-            const T uiT = (T)ui;
-            for (int w = 0; w < nw; ++w) {
-                unsigned bits = tile.mask[w * GT + t];
-                while (bits) {
-                    const int b = __ffs(bits) - 1;
-                    bits &= bits - 1;
-                    const int s = w * 32 + b;
+            MaskIter it(tile.mask, GT, t, nw);
+            int s;
+            while (it.next(s)) {
+                {
                     const V4 p = tile.pm[s];
                     const int j = tile.idx[s];
                     T r[D];
                     const T rr = sqrt(tile_r2<D, T>(xo, p, r));
-                    const T cf = KF::dw_coef(rr, hT);
+                    const T cf = KF::dw_coef(rr, rr > T(0) ? T(1) / rr : T(0), hinvT);
                     const V4 vj = a.mvel[j];
                     const T vjv[3] = {vj.x, vj.y, vj.z};
-                    const T mdu = p.w * (a.mu[j] - uiT);
+                    const T mdu = p.w * (tile.aux[s] - uiT);
 #pragma unroll
                     for (int k = 0; k < D; ++k) {
                         const T dw = r[k] * cf;
@@ -292,7 +289,8 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
                 }
             }
             if (active) {
-                const double rho_inv = 1.0 / dens;
+                const double ui = st.f[F_ENE][i];
+                const T rho_inv = T(1) / densT;
 #pragma unroll
                 for (int k = 0; k < D; ++k) {
                     const double ddk = (double)dd[k].get();
@@ -302,32 +300,31 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
 #pragma unroll
                 for (int q = 0; q < D; ++q)
 #pragma unroll
-                    for (int k = 0; k < D; ++k) st.f[F_GRADV + q * 3 + k][i] = (double)dv[q][k].get() * rho_inv;
+                    for (int k = 0; k < D; ++k) st.f[F_GRADV + q * 3 + k][i] = (double)((T)dv[q][k].get() * rho_inv);
             }
             continue;
         }
 
         // ---- Balsara switch and time-dependent alpha (src/pre_interaction.cpp:115-161) ----
-        double alpha = st.f[F_ALPHA][i];
-        double balsara = st.f[F_BALSARA][i];
-        const double dt = a.dt_run[run];
+        T alpha = (T)st.f[F_ALPHA][i];
+        T balsara = (T)st.f[F_BALSARA][i];
+        double alpha_out = st.f[F_ALPHA][i], balsara_out = st.f[F_BALSARA][i];
+        const T dt = (T)a.dt_run[run];
         const bool bal = a.use_balsara && D != 1;
         if (bal || a.use_tdav) {
             Sum<T> sdiv, srot[3];
             sdiv.zero(); srot[0].zero(); srot[1].zero(); srot[2].zero();
-            for (int w = 0; w < nw; ++w) {
-                unsigned bits = tile.mask[w * GT + t];
-                while (bits) {
-                    const int b = __ffs(bits) - 1;
-                    bits &= bits - 1;
-                    const int s = w * 32 + b;
+            MaskIter it(tile.mask, GT, t, nw);
+            int s;
+            while (it.next(s)) {
+                {
                     const V4 p = tile.pm[s];
                     const int j = tile.idx[s];
                     T r[D];
                     const T rr = sqrt(tile_r2<D, T>(xo, p, r));
-                    const T cf = KF::dw_coef(rr, hT);
+                    const T cf = KF::dw_coef(rr, rr > T(0) ? T(1) / rr : T(0), hinvT);
                     const V4 vj = a.mvel[j];
-                    const T wj = (TYPE == 1) ? p.w * a.mu[j] : p.w;
+                    const T wj = (TYPE == 1) ? p.w * tile.aux[s] : p.w;
                     T dw[3] = {T(0), T(0), T(0)}, vij[3] = {T(0), T(0), T(0)};
 #pragma unroll
                     for (int k = 0; k < D; ++k) dw[k] = r[k] * cf;
@@ -349,37 +346,38 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
                     }
                 }
             }
-            double div = (double)sdiv.get();
-            double rot[3] = {(double)srot[0].get(), (double)srot[1].get(), (double)srot[2].get()};
+            T div = (T)sdiv.get();
+            T rot[3] = {(T)srot[0].get(), (T)srot[1].get(), (T)srot[2].get()};
             if (TYPE == 1) {
-                const double p_inv = (a.gamma - 1.0) / pres;
+                const T p_inv = (T)((a.gamma - 1.0) / pres);
                 div *= p_inv;
                 for (int k = 0; k < 3; ++k) rot[k] *= p_inv;
             } else {
-                div /= dens;
-                for (int k = 0; k < 3; ++k) rot[k] /= dens;
+                const T rho_inv = T(1) / densT;
+                div *= rho_inv;
+                for (int k = 0; k < 3; ++k) rot[k] *= rho_inv;
             }
+            const T tau_inv = (T)a.eps_av * ciT / hT;
             if (bal) {
-                const double rot_abs = D == 2 ? fabs(rot[0]) : sqrt(rot[0] * rot[0] + rot[1] * rot[1] + rot[2] * rot[2]);
-                balsara = fabs(div) / (fabs(div) + rot_abs + 1e-4 * ci / hf);
+                const T rot_abs = D == 2 ? fabs(rot[0]) : sqrt(rot[0] * rot[0] + rot[1] * rot[1] + rot[2] * rot[2]);
+                balsara = fabs(div) / (fabs(div) + rot_abs + T(1e-4) * ciT / hT);
+                balsara_out = (double)balsara;
                 if (a.use_tdav) {
-                    const double tau_inv = a.eps_av * ci / hf;
-                    const double sdv = -div > 0.0 ? -div : 0.0;
-                    alpha += (-(alpha - a.alpha_min) * tau_inv + sdv * (a.alpha_max - alpha)) * dt;
+                    const T sdv = -div > T(0) ? -div : T(0);
+                    alpha_out = st.f[F_ALPHA][i] + (double)((-(alpha - (T)a.alpha_min) * tau_inv + sdv * ((T)a.alpha_max - alpha)) * dt);
                 }
             } else {
-                const double tau_inv = a.eps_av * ci / hf;
-                const double s_i = -div > 0.0 ? -div : 0.0;
-                alpha = (alpha + dt * tau_inv * a.alpha_min + s_i * dt * a.alpha_max) / (1.0 + dt * tau_inv + s_i * dt);
+                const T s_i = -div > T(0) ? -div : T(0);
+                alpha_out = (double)((alpha + dt * tau_inv * (T)a.alpha_min + s_i * dt * (T)a.alpha_max) / (T(1) + dt * tau_inv + s_i * dt));
             }
         }
         if (active) {
             st.f[F_SML][i] = hf;
             st.f[F_DENS][i] = dens;
             st.f[F_PRES][i] = pres;
-            st.f[F_GRADH][i] = gradh;
-            st.f[F_BALSARA][i] = balsara;
-            st.f[F_ALPHA][i] = alpha;
+            st.f[F_GRADH][i] = (double)gradh;
+            st.f[F_BALSARA][i] = balsara_out;
+            st.f[F_ALPHA][i] = alpha_out;
             st.neighbor[i] = nnb;
         }
     }
@@ -424,13 +422,14 @@ void run_pre(Ctx& c, bool initial)
     cudaStream_t s = c.stream;
     pre_mirror_kernel<D, T><<<ceil_div(c.n, 256), 256, 0, s>>>(c.st, c.n, (V4*)c.mir[0], (T*)c.mir[1]);
     // counters: [0] main work, [1] overflow count, [2] overflow work; plus h/v_sig and Newton
-    if (!initial) pre_reset_kernel<<<ceil_div(std::max(c.R, 4), 128), 128, 0, s>>>(c.R, c.d_hvs, c.d_work, 4);
-    else pre_reset_kernel<<<1, 32, 0, s>>>(0, c.d_hvs, c.d_work, 4);
+    if (!initial) pre_reset_kernel<<<ceil_div(std::max(c.R, 16), 128), 128, 0, s>>>(c.R, c.d_hvs, c.d_work, 16);
+    else pre_reset_kernel<<<1, 32, 0, s>>>(0, c.d_hvs, c.d_work, 16);
     cudaMemsetAsync(c.d_newton_fail, 0, sizeof(int), s);
     PreArgs<T> a{};
     a.st = c.st;
     a.tv = tree_view(c);
     a.pb = c.pb;
+    a.xrel = (const V4*)c.mir[6];
     a.mvel = (const V4*)c.mir[0];
     a.mu = (const T*)c.mir[1];
     a.nn = c.p.neighbor_number;
@@ -447,20 +446,11 @@ void run_pre(Ctx& c, bool initial)
     a.dt_run = c.d_dt;
     a.hvs = c.d_hvs;
     a.newton_fail = c.d_newton_fail;
-    const int gt = c.group_threads;
-    const int tcap = c.tile_cap ? c.tile_cap : default_tile_cap<D>();
-    a.L = make_layout(gt, tcap, sizeof(V4), 256, 256);
-    a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 0, nullptr, nullptr,
-                       c.d_ovf_list, c.d_work + 1, c.d_err};
-    cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, max_optin_smem(c));
-    const int nb = std::max(1, kernel_occupancy((const void*)kern, gt, a.L.total));
-    kern<<<nb * c.num_sms, gt, a.L.total, s>>>(a);
-    // overflow pass: groups that did not fit, with the largest capacities
-    const int big = big_tile_cap(c, gt, sizeof(V4), 1024, 2048);
-    a.L = make_layout(gt, big, sizeof(V4), 1024, 2048);
-    a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 2, c.d_ovf_list, c.d_work + 1,
-                       nullptr, nullptr, c.d_err};
-    kern<<<c.num_sms, gt, a.L.total, s>>>(a);
+    const int tcap = c.tile_cap_pre ? c.tile_cap_pre : default_tile_cap<D>();
+    launch_three_pass<PreArgs<T>>(c, (const void*)kern, a, tcap, sizeof(V4), sizeof(T),
+        [](const void* k, int grid, int block, size_t smem, cudaStream_t st, PreArgs<T>& args) {
+            reinterpret_cast<void (*)(PreArgs<T>)>(const_cast<void*>(k))<<<grid, block, smem, st>>>(args);
+        });
 }
 
 }  // namespace sphgpu

@@ -487,49 +487,85 @@ __global__ void ksize_kernel(const double* sml, const int* node_total_p, int* be
     }
 }
 
-// ---- target groups -------------------------------------------------------------------------
+// ---- target groups ----------------------------------------------------------------------------
+// Each fixed chunk of key-consecutive particles becomes group 2c; where the chunk straddles a
+// high-level node boundary (its two halves at the highest differing key bit are each less than
+// half its extent) it is split there, the second part becoming group 2c + 1 (else empty).
+template <int D>
+__global__ void split_groups_kernel(State st, const unsigned long long* keys, const int* ck_begin,
+                                    const int* ck_count, int nchunks, int* g_begin, int* g_count)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nchunks) return;
+    const int b = ck_begin[c], e = b + ck_count[c];
+    int s = e;
+    const unsigned long long diff = keys[b] ^ keys[e - 1];
+    if (diff) {
+        const unsigned long long bit = 1ull << (63 - __clzll((long long)diff));
+        int lo = b, hi = e - 1;   // first index with the bit set
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (keys[mid] & bit) hi = mid; else lo = mid + 1;
+        }
+        double ext = 0.0, ea = 0.0, eb = 0.0;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            double a0 = 1.7976931348623157e308, a1 = -a0, b0 = a0, b1 = -a0;
+            for (int i = b; i < e; ++i) {
+                const double x = st.f[F_POS + k][i];
+                if (i < lo) { a0 = fmin(a0, x); a1 = fmax(a1, x); }
+                else { b0 = fmin(b0, x); b1 = fmax(b1, x); }
+            }
+            ext = fmax(ext, fmax(a1, b1) - fmin(a0, b0));
+            ea = fmax(ea, a1 - a0);
+            eb = fmax(eb, b1 - b0);
+        }
+        if (lo > b && fmax(ea, eb) < 0.5 * ext) s = lo;
+    }
+    g_begin[2 * c] = b;
+    g_count[2 * c] = s - b;
+    g_begin[2 * c + 1] = s;
+    g_count[2 * c + 1] = e - s;
+}
 
-// Partition the particles into groups of at most G consecutive (key-ordered) particles that are
-// spatially compact: maximal nodes with <= G particles, with consecutive such siblings merged
-// while the merged count stays <= G; a leaf with more than G particles is cut into chunks.
-__global__ void groups_kernel(const int* node_total_p, int R, const int* begin, const int* count,
-                              const int* first, const int* nchild, int G, int* g_begin,
-                              int* g_count, int* n_groups, int max_groups, unsigned* err)
+// ---- FP32 node copies and leaf-relative particle offsets ------------------------------------
+
+template <int D, typename T>
+__global__ void node_mirror_kernel(State st, const int* node_total_p, TreeView tv, float* cf0,
+                                   float* cf1, float* cf2, float* ef, typename Vec4<T>::type* xrel)
+{
+    float* cf[3] = {cf0, cf1, cf2};
+    const int total = *node_total_p;
+    for (int nd = blockIdx.x * blockDim.x + threadIdx.x; nd < total; nd += gridDim.x * blockDim.x) {
+        double c[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            c[k] = tv.center[k][nd];
+            cf[k][nd] = (float)c[k];
+        }
+        ef[nd] = __double2float_ru(tv.edge[nd]);
+        if (tv.first_child[nd] >= 0) continue;
+        const int b = tv.begin[nd], e = b + tv.count[nd];
+        for (int j = b; j < e; ++j) {
+            typename Vec4<T>::type q;
+            q.x = (T)(st.f[F_POS][j] - c[0]);
+            q.y = D > 1 ? (T)(st.f[F_POS + (D > 1 ? 1 : 0)][j] - c[D > 1 ? 1 : 0]) : T(0);
+            q.z = D > 2 ? (T)(st.f[F_POS + (D > 2 ? 2 : 0)][j] - c[D > 2 ? 2 : 0]) : T(0);
+            q.w = (T)st.f[F_MASS][j];
+            xrel[j] = q;
+        }
+    }
+}
+
+// Kernel sizes rounded up to FP32, and the smoothing lengths in T.
+template <typename T>
+__global__ void kernel_size_mirror_kernel(const int* node_total_p, const double* ksize, float* kf,
+                                          const double* sml, int n, T* hm)
 {
     const int total = *node_total_p;
-    auto emit = [&](int b, int c) {
-        const int slot = atomicAdd(n_groups, 1);
-        if (slot < max_groups) { g_begin[slot] = b; g_count[slot] = c; }
-        else atomicOr(err, (unsigned)ERR_TILE);
-    };
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-        const int cnt = count[i];
-        if (i < R) {
-            if (cnt == 0) continue;
-            if (cnt <= G) { emit(begin[i], cnt); continue; }
-        } else if (cnt <= G || first[i] < 0) {
-            continue;
-        }
-        const int fc = first[i], nc = nchild[i];
-        if (fc < 0) {
-            // a root with > G particles that was not split (cannot happen: roots always split)
-            for (int b = begin[i]; b < begin[i] + cnt; b += G) emit(b, min(G, begin[i] + cnt - b));
-            continue;
-        }
-        int ab = -1, an = 0;
-        for (int c = 0; c < nc; ++c) {
-            const int ch = fc + c, cc = count[ch];
-            if (cc <= G) {
-                if (an + cc > G) { emit(ab, an); an = 0; }
-                if (an == 0) ab = begin[ch];
-                an += cc;
-            } else {
-                if (an > 0) { emit(ab, an); an = 0; }
-                if (first[ch] < 0)
-                    for (int b = begin[ch]; b < begin[ch] + cc; b += G) emit(b, min(G, begin[ch] + cc - b));
-            }
-        }
-        if (an > 0) emit(ab, an);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < max(total, n); i += gridDim.x * blockDim.x) {
+        if (i < total) kf[i] = __double2float_ru(ksize[i]);
+        if (i < n) hm[i] = (T)sml[i];
     }
 }
 
@@ -544,7 +580,9 @@ TreeView tree_view(const Ctx& c)
     t.count = c.nd_count;
     t.first_child = c.nd_first;
     t.nchild = c.nd_nchild;
-    for (int k = 0; k < 3; ++k) { t.center[k] = c.nd_center[k]; t.com[k] = c.nd_com[k]; }
+    for (int k = 0; k < 3; ++k) { t.center[k] = c.nd_center[k]; t.com[k] = c.nd_com[k]; t.cf[k] = c.nd_cf[k]; }
+    t.ef = c.nd_ef;
+    t.kf = c.nd_kf;
     t.edge = c.nd_edge;
     t.mass = c.nd_mass;
     t.ksize = c.nd_ksize;
@@ -574,7 +612,10 @@ int tree_alloc(Ctx& c)
     for (int k = 0; k < c.dim; ++k) {
         A((void**)&c.nd_center[k], sizeof(double) * nc);
         A((void**)&c.nd_com[k], sizeof(double) * nc);
+        A((void**)&c.nd_cf[k], sizeof(float) * nc);
     }
+    A((void**)&c.nd_ef, sizeof(float) * nc);
+    A((void**)&c.nd_kf, sizeof(float) * nc);
     A((void**)&c.nd_edge, sizeof(double) * nc);
     A((void**)&c.nd_mass, sizeof(double) * nc);
     A((void**)&c.nd_ksize, sizeof(double) * nc);
@@ -583,9 +624,11 @@ int tree_alloc(Ctx& c)
     A((void**)&c.chunk_sum, sizeof(int) * (ceil_div(nc, LEVEL_CHUNK) + 1));
     A((void**)&c.bbox, sizeof(long long) * 2 * 3 * c.R);
     A((void**)&c.node_total, sizeof(int));
-    c.max_groups = n + c.R;
+    c.max_groups = 2 * (n / 32 + c.R + 1);
     A((void**)&c.g_begin, sizeof(int) * c.max_groups);
     A((void**)&c.g_count, sizeof(int) * c.max_groups);
+    A((void**)&c.ck_begin, sizeof(int) * (c.max_groups / 2));
+    A((void**)&c.ck_count, sizeof(int) * (c.max_groups / 2));
     A((void**)&c.n_groups, sizeof(int));
     if (e != cudaSuccess) {
         c.last_error = std::string("tree allocation: ") + cudaGetErrorString(e);
@@ -601,7 +644,8 @@ void tree_free(Ctx& c)
                     c.nd_first, c.nd_nchild, c.nd_parent, c.nd_level, c.nd_arrive, c.nd_center[0],
                     c.nd_center[1], c.nd_center[2], c.nd_com[0], c.nd_com[1], c.nd_com[2],
                     c.nd_edge, c.nd_mass, c.nd_ksize, c.lvl_start, c.lvl_tmp, c.chunk_sum, c.bbox,
-                    c.node_total, c.g_begin, c.g_count, c.n_groups};
+                    c.node_total, c.g_begin, c.g_count, c.n_groups, c.nd_cf[0], c.nd_cf[1],
+                    c.nd_cf[2], c.nd_ef, c.nd_kf, c.ck_begin, c.ck_count};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -685,13 +729,13 @@ static void make_tree_d(Ctx& c, bool reorder_all)
     }
     cudaMemcpyAsync(c.node_total, c.lvl_start + levels + 2, sizeof(int), cudaMemcpyDeviceToDevice, s);
     launch_node_moments(c);
-    // target groups for the three pair kernels (one list; group size = 32 * max warps)
-    cudaMemsetAsync(c.n_groups, 0, sizeof(int), s);
-    const int G = 32 * c.gw_pre;
-    c.group_threads = G;
-    groups_kernel<<<c.num_sms * 4, 256, 0, s>>>(c.node_total, R, c.nd_begin, c.nd_count, c.nd_first,
-                                                c.nd_nchild, G, c.g_begin, c.g_count, c.n_groups,
-                                                c.max_groups, c.d_err);
+    split_groups_kernel<D><<<ceil_div(c.num_chunks, 128), 128, 0, s>>>(c.st, c.keys, c.ck_begin, c.ck_count,
+                                                                   c.num_chunks, c.g_begin, c.g_count);
+    tv = tree_view(c);
+    if (c.precision == SPHGPU_FP32_PAIR)
+        node_mirror_kernel<D, float><<<c.num_sms * 8, 128, 0, s>>>(c.st, c.node_total, tv, c.nd_cf[0], c.nd_cf[1], c.nd_cf[2], c.nd_ef, (float4*)c.mir[6]);
+    else
+        node_mirror_kernel<D, double><<<c.num_sms * 8, 128, 0, s>>>(c.st, c.node_total, tv, c.nd_cf[0], c.nd_cf[1], c.nd_cf[2], c.nd_ef, (double4_32a*)c.mir[6]);
     c.tree_valid = true;
     c.kernel_size_valid = false;
 }
@@ -725,7 +769,45 @@ void launch_set_kernel_size(Ctx& c)
     ksize_kernel<<<c.num_sms * 4, 256, 0, c.stream>>>(c.st.f[F_SML], c.node_total, c.nd_begin,
                                                       c.nd_count, c.nd_first, c.nd_nchild,
                                                       c.nd_parent, c.nd_arrive, c.nd_ksize);
+    if (c.precision == SPHGPU_FP32_PAIR)
+        kernel_size_mirror_kernel<float><<<c.num_sms * 8, 256, 0, c.stream>>>(c.node_total, c.nd_ksize, c.nd_kf, c.st.f[F_SML], c.n, (float*)c.mir[7]);
+    else
+        kernel_size_mirror_kernel<double><<<c.num_sms * 8, 256, 0, c.stream>>>(c.node_total, c.nd_ksize, c.nd_kf, c.st.f[F_SML], c.n, (double*)c.mir[7]);
     c.kernel_size_valid = true;
+}
+
+int build_groups(Ctx& c)
+{
+    const int G = 32 * c.gw_pre;
+    std::vector<int> cb, cc;
+    for (int r = 0; r < c.R; ++r)
+        for (int b = c.run_begin[r]; b < c.run_begin[r + 1]; b += G) {
+            cb.push_back(b);
+            cc.push_back(std::min(G, c.run_begin[r + 1] - b));
+        }
+    const int nck = (int)cb.size();
+    const int ng = 2 * nck;
+    if (ng > c.max_groups) return SPHGPU_ERR_CAPACITY;
+    // stream-ordered copies: later kernels on the library's (non-blocking) stream read these
+    cudaError_t e = cudaStreamSynchronize(c.stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c.ck_begin, cb.data(), sizeof(int) * nck, cudaMemcpyHostToDevice, c.stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c.ck_count, cc.data(), sizeof(int) * nck, cudaMemcpyHostToDevice, c.stream);
+    // until the first tree build splits them, group 2c is chunk c and group 2c + 1 is empty
+    std::vector<int> gb(ng), gc(ng);
+    for (int q = 0; q < nck; ++q) { gb[2 * q] = cb[q]; gc[2 * q] = cc[q]; gb[2 * q + 1] = cb[q] + cc[q]; gc[2 * q + 1] = 0; }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c.g_begin, gb.data(), sizeof(int) * ng, cudaMemcpyHostToDevice, c.stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c.g_count, gc.data(), sizeof(int) * ng, cudaMemcpyHostToDevice, c.stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c.n_groups, &ng, sizeof(int), cudaMemcpyHostToDevice, c.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);   // the host vectors go out of scope
+    if (e != cudaSuccess) {
+        c.last_error = std::string("group list: ") + cudaGetErrorString(e);
+        return SPHGPU_ERR_CUDA;
+    }
+    c.group_threads = G;
+    c.num_chunks = nck;
+    c.num_groups = ng;
+    c.tree_valid = false;
+    return SPHGPU_OK;
 }
 
 }  // namespace sphgpu

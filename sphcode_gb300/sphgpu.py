@@ -30,7 +30,8 @@ STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_NODE_POOL", 4: "ERR_CAPA
           5: "ERR_NOT_FINITE", 6: "ERR_STATE", 7: "ERR_NO_DEVICE"}
 
 TUNING = {"group_warps": 0, "fluid_warps": 1, "gravity_warps": 2, "tile_cap": 3, "autotune": 4,
-          "timing": 5, "graph": 6, "graph_kernels": 7}
+          "timing": 5, "graph": 6, "graph_kernels": 7, "overflow_pre": 8, "overflow_fluid": 9,
+          "tile_cap_pre": 10, "tune_rejects": 11}
 
 
 class SphGpuError(RuntimeError):

@@ -20,7 +20,7 @@ pytestmark = pytest.mark.gpu
 FP64_TOL = 1e-9
 # Neighbour-count mismatches are allowed only at r = h ties within 1e-12 (FP64) or 2e-5 (FP32)
 # relative to h.
-FP32_TOL = {"dens": 2e-5, "sml": 2e-5, "pres": 2e-5, "gradh": 1e-4, "alpha": 1e-4, "balsara": 2e-3,
+FP32_TOL = {"dens": 2e-5, "sml": 2e-5, "pres": 2e-5, "gradh": 1e-4, "alpha": 1e-4, "balsara": 5e-3,
             "acc": 5e-3, "dene": 5e-3, "phi": 1e-5, "pos": 1e-6, "vel": 5e-3, "ene": 1e-4,
             "grad_d": 1e-3, "grad_p": 1e-3, "grad_v": 1e-3, "sound": 1e-4}
 
@@ -104,3 +104,24 @@ def test_neighbor_sets_exact(gpu_lib, case):
                 for i in range(sim.n):
                     assert set(lg[i, :cg[i]].tolist()) == set(lr[i, :cr[i]].tolist()), \
                         f"{case} is_ij={is_ij}: set of particle {i} differs"
+
+
+def test_autotuner_picks_a_candidate_and_keeps_results(gpu_lib):
+    """The schedule tuner (run by initialize) only changes launch shapes: its choice is one of
+    the candidates and the fields agree with an explicitly scheduled run to FP32-pair rounding."""
+    from sphcode_gb300 import ics, sphgpu
+    p, f = ics.khi(96, 68)
+    with sphgpu.GpuSimulation(p, f, precision="fp32") as tuned, \
+            sphgpu.GpuSimulation(p, f, precision="fp32") as fixed:
+        fixed.set_tuning("group_warps", 1)
+        tuned.initialize()
+        fixed.initialize()
+        assert tuned.get_tuning("group_warps") in (1, 2)
+        assert tuned.get_tuning("tile_cap_pre") % 32 == 0 and tuned.get_tuning("tile_cap_pre") > 0
+        assert tuned.get_tuning("tile_cap") % 32 == 0 and tuned.get_tuning("tile_cap") > 0
+        tuned.step(2)
+        fixed.step(2)
+        for name in ("dens", "sml", "pres", "acc", "dene", "pos", "vel", "ene"):
+            assert rel_err(tuned.get(name), fixed.get(name)) <= FP32_TOL[name], name
+        assert np.array_equal(tuned.get("neighbor"), fixed.get("neighbor")) or \
+            np.mean(tuned.get("neighbor") != fixed.get("neighbor")) < 1e-3
