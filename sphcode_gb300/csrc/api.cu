@@ -369,9 +369,10 @@ int create_impl(const sphgpu_params* params, int dim, int n_runs, const int* run
         A((void**)&c.d_sums, sizeof(double) * (R * maxc * 7 + R * 7));
         A((void**)&c.d_err, sizeof(unsigned));
         A((void**)&c.d_newton_fail, sizeof(int));
-        A((void**)&c.d_work, sizeof(int) * 16);
-        A((void**)&c.d_ovf_list, sizeof(int) * c.max_groups);
-        A((void**)&c.d_ovf_list2, sizeof(int) * c.max_groups);
+        A((void**)&c.d_work, sizeof(int) * 32);
+        c.ovf_cap = 2 * c.max_groups + 64;
+        A((void**)&c.d_ovf_list, sizeof(int2) * c.ovf_cap);
+        A((void**)&c.d_ovf_list2, sizeof(int2) * c.ovf_cap);
         c.stage_bytes = sizeof(double) * n * (size_t)std::max(9, dim * dim);
         A((void**)&c.d_stage, c.stage_bytes);
         // key-ordered mirrors in the pair type, sized for FP64
@@ -393,7 +394,7 @@ int create_impl(const sphgpu_params* params, int dim, int n_runs, const int* run
         cudaMemset(c.d_dt, 0, sizeof(double) * c.R);
         cudaMemset(c.d_err, 0, sizeof(unsigned));
         cudaMemset(c.d_newton_fail, 0, sizeof(int));
-        cudaMemset(c.d_work, 0, sizeof(int) * 16);
+        cudaMemset(c.d_work, 0, sizeof(int) * 32);
         fill_ord_kernel<<<ceil_div(c.R, 128), 128>>>(c.d_hvs, c.R, 1.7976931348623157e308);
         fill_ord_kernel<<<ceil_div(c.R, 128), 128>>>(c.d_dtmin, c.R, 1.7976931348623157e308);
         init_ids_kernel<<<ceil_div(c.n, THREADS), THREADS>>>(c.st.id, c.st.run, c.d_run_begin, c.R, c.n);
@@ -589,7 +590,7 @@ int kernel_occupancy(const void* kern, int threads, size_t smem)
     return nb;
 }
 
-void reset_work_counters(Ctx& c) { cudaMemsetAsync(c.d_work, 0, sizeof(int) * 16, c.stream); }
+void reset_work_counters(Ctx& c) { cudaMemsetAsync(c.d_work, 0, sizeof(int) * 32, c.stream); }
 
 void set_global_error(const std::string& text)
 {

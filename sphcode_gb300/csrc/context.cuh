@@ -53,12 +53,13 @@ struct Ctx {
     int group_threads = 32;         // group size of the current group list
     int* g_begin = nullptr;
     int* g_count = nullptr;
-    int* n_groups = nullptr;        // device copy of the group count (2 per chunk)
+    int* n_groups = nullptr;        // device copy of the group count
     int max_groups = 0;
     int num_groups = 0;
     int* ck_begin = nullptr;        // fixed chunks of group_threads particles per run
     int* ck_count = nullptr;
     int num_chunks = 0;
+    int *part_begin = nullptr, *part_count = nullptr, *part_n = nullptr;   // split scratch
 
     // per-run scalars on the device
     double* d_time = nullptr;
@@ -74,9 +75,10 @@ struct Ctx {
     // 6 {x - leaf centre, m} (tree build), 7 h (end of PreInteraction)
     void* mir[16] = {nullptr};
     // persistent-kernel work counters and the overflow group list
-    int* d_work = nullptr;          // 16 counters (pair-kernel passes: [0] [2] [4] work, [1] [3] overflow)
-    int* d_ovf_list = nullptr;      // max_groups entries: groups left by the first pass
-    int* d_ovf_list2 = nullptr;     // max_groups entries: groups left by the second pass
+    int* d_work = nullptr;          // 32 counters (pair-kernel pass p: [2p] work, [2p+1] ranges left)
+    int2* d_ovf_list = nullptr;     // target ranges left by a pass (two lists, used alternately)
+    int2* d_ovf_list2 = nullptr;
+    int ovf_cap = 0;                // capacity of each list
 
     // staging buffer for field transfers
     double* d_stage = nullptr;
@@ -151,14 +153,17 @@ int kernel_occupancy(const void* kern, int threads, size_t smem);
 void reset_work_counters(Ctx& c);
 void set_global_error(const std::string& text);   // text of sphgpu_last_error(NULL)
 
-// Three passes of a CTA-per-group pair kernel over the group list.  Pass 1 runs every group with
-// the tuned capacities at full occupancy and lists those that do not fit; pass 2 runs that list
-// with 4x the tile and larger walk capacities, still at full occupancy; pass 3 runs what is left
-// with the largest tile the shared memory holds, one CTA per SM; a group that fits nowhere sets
-// the capacity error bit.  Args must carry `L` (SmemLayout) and `work` (GroupWork).
+// Passes of a CTA-per-group pair kernel.  Pass 1 runs every group with the tuned capacities at
+// full occupancy and lists the target ranges that do not fit; pass 2 runs that list with 4x the
+// tile and larger walk capacities, still at full occupancy; pass 3 runs what is left with the
+// largest tile the shared memory holds, one CTA per SM; passes 4 to 8 run what is still left
+// with the largest tile, each on the two halves of every range the previous pass could not fit
+// (a range of 32 targets is down to single targets after five halvings).  A range that fits
+// nowhere sets the capacity error bit.  Args must carry `L` (SmemLayout) and `work` (GroupWork).
+constexpr int PAIR_PASSES = 8;
 template <class Args>
-void launch_three_pass(Ctx& c, const void* kern, Args& a, int tcap, int elt4, int eltT,
-                       void (*launch)(const void*, int, int, size_t, cudaStream_t, Args&));
+void launch_pair_passes(Ctx& c, const void* kern, Args& a, int tcap, int elt4, int eltT,
+                        void (*launch)(const void*, int, int, size_t, cudaStream_t, Args&));
 
 // The largest source tile that fits the opt-in shared memory next to the walk capacities of the
 // overflow pass.
@@ -173,27 +178,28 @@ inline int big_tile_cap(const Ctx& c, int gt, int elt4, int eltT, int stack_cap,
 }
 
 template <class Args>
-void launch_three_pass(Ctx& c, const void* kern, Args& a, int tcap, int elt4, int eltT,
-                       void (*launch)(const void*, int, int, size_t, cudaStream_t, Args&))
+void launch_pair_passes(Ctx& c, const void* kern, Args& a, int tcap, int elt4, int eltT,
+                        void (*launch)(const void*, int, int, size_t, cudaStream_t, Args&))
 {
     const int gt = c.group_threads;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, max_optin_smem(c));
     const int big = big_tile_cap(c, gt, elt4, eltT, 1024, 1024);
-    // pass 1
-    a.L = make_layout(gt, std::min(tcap, big), elt4, eltT, 128, 96);
-    a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 0, nullptr, nullptr,
-                       c.d_ovf_list, c.d_work + 1, c.d_err};
-    launch(kern, std::max(1, kernel_occupancy(kern, gt, a.L.total)) * c.num_sms, gt, a.L.total, c.stream, a);
-    // pass 2
-    a.L = make_layout(gt, std::min(4 * tcap, big), elt4, eltT, 512, 512);
-    a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 2, c.d_ovf_list, c.d_work + 1,
-                       c.d_ovf_list2, c.d_work + 3, c.d_err};
-    launch(kern, std::max(1, kernel_occupancy(kern, gt, a.L.total)) * c.num_sms, gt, a.L.total, c.stream, a);
-    // pass 3
-    a.L = make_layout(gt, big, elt4, eltT, 1024, 1024);
-    a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 4, c.d_ovf_list2, c.d_work + 3,
-                       nullptr, nullptr, c.d_err};
-    launch(kern, c.num_sms, gt, a.L.total, c.stream, a);
+    int2* lists[2] = {c.d_ovf_list, c.d_ovf_list2};
+    for (int pass = 0; pass < PAIR_PASSES; ++pass) {
+        int cap, stack_cap, leaf_cap, grid;
+        if (pass == 0) { cap = std::min(tcap, big); stack_cap = 128; leaf_cap = 96; }
+        else if (pass == 1) { cap = std::min(4 * tcap, big); stack_cap = 512; leaf_cap = 512; }
+        else { cap = big; stack_cap = 1024; leaf_cap = 1024; }
+        a.L = make_layout(gt, cap, elt4, eltT, stack_cap, leaf_cap);
+        grid = pass < 2 ? std::max(1, kernel_occupancy(kern, gt, a.L.total)) * c.num_sms : c.num_sms;
+        // work counter 2 pass, produced-range count 2 pass + 1 (zeroed with the others)
+        a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 2 * pass,
+                           pass == 0 ? nullptr : lists[(pass - 1) & 1],
+                           pass == 0 ? nullptr : c.d_work + 2 * pass - 1,
+                           pass + 1 < PAIR_PASSES ? lists[pass & 1] : nullptr,
+                           c.d_work + 2 * pass + 1, c.ovf_cap, pass >= 2 ? 1 : 0, c.d_err};
+        launch(kern, grid, gt, a.L.total, c.stream, a);
+    }
 }
 
 }  // namespace sphgpu

@@ -80,9 +80,8 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
     const int GT = blockDim.x;
 
     for (;;) {
-        const int g = next_group(gm, a.work);
-        if (g < 0) break;
-        const int gb = a.work.g_begin[g], gn = a.work.g_count[g];
+        int gb, gn;
+        if (!next_group(gm, a.work, gb, gn)) break;
         if (gn == 0) continue;   // the unused half of an unsplit chunk
         const bool active = t < gn;
         const int i = gb + (active ? t : 0);
@@ -92,7 +91,7 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
         const double hi = st.f[F_SML][i];
         group_box<D>(gm, xi, active, hi, a.pb);
         const int run = st.run[gb];
-        if (!group_walk<D, T>(smem, L, gm, a.tv, run, true, a.pb)) { report_overflow(a.work, g); continue; }
+        if (!group_walk<D, T>(smem, L, gm, a.tv, run, true, a.pb)) { report_overflow(a.work, gb, gn); continue; }
         {
             // keep sources within max(R, h_j) of the group box per axis
             const double u = Unit<T>::u;
@@ -110,7 +109,7 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
                     if (fabs(off[k]) > (he[k] + r) * rel + slack) return false;
                 return true;
             }, [&](int j) { return a.rec0[j].w; });
-            if (ntile < 0) { report_overflow(a.work, g); continue; }
+            if (ntile < 0) { report_overflow(a.work, gb, gn); continue; }
             gm->ntile = ntile;
         }
         const int ntile = gm->ntile;
@@ -389,7 +388,7 @@ void run_fluid(Ctx& c)
     a.gsph_2nd = c.p.gsph_2nd_order;
     a.dt_run = c.d_dt;
     const int tcap = c.tile_cap ? c.tile_cap : fluid_default_tile_cap<D>();
-    launch_three_pass<FluidArgs<T>>(c, (const void*)kern, a, tcap, sizeof(V4), sizeof(T),
+    launch_pair_passes<FluidArgs<T>>(c, (const void*)kern, a, tcap, sizeof(V4), sizeof(T),
         [](const void* k, int grid, int block, size_t smem, cudaStream_t st, FluidArgs<T>& args) {
             reinterpret_cast<void (*)(FluidArgs<T>)>(const_cast<void*>(k))<<<grid, block, smem, st>>>(args);
         });

@@ -149,41 +149,61 @@ struct MaskIter {
     __device__ __forceinline__ void clear_current() { mask[w * gt + t] &= ~(1u << b); }
 };
 
-// Work distribution: next group for this CTA (block-uniform), or -1 when done.
+// Work distribution.  A work item is a range of key-consecutive targets (begin, count).  The
+// first pass takes the group list; later passes take the ranges earlier passes could not fit.
 struct GroupWork {
     const int* g_begin;
     const int* g_count;
     const int* n_groups;      // number of groups (device)
     int* counter;             // work counter (device, zeroed before the launch)
-    const int* list;          // optional explicit group list (overflow pass)
+    const int2* list;         // ranges left by the previous pass (nullptr in the first pass)
     const int* list_count;
-    int* ovf_list;            // overflow output (main pass) or nullptr
+    int2* ovf_list;           // ranges this pass cannot fit (nullptr in the last pass)
     int* ovf_count;
+    int ovf_cap;
+    int halve;                // pass a failing range on as its two halves
     unsigned* err;
 };
 
-__device__ __forceinline__ int next_group(GroupMisc* gm, const GroupWork& w)
+// Next work item for this CTA (block-uniform); false when done.
+__device__ __forceinline__ bool next_group(GroupMisc* gm, const GroupWork& w, int& gb, int& gn)
 {
     __syncthreads();
     if (threadIdx.x == 0) {
         const int k = atomicAdd(w.counter, 1);
-        int g = -1;
-        if (w.list) { if (k < *w.list_count) g = w.list[k]; }
-        else if (k < *w.n_groups) g = k;
-        gm->group = g;
+        int b = -1, n = 0;
+        if (w.list) {
+            if (k < *w.list_count) { const int2 r = w.list[k]; b = r.x; n = r.y; }
+        } else if (k < *w.n_groups) {
+            b = w.g_begin[k];
+            n = w.g_count[k];
+        }
+        gm->group = b;
+        gm->ntile = n;   // scratch: the range length
     }
     __syncthreads();
-    return gm->group;
+    gb = gm->group;
+    gn = gm->ntile;
+    return gb >= 0;
 }
 
-__device__ __forceinline__ void report_overflow(const GroupWork& w, int g)
+__device__ __forceinline__ void push_range(const GroupWork& w, int b, int n)
+{
+    const int k = atomicAdd(w.ovf_count, 1);
+    if (k < w.ovf_cap) w.ovf_list[k] = make_int2(b, n);
+    else atomicOr(w.err, (unsigned)ERR_TILE);
+}
+
+__device__ __forceinline__ void report_overflow(const GroupWork& w, int gb, int gn)
 {
     if (threadIdx.x == 0) {
-        if (w.ovf_list) {
-            const int k = atomicAdd(w.ovf_count, 1);
-            w.ovf_list[k] = g;
-        } else {
+        if (!w.ovf_list) {
             atomicOr(w.err, (unsigned)ERR_TILE);
+        } else if (w.halve && gn > 1) {
+            push_range(w, gb, gn / 2);
+            push_range(w, gb + gn / 2, gn - gn / 2);
+        } else {
+            push_range(w, gb, gn);
         }
     }
 }

@@ -33,9 +33,8 @@ __global__ void __launch_bounds__(256) neighbors_kernel(NbArgs<T> a)
     const State& st = a.st;
     const int t = threadIdx.x;
     for (;;) {
-        const int g = next_group(gm, a.work);
-        if (g < 0) break;
-        const int gb = a.work.g_begin[g], gn = a.work.g_count[g];
+        int gb, gn;
+        if (!next_group(gm, a.work, gb, gn)) break;
         if (gn == 0) continue;   // the unused half of an unsplit chunk
         const bool active = t < gn;
         const int i = gb + (active ? t : 0);
@@ -45,7 +44,7 @@ __global__ void __launch_bounds__(256) neighbors_kernel(NbArgs<T> a)
         const double hi = st.f[F_SML][i];
         group_box<D>(gm, xi, active, hi, a.pb);
         const int run = st.run[gb];
-        if (!group_walk<D, T>(smem, L, gm, a.tv, run, a.is_ij != 0, a.pb)) { report_overflow(a.work, g); continue; }
+        if (!group_walk<D, T>(smem, L, gm, a.tv, run, a.is_ij != 0, a.pb)) { report_overflow(a.work, gb, gn); continue; }
         {
             const double u = Unit<T>::u;
             const T Rt = to_T_up<T>(gm->R);
@@ -63,7 +62,7 @@ __global__ void __launch_bounds__(256) neighbors_kernel(NbArgs<T> a)
                     if (fabs(off[k]) > (he[k] + r) * rel + slack) return false;
                 return true;
             }, [&](int) { return T(0); });
-            if (ntile < 0) { report_overflow(a.work, g); continue; }
+            if (ntile < 0) { report_overflow(a.work, gb, gn); continue; }
             gm->ntile = ntile;
         }
         const int ntile = gm->ntile;
@@ -105,7 +104,7 @@ void run_neighbors(Ctx& c, int is_ij, int* d_counts, int* d_list, int cap)
     a.list = d_list;
     a.cap = cap;
     auto kern = neighbors_kernel<D, T>;
-    launch_three_pass<NbArgs<T>>(c, (const void*)kern, a, D == 1 ? 128 : 1024, sizeof(V4), sizeof(T),
+    launch_pair_passes<NbArgs<T>>(c, (const void*)kern, a, D == 1 ? 128 : 1024, sizeof(V4), sizeof(T),
         [](const void* k, int grid, int block, size_t smem, cudaStream_t st, NbArgs<T>& args) {
             reinterpret_cast<void (*)(NbArgs<T>)>(const_cast<void*>(k))<<<grid, block, smem, st>>>(args);
         });

@@ -66,9 +66,8 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
     constexpr double A = volume_const<D>();
 
     for (;;) {
-        const int g = next_group(gm, a.work);
-        if (g < 0) break;
-        const int gb = a.work.g_begin[g], gn = a.work.g_count[g];
+        int gb, gn;
+        if (!next_group(gm, a.work, gb, gn)) break;
         if (gn == 0) continue;   // the unused half of an unsplit chunk
         const bool active = t < gn;
         const int i = gb + (active ? t : 0);
@@ -80,7 +79,7 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
         const double hs = a.initial ? hg : hg * a.ratio;
         group_box<D>(gm, xi, active, hs, a.pb);
         const int run = st.run[gb];
-        if (!group_walk<D, T>(smem, L, gm, a.tv, run, false, a.pb)) { report_overflow(a.work, g); continue; }
+        if (!group_walk<D, T>(smem, L, gm, a.tv, run, false, a.pb)) { report_overflow(a.work, gb, gn); continue; }
         {
             T lim[D];
 #pragma unroll
@@ -92,7 +91,7 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
                     if (fabs(off[k]) > lim[k]) return false;
                 return true;
             }, [&](int j) { return mu[j]; });
-            if (ntile < 0) { report_overflow(a.work, g); continue; }
+            if (ntile < 0) { report_overflow(a.work, gb, gn); continue; }
             gm->ntile = ntile;   // every thread writes the same value
         }
         const int ntile = gm->ntile;
@@ -422,8 +421,8 @@ void run_pre(Ctx& c, bool initial)
     cudaStream_t s = c.stream;
     pre_mirror_kernel<D, T><<<ceil_div(c.n, 256), 256, 0, s>>>(c.st, c.n, (V4*)c.mir[0], (T*)c.mir[1]);
     // counters: [0] main work, [1] overflow count, [2] overflow work; plus h/v_sig and Newton
-    if (!initial) pre_reset_kernel<<<ceil_div(std::max(c.R, 16), 128), 128, 0, s>>>(c.R, c.d_hvs, c.d_work, 16);
-    else pre_reset_kernel<<<1, 32, 0, s>>>(0, c.d_hvs, c.d_work, 16);
+    if (!initial) pre_reset_kernel<<<ceil_div(std::max(c.R, 32), 128), 128, 0, s>>>(c.R, c.d_hvs, c.d_work, 32);
+    else pre_reset_kernel<<<1, 32, 0, s>>>(0, c.d_hvs, c.d_work, 32);
     cudaMemsetAsync(c.d_newton_fail, 0, sizeof(int), s);
     PreArgs<T> a{};
     a.st = c.st;
@@ -447,7 +446,7 @@ void run_pre(Ctx& c, bool initial)
     a.hvs = c.d_hvs;
     a.newton_fail = c.d_newton_fail;
     const int tcap = c.tile_cap_pre ? c.tile_cap_pre : default_tile_cap<D>();
-    launch_three_pass<PreArgs<T>>(c, (const void*)kern, a, tcap, sizeof(V4), sizeof(T),
+    launch_pair_passes<PreArgs<T>>(c, (const void*)kern, a, tcap, sizeof(V4), sizeof(T),
         [](const void* k, int grid, int block, size_t smem, cudaStream_t st, PreArgs<T>& args) {
             reinterpret_cast<void (*)(PreArgs<T>)>(const_cast<void*>(k))<<<grid, block, smem, st>>>(args);
         });

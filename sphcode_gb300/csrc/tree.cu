@@ -488,44 +488,116 @@ __global__ void ksize_kernel(const double* sml, const int* node_total_p, int* be
 }
 
 // ---- target groups ----------------------------------------------------------------------------
-// Each fixed chunk of key-consecutive particles becomes group 2c; where the chunk straddles a
-// high-level node boundary (its two halves at the highest differing key bit are each less than
-// half its extent) it is split there, the second part becoming group 2c + 1 (else empty).
+// Each fixed chunk of key-consecutive particles is split at the highest key bit in which its
+// first and last particle differ whenever both halves are less than half as wide as the whole
+// (the chunk straddles an octree boundary), recursively up to GROUP_SPLIT_DEPTH times; the parts
+// are then compacted into the group list in chunk order.
+constexpr int GROUP_SPLIT_DEPTH = 1;
+constexpr int GROUP_PARTS = 1 << GROUP_SPLIT_DEPTH;
+
+template <int D>
+__device__ double range_extent(const State& st, int b, int e)
+{
+    double ext = 0.0;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        double lo = 1.7976931348623157e308, hi = -lo;
+        for (int i = b; i < e; ++i) {
+            const double x = st.f[F_POS + k][i];
+            lo = fmin(lo, x);
+            hi = fmax(hi, x);
+        }
+        ext = fmax(ext, hi - lo);
+    }
+    return ext;
+}
+
 template <int D>
 __global__ void split_groups_kernel(State st, const unsigned long long* keys, const int* ck_begin,
-                                    const int* ck_count, int nchunks, int* g_begin, int* g_count)
+                                    const int* ck_count, int nchunks, int* part_begin, int* part_count,
+                                    int* nparts)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nchunks) return;
-    const int b = ck_begin[c], e = b + ck_count[c];
-    int s = e;
-    const unsigned long long diff = keys[b] ^ keys[e - 1];
-    if (diff) {
-        const unsigned long long bit = 1ull << (63 - __clzll((long long)diff));
-        int lo = b, hi = e - 1;   // first index with the bit set
-        while (lo < hi) {
-            const int mid = (lo + hi) >> 1;
-            if (keys[mid] & bit) hi = mid; else lo = mid + 1;
-        }
-        double ext = 0.0, ea = 0.0, eb = 0.0;
-#pragma unroll
-        for (int k = 0; k < D; ++k) {
-            double a0 = 1.7976931348623157e308, a1 = -a0, b0 = a0, b1 = -a0;
-            for (int i = b; i < e; ++i) {
-                const double x = st.f[F_POS + k][i];
-                if (i < lo) { a0 = fmin(a0, x); a1 = fmax(a1, x); }
-                else { b0 = fmin(b0, x); b1 = fmax(b1, x); }
+    int pb[GROUP_PARTS], pe[GROUP_PARTS], pd[GROUP_PARTS];
+    int np = 0, out = 0;
+    int ob[GROUP_PARTS], oc[GROUP_PARTS];
+    pb[0] = ck_begin[c];
+    pe[0] = pb[0] + ck_count[c];
+    pd[0] = 0;
+    np = 1;
+    while (np > 0) {
+        --np;
+        const int b = pb[np], e = pe[np], d = pd[np];
+        int s = e;
+        const unsigned long long diff = keys[b] ^ keys[e - 1];
+        if (diff && d < GROUP_SPLIT_DEPTH && e - b > 1) {
+            const unsigned long long bit = 1ull << (63 - __clzll((long long)diff));
+            int lo = b, hi = e - 1;   // first index with the bit set
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (keys[mid] & bit) hi = mid; else lo = mid + 1;
             }
-            ext = fmax(ext, fmax(a1, b1) - fmin(a0, b0));
-            ea = fmax(ea, a1 - a0);
-            eb = fmax(eb, b1 - b0);
+            if (lo > b) {
+                const double ext = range_extent<D>(st, b, e);
+                const double ea = range_extent<D>(st, b, lo), eb = range_extent<D>(st, lo, e);
+                if (fmax(ea, eb) < 0.5 * ext) s = lo;
+            }
         }
-        if (lo > b && fmax(ea, eb) < 0.5 * ext) s = lo;
+        if (s < e) {
+            // second half first on the stack so that parts come out in key order
+            pb[np] = s; pe[np] = e; pd[np] = d + 1; ++np;
+            pb[np] = b; pe[np] = s; pd[np] = d + 1; ++np;
+        } else {
+            ob[out] = b;
+            oc[out] = e - b;
+            ++out;
+        }
     }
-    g_begin[2 * c] = b;
-    g_count[2 * c] = s - b;
-    g_begin[2 * c + 1] = s;
-    g_count[2 * c + 1] = e - s;
+    for (int q = 0; q < out; ++q) {
+        part_begin[(size_t)c * GROUP_PARTS + q] = ob[q];
+        part_count[(size_t)c * GROUP_PARTS + q] = oc[q];
+    }
+    nparts[c] = out;
+}
+
+// Exclusive scan of the per-chunk part counts in one block; total to *n_groups.
+__global__ void scan_parts_kernel(int* nparts, int nchunks, int* n_groups)
+{
+    __shared__ int part[1024];
+    const int t = threadIdx.x;
+    const int per = (nchunks + 1023) / 1024;
+    const int b = t * per, e = min(nchunks, b + per);
+    int sum = 0;
+    for (int i = b; i < e; ++i) sum += nparts[i];
+    part[t] = sum;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const int v = t >= o ? part[t - o] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    int run = t > 0 ? part[t - 1] : 0;
+    for (int i = b; i < e; ++i) {
+        const int v = nparts[i];
+        nparts[i] = run;
+        run += v;
+    }
+    if (t == 1023) *n_groups = part[1023];
+}
+
+__global__ void compact_groups_kernel(const int* part_begin, const int* part_count, const int* offs,
+                                      const int* n_groups, int nchunks, int* g_begin, int* g_count)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nchunks) return;
+    const int o = offs[c];
+    const int cnt = (c + 1 < nchunks ? offs[c + 1] : *n_groups) - o;
+    for (int q = 0; q < cnt; ++q) {
+        g_begin[o + q] = part_begin[(size_t)c * GROUP_PARTS + q];
+        g_count[o + q] = part_count[(size_t)c * GROUP_PARTS + q];
+    }
 }
 
 // ---- FP32 node copies and leaf-relative particle offsets ------------------------------------
@@ -624,11 +696,15 @@ int tree_alloc(Ctx& c)
     A((void**)&c.chunk_sum, sizeof(int) * (ceil_div(nc, LEVEL_CHUNK) + 1));
     A((void**)&c.bbox, sizeof(long long) * 2 * 3 * c.R);
     A((void**)&c.node_total, sizeof(int));
-    c.max_groups = 2 * (n / 32 + c.R + 1);
+    const int max_chunks = n / 32 + c.R + 1;
+    c.max_groups = GROUP_PARTS * max_chunks;
     A((void**)&c.g_begin, sizeof(int) * c.max_groups);
     A((void**)&c.g_count, sizeof(int) * c.max_groups);
-    A((void**)&c.ck_begin, sizeof(int) * (c.max_groups / 2));
-    A((void**)&c.ck_count, sizeof(int) * (c.max_groups / 2));
+    A((void**)&c.ck_begin, sizeof(int) * max_chunks);
+    A((void**)&c.ck_count, sizeof(int) * max_chunks);
+    A((void**)&c.part_begin, sizeof(int) * c.max_groups);
+    A((void**)&c.part_count, sizeof(int) * c.max_groups);
+    A((void**)&c.part_n, sizeof(int) * max_chunks);
     A((void**)&c.n_groups, sizeof(int));
     if (e != cudaSuccess) {
         c.last_error = std::string("tree allocation: ") + cudaGetErrorString(e);
@@ -645,7 +721,8 @@ void tree_free(Ctx& c)
                     c.nd_center[1], c.nd_center[2], c.nd_com[0], c.nd_com[1], c.nd_com[2],
                     c.nd_edge, c.nd_mass, c.nd_ksize, c.lvl_start, c.lvl_tmp, c.chunk_sum, c.bbox,
                     c.node_total, c.g_begin, c.g_count, c.n_groups, c.nd_cf[0], c.nd_cf[1],
-                    c.nd_cf[2], c.nd_ef, c.nd_kf, c.ck_begin, c.ck_count};
+                    c.nd_cf[2], c.nd_ef, c.nd_kf, c.ck_begin, c.ck_count, c.part_begin,
+                    c.part_count, c.part_n};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -730,7 +807,12 @@ static void make_tree_d(Ctx& c, bool reorder_all)
     cudaMemcpyAsync(c.node_total, c.lvl_start + levels + 2, sizeof(int), cudaMemcpyDeviceToDevice, s);
     launch_node_moments(c);
     split_groups_kernel<D><<<ceil_div(c.num_chunks, 128), 128, 0, s>>>(c.st, c.keys, c.ck_begin, c.ck_count,
-                                                                   c.num_chunks, c.g_begin, c.g_count);
+                                                                   c.num_chunks, c.part_begin, c.part_count,
+                                                                   c.part_n);
+    scan_parts_kernel<<<1, 1024, 0, s>>>(c.part_n, c.num_chunks, c.n_groups);
+    compact_groups_kernel<<<ceil_div(c.num_chunks, 128), 128, 0, s>>>(c.part_begin, c.part_count, c.part_n,
+                                                                     c.n_groups, c.num_chunks, c.g_begin,
+                                                                     c.g_count);
     tv = tree_view(c);
     if (c.precision == SPHGPU_FP32_PAIR)
         node_mirror_kernel<D, float><<<c.num_sms * 8, 128, 0, s>>>(c.st, c.node_total, tv, c.nd_cf[0], c.nd_cf[1], c.nd_cf[2], c.nd_ef, (float4*)c.mir[6]);
@@ -786,17 +868,14 @@ int build_groups(Ctx& c)
             cc.push_back(std::min(G, c.run_begin[r + 1] - b));
         }
     const int nck = (int)cb.size();
-    const int ng = 2 * nck;
+    const int ng = nck;   // until the first tree build splits them, the groups are the chunks
     if (ng > c.max_groups) return SPHGPU_ERR_CAPACITY;
     // stream-ordered copies: later kernels on the library's (non-blocking) stream read these
     cudaError_t e = cudaStreamSynchronize(c.stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(c.ck_begin, cb.data(), sizeof(int) * nck, cudaMemcpyHostToDevice, c.stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(c.ck_count, cc.data(), sizeof(int) * nck, cudaMemcpyHostToDevice, c.stream);
-    // until the first tree build splits them, group 2c is chunk c and group 2c + 1 is empty
-    std::vector<int> gb(ng), gc(ng);
-    for (int q = 0; q < nck; ++q) { gb[2 * q] = cb[q]; gc[2 * q] = cc[q]; gb[2 * q + 1] = cb[q] + cc[q]; gc[2 * q + 1] = 0; }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(c.g_begin, gb.data(), sizeof(int) * ng, cudaMemcpyHostToDevice, c.stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(c.g_count, gc.data(), sizeof(int) * ng, cudaMemcpyHostToDevice, c.stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c.g_begin, cb.data(), sizeof(int) * nck, cudaMemcpyHostToDevice, c.stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c.g_count, cc.data(), sizeof(int) * nck, cudaMemcpyHostToDevice, c.stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(c.n_groups, &ng, sizeof(int), cudaMemcpyHostToDevice, c.stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);   // the host vectors go out of scope
     if (e != cudaSuccess) {
