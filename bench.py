@@ -43,7 +43,11 @@ def fluid_bytes_per_particle(D):
 
 
 def workload(name):
+    """(params, fields, description, run sizes or None)."""
     from sphcode_gb300 import ics
+    if name == "ensemble":
+        p, f, sizes = ics.ensemble()
+        return p, f, "ensemble_1d_gsph2_4096_tubes", sizes
     if name == "khi":
         p, f = ics.khi()
         desc = "khi_2d_disph_wendland_ac"
@@ -58,7 +62,7 @@ def workload(name):
         desc = "sod_1d_ssph_cubic"
     else:
         raise SystemExit(f"unknown workload {name}")
-    return p, f, desc
+    return p, f, desc, None
 
 
 # ---- clocks --------------------------------------------------------------------------------
@@ -144,10 +148,29 @@ def cpu_reference_run(name, steps, threads):
     reference Makefile's flags) or, where they are not built, the C restatement in oracle/, on
     the host cores.  Returns (particle-steps/s, kind, sample text, seconds)."""
     from oracle import pyoracle
-    p, f, desc = workload(name)
+    p, f, desc, runs = workload(name)
     kind = "reference" if pyoracle.reference_available("fast") else "port"
-    sim = pyoracle.OracleSim(p, f, kind="ref" if kind == "reference" else "port", flavor="fast",
-                             threads=threads)
+    okind = "ref" if kind == "reference" else "port"
+    if runs is not None:
+        # the reference runs one tube per process: time the first tubes one after another
+        begins = np.concatenate([[0], np.cumsum(runs)])
+        ntubes = min(len(runs), 64)
+        dt = 0.0
+        n = 0
+        for r in range(ntubes):
+            sub = {k: np.asarray(v)[begins[r]:begins[r + 1]] for k, v in f.items()}
+            sim = pyoracle.OracleSim(p, sub, kind=okind, flavor="fast", threads=threads)
+            sim.initialize()
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                sim.step()
+            dt += time.perf_counter() - t0
+            n += sim.n
+            sim.close()
+        sample = (f"{desc}: the first {ntubes} tubes ({n} particles) one after another, "
+                  f"{steps} timed steps each after an untimed initialize, {threads} OpenMP threads")
+        return n * steps / dt, kind, sample, dt
+    sim = pyoracle.OracleSim(p, f, kind=okind, flavor="fast", threads=threads)
     t0 = time.perf_counter()
     sim.initialize()
     t_init = time.perf_counter() - t0
@@ -169,7 +192,7 @@ def run_reference_arm(args):
     threads = os.cpu_count() or 1
     steps = max(1, min(args.steps, args.ref_steps))
     value, kind, sample, secs = cpu_reference_run(args.workload, steps, threads)
-    _, _, desc = workload(args.workload)
+    _, _, desc, _ = workload(args.workload)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "particle-steps/s",
             "n_gpus": args.gpus, "steps": steps, "warmup": 0, "ms_per_step": secs / steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -209,8 +232,8 @@ def main():
         import __graft_entry__ as g
         g.build()
         from sphcode_gb300 import sphgpu
-        p, f, desc = workload(args.workload)
-        with sphgpu.GpuSimulation(p, f, precision=args.precision) as sim:
+        p, f, desc, runs = workload(args.workload)
+        with sphgpu.GpuSimulation(p, f, precision=args.precision, runs=runs) as sim:
             sim.set_tuning("graph", 0)
             sim.initialize()
             sim.step(args.steps)
@@ -237,7 +260,7 @@ def main():
         dist.barrier()
     from sphcode_gb300 import sphgpu
 
-    p, f, desc = workload(args.workload)
+    p, f, desc, runs = workload(args.workload)
     n = int(f["mass"].shape[0])
     D = p.dim
 
@@ -255,7 +278,7 @@ def main():
 
     # ---- FP32-pair form: device-resident throughput --------------------------------------
     def make(prec):
-        s_ = sphgpu.GpuSimulation(p, f, precision=prec)
+        s_ = sphgpu.GpuSimulation(p, f, precision=prec, runs=runs)
         if args.group_warps:
             s_.set_tuning("group_warps", args.group_warps)
         if args.tile_pre:

@@ -157,3 +157,17 @@ def ensemble_tubes(n_runs: int = 4096, n_min: int = 200, n_max: int = 5000, seed
         nl = min(max(nl, 1), counts[k] - 1)
         tubes.append(dict(n_left=nl, n_right=int(counts[k] - nl), rho_l=rl, rho_r=rr, p_l=pl, p_r=pr))
     return tubes
+
+
+def ensemble(n_runs: int = 4096, n_min: int = 200, n_max: int = 5000, seed: int = 20261203):
+    """The gsph ensemble as one batch: ``(params, fields, run_sizes)`` with the tubes of
+    :func:`ensemble_tubes` stored back to back (each tube keeps its own coordinates in
+    [-0.5, 0.5]; runs never interact)."""
+    tubes = ensemble_tubes(n_runs, n_min, n_max, seed)
+    parts = [shock_tube_gsph(t["n_left"], t["n_right"], t["rho_l"], t["rho_r"], t["p_l"], t["p_r"])
+             for t in tubes]
+    p = parts[0][0]
+    names = parts[0][1].keys()
+    fields = {k: np.concatenate([f[k] for _, f in parts]) for k in names}
+    sizes = [int(f["mass"].shape[0]) for _, f in parts]
+    return p, fields, sizes
