@@ -34,6 +34,7 @@ struct Ctx {
     unsigned long long *keys = nullptr, *keys_alt = nullptr;
     int *perm = nullptr, *perm_alt = nullptr;
     int* radix_hist = nullptr;      // 256 * max blocks
+    int* radix_dtot = nullptr;      // 256 digit totals
     int radix_blocks = 0;
 
     // tree (breadth-first node arrays)

@@ -147,16 +147,18 @@ __global__ void radix_hist_kernel(const unsigned long long* keys, int n, int shi
     hist[threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
 }
 
-// Exclusive scan of m ints in one block of 1024 threads.
-__global__ void scan_single_block_kernel(int* data, int m)
+// Exclusive scan of each digit's column of per-block counts (hist[d * nblocks + b]), one block per
+// digit; the digit totals go to dtot.
+__global__ void radix_scan_columns_kernel(int* hist, int nblocks, int* dtot)
 {
     __shared__ int part[1024];
+    int* col = hist + (size_t)blockIdx.x * nblocks;
     const int t = threadIdx.x;
-    const int per = (m + 1023) / 1024;
-    const int b = t * per, e = min(m, b + per);
-    int s = 0;
-    for (int i = b; i < e; ++i) s += data[i];
-    part[t] = s;
+    const int per = (nblocks + 1023) / 1024;
+    const int b = t * per, e = min(nblocks, b + per);
+    int sum = 0;
+    for (int i = b; i < e; ++i) sum += col[i];
+    part[t] = sum;
     __syncthreads();
     for (int o = 1; o < 1024; o <<= 1) {
         const int v = t >= o ? part[t - o] : 0;
@@ -166,20 +168,32 @@ __global__ void scan_single_block_kernel(int* data, int m)
     }
     int run = t > 0 ? part[t - 1] : 0;
     for (int i = b; i < e; ++i) {
-        const int v = data[i];
-        data[i] = run;
+        const int v = col[i];
+        col[i] = run;
         run += v;
     }
+    if (t == 1023) dtot[blockIdx.x] = part[1023];
 }
 
 __global__ void radix_scatter_kernel(const unsigned long long* kin, const int* vin,
                                      unsigned long long* kout, int* vout, int n, int shift,
-                                     const int* hist, int nblocks)
+                                     const int* hist, int nblocks, const int* dtot)
 {
     __shared__ int base[256];
     __shared__ int wcnt[RADIX_THREADS / 32][256];
     const int t = threadIdx.x, w = t >> 5, lane = t & 31;
-    base[t] = hist[t * nblocks + blockIdx.x];
+    // digit offset = sum of the totals of the smaller digits (block scan of dtot)
+    base[t] = dtot[t];
+    __syncthreads();
+    for (int o = 1; o < 256; o <<= 1) {
+        const int v = t >= o ? base[t - o] : 0;
+        __syncthreads();
+        base[t] += v;
+        __syncthreads();
+    }
+    const int excl = base[t] - dtot[t];
+    __syncthreads();
+    base[t] = excl + hist[t * nblocks + blockIdx.x];
     for (int round = 0; round < RADIX_ITEMS; ++round) {
         const int idx = blockIdx.x * RADIX_TILE + round * RADIX_THREADS + t;
         const bool valid = idx < n;
@@ -394,54 +408,44 @@ __global__ void level_emit_kernel(NodeArrays na, const unsigned long long* keys,
     }
 }
 
-// ---- bottom-up reductions ---------------------------------------------------------------
+// ---- bottom-up reductions, one tree level per launch -------------------------------------------
+// Level l occupies the node range [lvl_start[l], lvl_start[l + 1]) of the breadth-first arrays;
+// deeper levels are done first, so a node reads its finished children (no atomics, and the sums
+// do not depend on scheduling).
 
-// Mass and sum of m x per node: leaves sum their particles; the last child to finish sums its
-// parent's children (in child order, so the result does not depend on scheduling).
+// Mass and sum of m x per node: leaves sum their particles, inner nodes their children.  The roots
+// keep zero mass and centre, as in the reference, whose root never receives them.
 template <int D>
-__global__ void moments_kernel(State st, const int* node_total_p, int R, int* begin, int* count,
-                               int* first, int* nchild, int* parent, int* arrive, double* mass,
-                               double* mx0, double* mx1, double* mx2)
+__global__ void moments_level_kernel(State st, const int* lvl_start, int l, int R, const int* begin,
+                                     const int* count, const int* first, const int* nchild,
+                                     double* mass, double* mx0, double* mx1, double* mx2)
 {
     double* mx[3] = {mx0, mx1, mx2};
-    const int total = *node_total_p;
-    for (int i = R + blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-        if (first[i] >= 0) continue;
-        double m = 0.0, s[D];
+    const int s = lvl_start[l], e = lvl_start[l + 1];
+    for (int i = max(s, R) + blockIdx.x * blockDim.x + threadIdx.x; i < e; i += gridDim.x * blockDim.x) {
+        double m = 0.0, sx[D];
 #pragma unroll
-        for (int k = 0; k < D; ++k) s[k] = 0.0;
-        const int b = begin[i], e = b + count[i];
-        for (int j = b; j < e; ++j) {
-            const double mj = st.f[F_MASS][j];
-            m += mj;
+        for (int k = 0; k < D; ++k) sx[k] = 0.0;
+        const int fc = first[i];
+        if (fc < 0) {
+            const int b = begin[i], en = b + count[i];
+            for (int j = b; j < en; ++j) {
+                const double mj = st.f[F_MASS][j];
+                m += mj;
 #pragma unroll
-            for (int k = 0; k < D; ++k) s[k] += st.f[F_POS + k][j] * mj;
+                for (int k = 0; k < D; ++k) sx[k] += st.f[F_POS + k][j] * mj;
+            }
+        } else {
+            const int nc = nchild[i];
+            for (int c = 0; c < nc; ++c) {
+                m += mass[fc + c];
+#pragma unroll
+                for (int k = 0; k < D; ++k) sx[k] += mx[k][fc + c];
+            }
         }
         mass[i] = m;
 #pragma unroll
-        for (int k = 0; k < D; ++k) mx[k][i] = s[k];
-        int node = i;
-        while (true) {
-            const int p = parent[node];
-            if (p < R) break;   // roots keep zero mass and centre (reference quirk)
-            __threadfence();
-            const int old = atomicAdd(&arrive[p], 1);
-            if (old != nchild[p] - 1) break;
-            __threadfence();
-            const int fc = first[p], nc = nchild[p];
-            double pm = 0.0, ps[D];
-#pragma unroll
-            for (int k = 0; k < D; ++k) ps[k] = 0.0;
-            for (int c = 0; c < nc; ++c) {
-                pm += __ldcg(&mass[fc + c]);
-#pragma unroll
-                for (int k = 0; k < D; ++k) ps[k] += __ldcg(&mx[k][fc + c]);
-            }
-            mass[p] = pm;
-#pragma unroll
-            for (int k = 0; k < D; ++k) mx[k][p] = ps[k];
-            node = p;
-        }
+        for (int k = 0; k < D; ++k) mx[k][i] = sx[k];
     }
 }
 
@@ -459,31 +463,22 @@ __global__ void com_finalize_kernel(const int* node_total_p, int R, const double
     }
 }
 
-// Per-node maximum smoothing length (BHNode::set_kernel, src/bhtree.cpp:206-232), bottom-up.
-__global__ void ksize_kernel(const double* sml, const int* node_total_p, int* begin, int* count,
-                             int* first, int* nchild, int* parent, int* arrive, double* ksize)
+// Per-node maximum smoothing length (BHNode::set_kernel, src/bhtree.cpp:206-232).
+__global__ void ksize_level_kernel(const double* sml, const int* lvl_start, int l, const int* begin,
+                                   const int* count, const int* first, const int* nchild, double* ksize)
 {
-    const int total = *node_total_p;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-        if (first[i] >= 0) continue;
+    const int s = lvl_start[l], e = lvl_start[l + 1];
+    for (int i = s + blockIdx.x * blockDim.x + threadIdx.x; i < e; i += gridDim.x * blockDim.x) {
         double h = 0.0;
-        const int b = begin[i], e = b + count[i];
-        for (int j = b; j < e; ++j) h = fmax(h, sml[j]);
-        ksize[i] = h;
-        int node = i;
-        while (true) {
-            const int p = parent[node];
-            if (p < 0) break;
-            __threadfence();
-            const int old = atomicAdd(&arrive[p], 1);
-            if (old != nchild[p] - 1) break;
-            __threadfence();
-            const int fc = first[p], nc = nchild[p];
-            double hm = 0.0;
-            for (int c = 0; c < nc; ++c) hm = fmax(hm, __ldcg(&ksize[fc + c]));
-            ksize[p] = hm;
-            node = p;
+        const int fc = first[i];
+        if (fc < 0) {
+            const int b = begin[i], en = b + count[i];
+            for (int j = b; j < en; ++j) h = fmax(h, sml[j]);
+        } else {
+            const int nc = nchild[i];
+            for (int c = 0; c < nc; ++c) h = fmax(h, ksize[fc + c]);
         }
+        ksize[i] = h;
     }
 }
 
@@ -674,6 +669,7 @@ int tree_alloc(Ctx& c)
     A((void**)&c.perm_alt, sizeof(int) * n);
     c.radix_blocks = ceil_div(n, RADIX_TILE);
     A((void**)&c.radix_hist, sizeof(int) * 256 * c.radix_blocks);
+    A((void**)&c.radix_dtot, sizeof(int) * 256);
     A((void**)&c.nd_begin, sizeof(int) * nc);
     A((void**)&c.nd_count, sizeof(int) * nc);
     A((void**)&c.nd_first, sizeof(int) * nc);
@@ -721,7 +717,7 @@ void tree_free(Ctx& c)
                     c.nd_center[1], c.nd_center[2], c.nd_com[0], c.nd_com[1], c.nd_com[2],
                     c.nd_edge, c.nd_mass, c.nd_ksize, c.lvl_start, c.lvl_tmp, c.chunk_sum, c.bbox,
                     c.node_total, c.g_begin, c.g_count, c.n_groups, c.nd_cf[0], c.nd_cf[1],
-                    c.nd_cf[2], c.nd_ef, c.nd_kf, c.ck_begin, c.ck_count, c.part_begin,
+                    c.nd_cf[2], c.nd_ef, c.nd_kf, c.ck_begin, c.ck_count, c.radix_dtot, c.part_begin,
                     c.part_count, c.part_n};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -782,9 +778,9 @@ static void make_tree_d(Ctx& c, bool reorder_all)
     for (int p = 0; p < passes; ++p) {
         const int shift = 8 * p;
         radix_hist_kernel<<<c.radix_blocks, RADIX_THREADS, 0, s>>>(c.keys, n, shift, c.radix_hist, c.radix_blocks);
-        scan_single_block_kernel<<<1, 1024, 0, s>>>(c.radix_hist, 256 * c.radix_blocks);
+        radix_scan_columns_kernel<<<256, 1024, 0, s>>>(c.radix_hist, c.radix_blocks, c.radix_dtot);
         radix_scatter_kernel<<<c.radix_blocks, RADIX_THREADS, 0, s>>>(
-            c.keys, c.perm, c.keys_alt, c.perm_alt, n, shift, c.radix_hist, c.radix_blocks);
+            c.keys, c.perm, c.keys_alt, c.perm_alt, n, shift, c.radix_hist, c.radix_blocks, c.radix_dtot);
         std::swap(c.keys, c.keys_alt);
         std::swap(c.perm, c.perm_alt);
     }
@@ -831,26 +827,26 @@ void launch_make_tree(Ctx& c, bool reorder_all)
 
 void launch_node_moments(Ctx& c)
 {
-    const int grid = c.num_sms * 4;
-    if (c.dim == 1) {
-        moments_kernel<1><<<grid, 256, 0, c.stream>>>(c.st, c.node_total, c.R, c.nd_begin, c.nd_count, c.nd_first, c.nd_nchild, c.nd_parent, c.nd_arrive, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
-        com_finalize_kernel<1><<<grid, 256, 0, c.stream>>>(c.node_total, c.R, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
-    } else if (c.dim == 2) {
-        moments_kernel<2><<<grid, 256, 0, c.stream>>>(c.st, c.node_total, c.R, c.nd_begin, c.nd_count, c.nd_first, c.nd_nchild, c.nd_parent, c.nd_arrive, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
-        com_finalize_kernel<2><<<grid, 256, 0, c.stream>>>(c.node_total, c.R, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
-    } else {
-        moments_kernel<3><<<grid, 256, 0, c.stream>>>(c.st, c.node_total, c.R, c.nd_begin, c.nd_count, c.nd_first, c.nd_nchild, c.nd_parent, c.nd_arrive, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
-        com_finalize_kernel<3><<<grid, 256, 0, c.stream>>>(c.node_total, c.R, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
+    const int grid = c.num_sms * 8;
+    for (int l = c.key_levels + 1; l >= 2; --l) {
+        if (c.dim == 1)
+            moments_level_kernel<1><<<grid, 256, 0, c.stream>>>(c.st, c.lvl_start, l, c.R, c.nd_begin, c.nd_count, c.nd_first, c.nd_nchild, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
+        else if (c.dim == 2)
+            moments_level_kernel<2><<<grid, 256, 0, c.stream>>>(c.st, c.lvl_start, l, c.R, c.nd_begin, c.nd_count, c.nd_first, c.nd_nchild, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
+        else
+            moments_level_kernel<3><<<grid, 256, 0, c.stream>>>(c.st, c.lvl_start, l, c.R, c.nd_begin, c.nd_count, c.nd_first, c.nd_nchild, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
     }
+    if (c.dim == 1) com_finalize_kernel<1><<<grid, 256, 0, c.stream>>>(c.node_total, c.R, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
+    else if (c.dim == 2) com_finalize_kernel<2><<<grid, 256, 0, c.stream>>>(c.node_total, c.R, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
+    else com_finalize_kernel<3><<<grid, 256, 0, c.stream>>>(c.node_total, c.R, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
 }
 
 void launch_set_kernel_size(Ctx& c)
 {
-    // counters reset: the moments pass left arrive[p] = nchild[p]
-    cudaMemsetAsync(c.nd_arrive, 0, sizeof(int) * c.node_cap, c.stream);
-    ksize_kernel<<<c.num_sms * 4, 256, 0, c.stream>>>(c.st.f[F_SML], c.node_total, c.nd_begin,
-                                                      c.nd_count, c.nd_first, c.nd_nchild,
-                                                      c.nd_parent, c.nd_arrive, c.nd_ksize);
+    for (int l = c.key_levels + 1; l >= 1; --l)
+        ksize_level_kernel<<<c.num_sms * 8, 256, 0, c.stream>>>(c.st.f[F_SML], c.lvl_start, l, c.nd_begin,
+                                                               c.nd_count, c.nd_first, c.nd_nchild,
+                                                               c.nd_ksize);
     if (c.precision == SPHGPU_FP32_PAIR)
         kernel_size_mirror_kernel<float><<<c.num_sms * 8, 256, 0, c.stream>>>(c.node_total, c.nd_ksize, c.nd_kf, c.st.f[F_SML], c.n, (float*)c.mir[7]);
     else
