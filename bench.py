@@ -54,6 +54,9 @@ def workload(name):
     elif name == "evrard":
         p, f = ics.evrard()
         desc = "evrard_3d_disph_wendland_balsara_tdav_gravity"
+    elif name == "evrard_small":   # 2^18 particles, for profiling captures
+        p, f = ics.evrard(1 << 18)
+        desc = "evrard_3d_disph_wendland_balsara_tdav_gravity_262144"
     elif name == "gresho":
         p, f = ics.gresho(256)
         desc = "gresho_chan_2d_ssph_cubic"
@@ -219,6 +222,7 @@ def main():
     ap.add_argument("--group-warps", type=int, default=0,
                     help="target-group size in warps (0 = the library's default)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--tile-pre", type=int, default=0)
     ap.add_argument("--tile-fluid", type=int, default=0)
     ap.add_argument("--profile-run", action="store_true",
@@ -235,6 +239,8 @@ def main():
         p, f, desc, runs = workload(args.workload)
         with sphgpu.GpuSimulation(p, f, precision=args.precision, runs=runs) as sim:
             sim.set_tuning("graph", 0)
+            if args.no_autotune:
+                sim.set_tuning("autotune", 0)
             sim.initialize()
             sim.step(args.steps)
             print(json.dumps({"profile_run": desc, "n": sim.n, "steps": args.steps,

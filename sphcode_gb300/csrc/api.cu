@@ -370,7 +370,8 @@ int create_impl(const sphgpu_params* params, int dim, int n_runs, const int* run
         A((void**)&c.d_err, sizeof(unsigned));
         A((void**)&c.d_newton_fail, sizeof(int));
         A((void**)&c.d_work, sizeof(int) * 32);
-        c.ovf_cap = 2 * c.max_groups + 64;
+        // halving can leave every target as a range of its own: n entries at most
+        c.ovf_cap = std::max(c.n, 2 * c.max_groups) + 64;
         A((void**)&c.d_ovf_list, sizeof(int2) * c.ovf_cap);
         A((void**)&c.d_ovf_list2, sizeof(int2) * c.ovf_cap);
         c.stage_bytes = sizeof(double) * n * (size_t)std::max(9, dim * dim);

@@ -76,6 +76,13 @@ struct TreeView {
     const float* cf[3];
     const float* ef;
     const float* kf;
+    // FP32 copies for the Barnes-Hut walk: centre of mass and geometric centre as two-float
+    // pairs (hi = nearest float, lo = nearest float of the remainder), edge^2 and mass
+    const float* comf[3];
+    const float* comlo[3];
+    const float* clo[3];
+    const float* l2f;
+    const float* massf;
 };
 
 struct Periodic {

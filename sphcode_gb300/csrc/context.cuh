@@ -44,6 +44,9 @@ struct Ctx {
     double *nd_center[3] = {nullptr, nullptr, nullptr}, *nd_edge = nullptr, *nd_mass = nullptr;
     double *nd_com[3] = {nullptr, nullptr, nullptr}, *nd_ksize = nullptr;
     float *nd_cf[3] = {nullptr, nullptr, nullptr}, *nd_ef = nullptr, *nd_kf = nullptr;
+    float *nd_comf[3] = {nullptr, nullptr, nullptr}, *nd_l2f = nullptr;
+    float *nd_comlo[3] = {nullptr, nullptr, nullptr}, *nd_clo[3] = {nullptr, nullptr, nullptr};
+    float* nd_massf = nullptr;
     int* lvl_start = nullptr;       // device, MAX_LEVELS + 2 entries
     int* lvl_tmp = nullptr;         // per-node child counts of the frontier
     int* chunk_sum = nullptr;       // per-1024-node chunk sums
@@ -155,12 +158,13 @@ void reset_work_counters(Ctx& c);
 void set_global_error(const std::string& text);   // text of sphgpu_last_error(NULL)
 
 // Passes of a CTA-per-group pair kernel.  Pass 1 runs every group with the tuned capacities at
-// full occupancy and lists the target ranges that do not fit; pass 2 runs that list with 4x the
-// tile and larger walk capacities, still at full occupancy; pass 3 runs what is left with the
-// largest tile the shared memory holds, one CTA per SM; passes 4 to 8 run what is still left
-// with the largest tile, each on the two halves of every range the previous pass could not fit
-// (a range of 32 targets is down to single targets after five halvings).  A range that fits
-// nowhere sets the capacity error bit.  Args must carry `L` (SmemLayout) and `work` (GroupWork).
+// full occupancy and lists the target ranges that do not fit; pass 2 runs them with 4x the tile
+// and larger walk capacities (occupancy as the shared memory allows) and passes a range that
+// still does not fit on as its two halves; passes 3 to 6 run those halves with the same
+// capacities, halving again on failure; passes 7 and 8 run what is left (single targets with
+// very large neighbourhoods) with the largest tile the shared memory holds, one CTA per SM.
+// A range that fits nowhere sets the capacity error bit.  Args must carry `L` (SmemLayout) and
+// `work` (GroupWork).
 constexpr int PAIR_PASSES = 8;
 template <class Args>
 void launch_pair_passes(Ctx& c, const void* kern, Args& a, int tcap, int elt4, int eltT,
@@ -188,17 +192,18 @@ void launch_pair_passes(Ctx& c, const void* kern, Args& a, int tcap, int elt4, i
     int2* lists[2] = {c.d_ovf_list, c.d_ovf_list2};
     for (int pass = 0; pass < PAIR_PASSES; ++pass) {
         int cap, stack_cap, leaf_cap, grid;
+        const bool last_tier = pass >= PAIR_PASSES - 2;
         if (pass == 0) { cap = std::min(tcap, big); stack_cap = 128; leaf_cap = 96; }
-        else if (pass == 1) { cap = std::min(4 * tcap, big); stack_cap = 512; leaf_cap = 512; }
+        else if (!last_tier) { cap = std::min(4 * tcap, big); stack_cap = 512; leaf_cap = 512; }
         else { cap = big; stack_cap = 1024; leaf_cap = 1024; }
         a.L = make_layout(gt, cap, elt4, eltT, stack_cap, leaf_cap);
-        grid = pass < 2 ? std::max(1, kernel_occupancy(kern, gt, a.L.total)) * c.num_sms : c.num_sms;
+        grid = last_tier ? c.num_sms : std::max(1, kernel_occupancy(kern, gt, a.L.total)) * c.num_sms;
         // work counter 2 pass, produced-range count 2 pass + 1 (zeroed with the others)
         a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 2 * pass,
                            pass == 0 ? nullptr : lists[(pass - 1) & 1],
                            pass == 0 ? nullptr : c.d_work + 2 * pass - 1,
                            pass + 1 < PAIR_PASSES ? lists[pass & 1] : nullptr,
-                           c.d_work + 2 * pass + 1, c.ovf_cap, pass >= 2 ? 1 : 0, c.d_err};
+                           c.d_work + 2 * pass + 1, c.ovf_cap, (pass >= 1 && pass != PAIR_PASSES - 3) ? 1 : 0, c.d_err};
         launch(kern, grid, gt, a.L.total, c.stream, a);
     }
 }

@@ -95,6 +95,20 @@ __global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
         for (int k = 0; k < D; ++k) xi[k] = st.f[F_POS + k][i];
         const double hi = st.f[F_SML][i];
         const T hiT = (T)hi;
+        // FP32 opening test (FP32 pair form): x_i and the centres of mass in FP32 differ from the
+        // exact values by at most u (|x| + |com| + |d|) per component; xmag bounds |x| (plus a
+        // periodic length), which the test's margin scales with.
+        // x_i as a two-float pair: for nearby points hi_i - hi_c is exact in FP32 (Sterbenz), so
+        // (hi_i - hi_c) + (lo_i - lo_c) reproduces x_i - c to FP32 rounding of the difference.
+        float xf[D], xlo[D];
+        float xmag = 0.f;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            xf[k] = (float)xi[k];
+            xlo[k] = (float)(xi[k] - (double)xf[k]);
+            xmag = fmaxf(xmag, fabsf(xf[k]) + (a.pb.on ? a.pb.lenf[k] : 0.f));
+        }
+        const float theta2f = (float)a.theta2;
         Sum<T> phi, acc[D];
         phi.zero();
 #pragma unroll
@@ -114,22 +128,46 @@ __global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
             const bool in = (m >> lane) & 1u;
             bool open = false;
             if (in) {
-                double d[D];
+                T dT[D];
+                bool decided = false;
+                if (!exact_pairs) {
+                    // edge^2 > theta^2 |d|^2 in FP32, certain outside the margin
+                    float df[D], d2f = 0.f;
 #pragma unroll
-                for (int k = 0; k < D; ++k) d[k] = ref_axis(xi[k], tv.com[k][node], a.pb, k);
-                double d2 = __dmul_rn(d[0], d[0]);
+                    for (int k = 0; k < D; ++k) {
+                        df[k] = min_image_f((xf[k] - tv.comf[k][node]) + (xlo[k] - tv.comlo[k][node]), a.pb, k);
+                        d2f = fmaf(df[k], df[k], d2f);
+                    }
+                    const float l2 = tv.l2f[node];
+                    const float dabs = sqrtf(d2f);
+                    const float u = 5.9604645e-08f;
+                    const float margin = theta2f * (8.f * u * dabs * (xmag + dabs) + 8.f * u * d2f) + 8.f * u * l2;
+                    const float t2d2 = theta2f * d2f;
+                    if (l2 > t2d2 + margin) { open = true; decided = true; }
+                    else if (l2 < t2d2 - margin) { open = false; decided = true; }
 #pragma unroll
-                for (int k = 1; k < D; ++k) d2 = __dadd_rn(d2, __dmul_rn(d[k], d[k]));
-                const double edge = tv.edge[node];
-                open = __dmul_rn(edge, edge) > __dmul_rn(a.theta2, d2);
+                    for (int k = 0; k < D; ++k) dT[k] = (T)df[k];
+                }
+                if (!decided) {
+                    // the reference's FP64 test (src/bhtree.cpp:304-308)
+                    double d[D];
+#pragma unroll
+                    for (int k = 0; k < D; ++k) d[k] = ref_axis(xi[k], tv.com[k][node], a.pb, k);
+                    double d2 = __dmul_rn(d[0], d[0]);
+#pragma unroll
+                    for (int k = 1; k < D; ++k) d2 = __dadd_rn(d2, __dmul_rn(d[k], d[k]));
+                    const double edge = tv.edge[node];
+                    open = __dmul_rn(edge, edge) > __dmul_rn(a.theta2, d2);
+#pragma unroll
+                    for (int k = 0; k < D; ++k) dT[k] = (T)d[k];
+                }
                 if (!open) {
-                    const double M = tv.mass[node];
-                    if (M != 0.0) {
+                    const T M = exact_pairs ? (T)tv.mass[node] : (T)tv.massf[node];
+                    if (M != T(0)) {
                         // monopole: phi -= G M / r, acc -= d G M / r^3 (src/bhtree.cpp:327-329)
-                        T dT[D];
                         T r2 = T(0);
 #pragma unroll
-                        for (int k = 0; k < D; ++k) { dT[k] = (T)d[k]; r2 += dT[k] * dT[k]; }
+                        for (int k = 0; k < D; ++k) r2 += dT[k] * dT[k];
                         const T r_inv = T(1) / sqrt(r2);
                         const T gmr = G * (T)M * r_inv;
                         phi.add(-gmr);
@@ -148,7 +186,8 @@ __global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
                     T base[D];
                     if (!exact_pairs) {
 #pragma unroll
-                        for (int k = 0; k < D; ++k) base[k] = (T)min_image(xi[k] - tv.center[k][node], a.pb, k);
+                        for (int k = 0; k < D; ++k)
+                            base[k] = (T)min_image_f((xf[k] - tv.cf[k][node]) + (xlo[k] - tv.clo[k][node]), a.pb, k);
                     }
                     for (int j = b; j < b + cnt; ++j) {
                         T rv[D], mj, hj;
@@ -168,10 +207,22 @@ __global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
                         T r2 = rv[0] * rv[0];
 #pragma unroll
                         for (int k = 1; k < D; ++k) r2 += rv[k] * rv[k];
-                        const T r = sqrt(r2);
+                        T fsum, gsum;
+                        const T hmax = hiT > hj ? hiT : hj;
+                        if (r2 >= hmax * hmax && r2 > T(0)) {
+                            // beyond both softening lengths (u = 2 r / h >= 2 for h_i and h_j):
+                            // f = 1/r and g = 1/r^3 for both (src/bhtree.cpp:282-283,296-297)
+                            const T rinv = T(1) / sqrt(r2);
+                            fsum = T(2) * rinv;
+                            gsum = fsum * rinv * rinv;
+                        } else {
+                            const T r = sqrt(r2);
+                            fsum = hk_f(r, hiT) + hk_f(r, hj);
+                            gsum = hk_g(r, hiT) + hk_g(r, hj);
+                        }
                         const T gm = G * mj * T(0.5);
-                        phi.add(-gm * (hk_f(r, hiT) + hk_f(r, hj)));
-                        const T c = gm * (hk_g(r, hiT) + hk_g(r, hj));
+                        phi.add(-gm * fsum);
+                        const T c = gm * gsum;
 #pragma unroll
                         for (int k = 0; k < D; ++k) acc[k].add(-rv[k] * c);
                     }
