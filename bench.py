@@ -223,6 +223,7 @@ def main():
                     help="target-group size in warps (0 = the library's default)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--pass2-scale", type=int, default=0)
     ap.add_argument("--tile-pre", type=int, default=0)
     ap.add_argument("--tile-fluid", type=int, default=0)
     ap.add_argument("--profile-run", action="store_true",
@@ -291,6 +292,8 @@ def main():
             s_.set_tuning("tile_cap_pre", args.tile_pre)
         if args.tile_fluid:
             s_.set_tuning("tile_cap", args.tile_fluid)
+        if args.pass2_scale:
+            s_.set_tuning("pass2_scale", args.pass2_scale)
         return s_
 
     sim = make("fp32")

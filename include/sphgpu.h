@@ -199,7 +199,9 @@ const char* sphgpu_last_error(const sphgpu_ctx* ctx);
  * in one captured step; 8, 9 (read only) target groups that overflowed into the large-capacity
  * pass in the last timed PreInteraction / FluidForce; 10 PreInteraction source-tile capacity
  * (0 = automatic; 3 then applies to FluidForce); 11 (read only) status bits raised by tuning
- * candidates that the tuner rejected. */
+ * candidates that the tuner rejected; 12 tile of the second pair-kernel pass in multiples of the
+ * first (1..8, default 2); 13..17 (read only) the last target range no pair-kernel pass could
+ * fit: {first particle (key order), count, search radius x 1e9, leaves, overflow code}. */
 int sphgpu_set_tuning(sphgpu_ctx* ctx, int which, int value);
 int sphgpu_get_tuning(sphgpu_ctx* ctx, int which, int* value);
 

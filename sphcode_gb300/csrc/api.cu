@@ -369,7 +369,7 @@ int create_impl(const sphgpu_params* params, int dim, int n_runs, const int* run
         A((void**)&c.d_sums, sizeof(double) * (R * maxc * 7 + R * 7));
         A((void**)&c.d_err, sizeof(unsigned));
         A((void**)&c.d_newton_fail, sizeof(int));
-        A((void**)&c.d_work, sizeof(int) * 32);
+        A((void**)&c.d_work, sizeof(int) * 64);
         // halving can leave every target as a range of its own: n entries at most
         c.ovf_cap = std::max(c.n, 2 * c.max_groups) + 64;
         A((void**)&c.d_ovf_list, sizeof(int2) * c.ovf_cap);
@@ -395,7 +395,7 @@ int create_impl(const sphgpu_params* params, int dim, int n_runs, const int* run
         cudaMemset(c.d_dt, 0, sizeof(double) * c.R);
         cudaMemset(c.d_err, 0, sizeof(unsigned));
         cudaMemset(c.d_newton_fail, 0, sizeof(int));
-        cudaMemset(c.d_work, 0, sizeof(int) * 32);
+        cudaMemset(c.d_work, 0, sizeof(int) * 64);
         fill_ord_kernel<<<ceil_div(c.R, 128), 128>>>(c.d_hvs, c.R, 1.7976931348623157e308);
         fill_ord_kernel<<<ceil_div(c.R, 128), 128>>>(c.d_dtmin, c.R, 1.7976931348623157e308);
         init_ids_kernel<<<ceil_div(c.n, THREADS), THREADS>>>(c.st.id, c.st.run, c.d_run_begin, c.R, c.n);
@@ -591,7 +591,7 @@ int kernel_occupancy(const void* kern, int threads, size_t smem)
     return nb;
 }
 
-void reset_work_counters(Ctx& c) { cudaMemsetAsync(c.d_work, 0, sizeof(int) * 32, c.stream); }
+void reset_work_counters(Ctx& c) { cudaMemsetAsync(c.d_work, 0, sizeof(int) * 48, c.stream); }
 
 void set_global_error(const std::string& text)
 {
@@ -1044,6 +1044,10 @@ int sphgpu_set_tuning(sphgpu_ctx* h, int which, int value)
         c.tile_cap_pre = value;
         c.autotune = 0;
         break;
+    case 12:
+        if (value < 1 || value > 8) return SPHGPU_ERR_ARG;
+        c.pass2_scale = value;
+        break;
     case 4: c.autotune = value != 0; break;
     case 5: c.timing = value != 0; break;
     case 6: c.use_graph = value != 0; break;
@@ -1071,6 +1075,12 @@ int sphgpu_get_tuning(sphgpu_ctx* h, int which, int* value)
     case 9: *value = c.stage_ovf[1]; break;
     case 10: *value = c.tile_cap_pre; break;
     case 11: *value = (int)c.tune_rejects; break;
+    case 12: *value = c.pass2_scale; break;
+    case 13: case 14: case 15: case 16: case 17: {
+        cudaStreamSynchronize(c.stream);
+        cudaMemcpy(value, c.d_work + sphgpu::FAIL_INFO_SLOT + (which - 13), sizeof(int), cudaMemcpyDeviceToHost);
+        break;
+    }
     default: return SPHGPU_ERR_ARG;
     }
     return SPHGPU_OK;

@@ -79,7 +79,8 @@ struct Ctx {
     // 6 {x - leaf centre, m} (tree build), 7 h (end of PreInteraction)
     void* mir[16] = {nullptr};
     // persistent-kernel work counters and the overflow group list
-    int* d_work = nullptr;          // 32 counters (pair-kernel pass p: [2p] work, [2p+1] ranges left)
+    int* d_work = nullptr;          // 64 ints: pair-kernel pass p uses [2p] work, [2p+1] ranges left;
+                                    // [48..52] the last range no pass could fit
     int2* d_ovf_list = nullptr;     // target ranges left by a pass (two lists, used alternately)
     int2* d_ovf_list2 = nullptr;
     int ovf_cap = 0;                // capacity of each list
@@ -117,6 +118,7 @@ struct Ctx {
     double stage_ms[5] = {0, 0, 0, 0, 0};
     int stage_ovf[2] = {0, 0};      // groups sent to the overflow pass by Pre / Fluid (timing mode)
     int tile_cap_pre = 0;           // per-stage source tile capacities (0 = automatic)
+    int pass2_scale = 2;            // tile of the second pair pass, in multiples of the first
 
     std::string last_error;
 };
@@ -158,14 +160,15 @@ void reset_work_counters(Ctx& c);
 void set_global_error(const std::string& text);   // text of sphgpu_last_error(NULL)
 
 // Passes of a CTA-per-group pair kernel.  Pass 1 runs every group with the tuned capacities at
-// full occupancy and lists the target ranges that do not fit; pass 2 runs them with 4x the tile
-// and larger walk capacities (occupancy as the shared memory allows) and passes a range that
-// still does not fit on as its two halves; passes 3 to 6 run those halves with the same
-// capacities, halving again on failure; passes 7 and 8 run what is left (single targets with
-// very large neighbourhoods) with the largest tile the shared memory holds, one CTA per SM.
-// A range that fits nowhere sets the capacity error bit.  Args must carry `L` (SmemLayout) and
-// `work` (GroupWork).
-constexpr int PAIR_PASSES = 8;
+// full occupancy and lists the target ranges that do not fit.  The next log2(G) + 1 passes run
+// them with a larger tile (pass2_scale times the first) and larger walk capacities, passing a
+// range that still does not fit on as its two halves, so that ranges come down to single targets
+// (whose search box is just their own search sphere).  The last two passes run what is left with
+// the largest tile the shared memory holds, one CTA per SM.  A range that fits nowhere sets the
+// capacity error bit and records itself in the work counters' diagnostic slots.  Args must carry
+// `L` (SmemLayout) and `work` (GroupWork).
+constexpr int MAX_PAIR_PASSES = 14;
+constexpr int FAIL_INFO_SLOT = 48;   // d_work[48..52]: the last failing range
 template <class Args>
 void launch_pair_passes(Ctx& c, const void* kern, Args& a, int tcap, int elt4, int eltT,
                         void (*launch)(const void*, int, int, size_t, cudaStream_t, Args&));
@@ -190,20 +193,24 @@ void launch_pair_passes(Ctx& c, const void* kern, Args& a, int tcap, int elt4, i
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, max_optin_smem(c));
     const int big = big_tile_cap(c, gt, elt4, eltT, 1024, 1024);
     int2* lists[2] = {c.d_ovf_list, c.d_ovf_list2};
-    for (int pass = 0; pass < PAIR_PASSES; ++pass) {
+    int halvings = 0;
+    while ((1 << halvings) < gt) ++halvings;
+    const int passes = std::min(MAX_PAIR_PASSES, 1 + (halvings + 1) + 2);
+    for (int pass = 0; pass < passes; ++pass) {
         int cap, stack_cap, leaf_cap, grid;
-        const bool last_tier = pass >= PAIR_PASSES - 2;
+        const bool last_tier = pass >= passes - 2;
         if (pass == 0) { cap = std::min(tcap, big); stack_cap = 128; leaf_cap = 96; }
-        else if (!last_tier) { cap = std::min(4 * tcap, big); stack_cap = 512; leaf_cap = 512; }
+        else if (!last_tier) { cap = std::min(c.pass2_scale * tcap, big); stack_cap = 512; leaf_cap = 512; }
         else { cap = big; stack_cap = 1024; leaf_cap = 1024; }
         a.L = make_layout(gt, cap, elt4, eltT, stack_cap, leaf_cap);
         grid = last_tier ? c.num_sms : std::max(1, kernel_occupancy(kern, gt, a.L.total)) * c.num_sms;
         // work counter 2 pass, produced-range count 2 pass + 1 (zeroed with the others)
         a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 2 * pass,
                            pass == 0 ? nullptr : lists[(pass - 1) & 1],
-                           pass == 0 ? nullptr : c.d_work + 2 * pass - 1,
-                           pass + 1 < PAIR_PASSES ? lists[pass & 1] : nullptr,
-                           c.d_work + 2 * pass + 1, c.ovf_cap, (pass >= 1 && pass != PAIR_PASSES - 3) ? 1 : 0, c.d_err};
+                           pass == 0 ? nullptr : c.d_work + 2 * pass - 1, c.ovf_cap,
+                           pass + 1 < passes ? lists[pass & 1] : nullptr,
+                           c.d_work + 2 * pass + 1, c.ovf_cap, pass >= 1 ? 1 : 0, c.d_err,
+                           c.d_work + FAIL_INFO_SLOT};
         launch(kern, grid, gt, a.L.total, c.stream, a);
     }
 }

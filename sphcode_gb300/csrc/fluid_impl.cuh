@@ -91,25 +91,18 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
         const double hi = st.f[F_SML][i];
         group_box<D>(gm, xi, active, hi, a.pb);
         const int run = st.run[gb];
-        if (!group_walk<D, T>(smem, L, gm, a.tv, run, true, a.pb)) { report_overflow(a.work, gb, gn); continue; }
+        if (!group_walk<D, T>(smem, L, gm, a.tv, run, true, a.pb)) { report_overflow(a.work, gb, gn, gm); continue; }
         {
-            // keep sources within max(R, h_j) of the group box per axis
-            const double u = Unit<T>::u;
+            // keep sources within max(R, h_j) of the group box
+            BoxAccept<D, T> box;
+            box.init(gm);
             const T Rt = to_T_up<T>(gm->R);
-            const T rel = (T)(1.0 + 8.0 * u), slack = to_T_up<T>(4.0 * u * gm->bmax + 1e-300);
-            T he[D];
-#pragma unroll
-            for (int k = 0; k < D; ++k) he[k] = to_T_up<T>(gm->he[k]);
             const T* hmir = a.hmir;
             const int ntile = stage_sources<D, T>(smem, L, gm, a.xrel, tile, [&](int j, const T* off) {
                 const T hj = hmir[j];
-                const T r = Rt > hj ? Rt : hj;
-#pragma unroll
-                for (int k = 0; k < D; ++k)
-                    if (fabs(off[k]) > (he[k] + r) * rel + slack) return false;
-                return true;
+                return box(off, Rt > hj ? Rt : hj);
             }, [&](int j) { return a.rec0[j].w; });
-            if (ntile < 0) { report_overflow(a.work, gb, gn); continue; }
+            if (ntile < 0) { report_overflow(a.work, gb, gn, gm); continue; }
             gm->ntile = ntile;
         }
         const int ntile = gm->ntile;

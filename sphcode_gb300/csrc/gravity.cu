@@ -265,8 +265,8 @@ void run_gravity(Ctx& c)
     a.G = c.p.g_constant;
     a.theta2 = c.p.theta * c.p.theta;
     a.stack_cap = 1024;
-    a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 0, nullptr, nullptr, nullptr,
-                       nullptr, 0, 0, c.d_err};
+    a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 0, nullptr, nullptr, 0, nullptr,
+                       nullptr, 0, 0, c.d_err, nullptr};
     const int gt = c.group_threads;
     const size_t smem = sizeof(int2) * (size_t)a.stack_cap * (gt / 32);
     auto kern = gravity_kernel<D, T>;

@@ -158,11 +158,13 @@ struct GroupWork {
     int* counter;             // work counter (device, zeroed before the launch)
     const int2* list;         // ranges left by the previous pass (nullptr in the first pass)
     const int* list_count;
+    int list_cap;             // capacity of both range lists
     int2* ovf_list;           // ranges this pass cannot fit (nullptr in the last pass)
     int* ovf_count;
     int ovf_cap;
     int halve;                // pass a failing range on as its two halves
     unsigned* err;
+    int* fail_info;           // last pass: {begin, count, R in units of 1e-9, leaves, sources}
 };
 
 // Next work item for this CTA (block-uniform); false when done.
@@ -173,7 +175,7 @@ __device__ __forceinline__ bool next_group(GroupMisc* gm, const GroupWork& w, in
         const int k = atomicAdd(w.counter, 1);
         int b = -1, n = 0;
         if (w.list) {
-            if (k < *w.list_count) { const int2 r = w.list[k]; b = r.x; n = r.y; }
+            if (k < min(*w.list_count, w.list_cap)) { const int2 r = w.list[k]; b = r.x; n = r.y; }
         } else if (k < *w.n_groups) {
             b = w.g_begin[k];
             n = w.g_count[k];
@@ -194,11 +196,18 @@ __device__ __forceinline__ void push_range(const GroupWork& w, int b, int n)
     else atomicOr(w.err, (unsigned)ERR_TILE);
 }
 
-__device__ __forceinline__ void report_overflow(const GroupWork& w, int gb, int gn)
+__device__ __forceinline__ void report_overflow(const GroupWork& w, int gb, int gn, const GroupMisc* gm = nullptr)
 {
     if (threadIdx.x == 0) {
         if (!w.ovf_list) {
             atomicOr(w.err, (unsigned)ERR_TILE);
+            if (w.fail_info && gm) {
+                w.fail_info[0] = gb;
+                w.fail_info[1] = gn;
+                w.fail_info[2] = (int)fmin(gm->R * 1e9, 2e9);
+                w.fail_info[3] = gm->nleaves;
+                w.fail_info[4] = gm->overflow;
+            }
         } else if (w.halve && gn > 1) {
             push_range(w, gb, gn / 2);
             push_range(w, gb + gn / 2, gn - gn / 2);
@@ -373,6 +382,36 @@ __device__ __forceinline__ T accept_limit(double ext, const GroupMisc* gm)
     return to_T_up<T>(ext * (1.0 + 8.0 * u) + 4.0 * u * gm->bmax + 1e-300);
 }
 
+// Rounded-box acceptance for staging: keep a source whose distance from the group's bounding
+// box (gc +/- he) is at most r.  Every target lies in the box, so this keeps every source within
+// r of some target.  The T offsets differ from the exact ones by at most u (2 |off| + 2 bmax) per
+// component; the test shrinks the computed per-axis distances by that bound and widens r, so it
+// never drops a source the exact test keeps.
+template <int D, typename T>
+struct BoxAccept {
+    T he[D];
+    T slack;
+    __device__ __forceinline__ void init(const GroupMisc* gm)
+    {
+        const double u = Unit<T>::u;
+#pragma unroll
+        for (int k = 0; k < D; ++k) he[k] = to_T_up<T>(gm->he[k] * (1.0 + 8.0 * u));
+        slack = to_T_up<T>(3.0 * u * gm->bmax + 1e-300);
+    }
+    __device__ __forceinline__ bool operator()(const T* off, T r) const
+    {
+        const T shrink = T(1) - T(4.0 * Unit<T>::u);
+        T d2 = T(0);
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            const T dk = fabs(off[k]) * shrink - he[k] - slack;
+            if (dk > T(0)) d2 += dk * dk;
+        }
+        const T rr = r * T(1.0 + 8.0 * Unit<T>::u);
+        return d2 <= rr * rr;
+    }
+};
+
 // ---- 3. staging -------------------------------------------------------------------------------
 // Flattens the leaf ranges and calls, for each particle j (key slot) in deterministic order,
 // accept(j, off) with off[k] = (leaf centre - gc) + (x_j - leaf centre) in T; accepted sources
@@ -455,6 +494,7 @@ __device__ int stage_sources(unsigned char* smem, const SmemLayout& L, GroupMisc
         base += tot;
     }
     __syncthreads();
+    if (base > L.tcap && threadIdx.x == 0) gm->overflow = 1000000 + base;   // diagnostic: sources needed
     return base > L.tcap ? -1 : base;
 }
 

@@ -44,25 +44,19 @@ __global__ void __launch_bounds__(256) neighbors_kernel(NbArgs<T> a)
         const double hi = st.f[F_SML][i];
         group_box<D>(gm, xi, active, hi, a.pb);
         const int run = st.run[gb];
-        if (!group_walk<D, T>(smem, L, gm, a.tv, run, a.is_ij != 0, a.pb)) { report_overflow(a.work, gb, gn); continue; }
+        if (!group_walk<D, T>(smem, L, gm, a.tv, run, a.is_ij != 0, a.pb)) { report_overflow(a.work, gb, gn, gm); continue; }
         {
-            const double u = Unit<T>::u;
+            BoxAccept<D, T> box;
+            box.init(gm);
             const T Rt = to_T_up<T>(gm->R);
-            const T rel = (T)(1.0 + 8.0 * u), slack = to_T_up<T>(4.0 * u * gm->bmax + 1e-300);
             const int is_ij = a.is_ij;
             const T* hmir = a.hmir;
-            T he[D];
-#pragma unroll
-            for (int k = 0; k < D; ++k) he[k] = to_T_up<T>(gm->he[k]);
             const int ntile = stage_sources<D, T>(smem, L, gm, a.xrel, tile, [&](int j, const T* off) {
                 T r = Rt;
                 if (is_ij) { const T hj = hmir[j]; r = r > hj ? r : hj; }
-#pragma unroll
-                for (int k = 0; k < D; ++k)
-                    if (fabs(off[k]) > (he[k] + r) * rel + slack) return false;
-                return true;
+                return box(off, r);
             }, [&](int) { return T(0); });
-            if (ntile < 0) { report_overflow(a.work, gb, gn); continue; }
+            if (ntile < 0) { report_overflow(a.work, gb, gn, gm); continue; }
             gm->ntile = ntile;
         }
         const int ntile = gm->ntile;

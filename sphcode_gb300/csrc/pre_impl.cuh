@@ -79,19 +79,16 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
         const double hs = a.initial ? hg : hg * a.ratio;
         group_box<D>(gm, xi, active, hs, a.pb);
         const int run = st.run[gb];
-        if (!group_walk<D, T>(smem, L, gm, a.tv, run, false, a.pb)) { report_overflow(a.work, gb, gn); continue; }
+        if (!group_walk<D, T>(smem, L, gm, a.tv, run, false, a.pb)) { report_overflow(a.work, gb, gn, gm); continue; }
         {
-            T lim[D];
-#pragma unroll
-            for (int k = 0; k < D; ++k) lim[k] = accept_limit<T>(gm->he[k] + gm->R, gm);
+            BoxAccept<D, T> box;
+            box.init(gm);
+            const T Rt = to_T_up<T>(gm->R);
             const T* mu = a.mu;
             const int ntile = stage_sources<D, T>(smem, L, gm, a.xrel, tile, [&](int, const T* off) {
-#pragma unroll
-                for (int k = 0; k < D; ++k)
-                    if (fabs(off[k]) > lim[k]) return false;
-                return true;
+                return box(off, Rt);
             }, [&](int j) { return mu[j]; });
-            if (ntile < 0) { report_overflow(a.work, gb, gn); continue; }
+            if (ntile < 0) { report_overflow(a.work, gb, gn, gm); continue; }
             gm->ntile = ntile;   // every thread writes the same value
         }
         const int ntile = gm->ntile;
@@ -421,8 +418,8 @@ void run_pre(Ctx& c, bool initial)
     cudaStream_t s = c.stream;
     pre_mirror_kernel<D, T><<<ceil_div(c.n, 256), 256, 0, s>>>(c.st, c.n, (V4*)c.mir[0], (T*)c.mir[1]);
     // counters: [0] main work, [1] overflow count, [2] overflow work; plus h/v_sig and Newton
-    if (!initial) pre_reset_kernel<<<ceil_div(std::max(c.R, 32), 128), 128, 0, s>>>(c.R, c.d_hvs, c.d_work, 32);
-    else pre_reset_kernel<<<1, 32, 0, s>>>(0, c.d_hvs, c.d_work, 32);
+    if (!initial) pre_reset_kernel<<<ceil_div(std::max(c.R, 48), 128), 128, 0, s>>>(c.R, c.d_hvs, c.d_work, 48);
+    else pre_reset_kernel<<<1, 64, 0, s>>>(0, c.d_hvs, c.d_work, 48);
     cudaMemsetAsync(c.d_newton_fail, 0, sizeof(int), s);
     PreArgs<T> a{};
     a.st = c.st;
