@@ -42,6 +42,20 @@ def fluid_bytes_per_particle(D):
     return 8 * (2 * D + 9) + 48 * 2 + 8 * (D + 1)
 
 
+def aggregate(ms_local, n_local, steps, dist=None, device="cpu"):
+    """Whole-job throughput of independent replicas: the slowest rank's time (max over ranks)
+    and the particles of all ranks.  Returns (ms_max, particle-steps/s)."""
+    if dist is None:
+        return ms_local, n_local * steps / (ms_local * 1e-3)
+    import torch
+    t = torch.tensor([ms_local, float(n_local)], dtype=torch.float64, device=device)
+    mx = t.clone()
+    dist.all_reduce(mx[:1], op=dist.ReduceOp.MAX)
+    dist.all_reduce(t[1:], op=dist.ReduceOp.SUM)
+    ms = float(mx[0].item())
+    return ms, float(t[1].item()) * steps / (ms * 1e-3)
+
+
 def workload(name):
     """(params, fields, description, run sizes or None)."""
     from sphcode_gb300 import ics
@@ -306,8 +320,7 @@ def main():
     ms = sim.bench_steps(args.steps, flush_l2=True)
     barrier()
     clk = clocks.stop()
-    ms = max_over_ranks(ms)
-    value = world * n * args.steps / (ms * 1e-3)
+    ms, value = aggregate(ms, n, args.steps, dist, "cuda")
 
     # per-stage device times (eager launches, CUDA events between stages)
     sim.set_tuning("timing", 1)
