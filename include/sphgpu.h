@@ -201,7 +201,9 @@ const char* sphgpu_last_error(const sphgpu_ctx* ctx);
  * (0 = automatic; 3 then applies to FluidForce); 11 (read only) status bits raised by tuning
  * candidates that the tuner rejected; 12 tile of the second pair-kernel pass in multiples of the
  * first (1..8, default 2); 13..17 (read only) the last target range no pair-kernel pass could
- * fit: {first particle (key order), count, search radius x 1e9, leaves, overflow code}. */
+ * fit: {first particle (key order), count, search radius x 1e9, leaves, overflow code};
+ * 18 fixed time step on/off: with 1, sphgpu_step skips TimeStep and advances every run by the
+ * dt last set with sphgpu_set_scalar(SPHGPU_SCALAR_DT) (the adjoint requires it). */
 int sphgpu_set_tuning(sphgpu_ctx* ctx, int which, int value);
 int sphgpu_get_tuning(sphgpu_ctx* ctx, int which, int* value);
 
@@ -218,6 +220,42 @@ int sphgpu_bench_steps(sphgpu_ctx* ctx, int n_steps, int flush_l2, double* ms);
 /* Calibration (no reference counterpart): sustained FP32 and FP64 FMA throughput of the current
  * device in TFLOP/s, the denominators of the pair kernels' compute rooflines. */
 int sphgpu_measure_peaks(double* fp32_tflops, double* fp64_tflops);
+
+/* ---- adjoint (reverse mode) of the standard-SPH step ---------------------------------------
+ *
+ * No counterpart in the reference: these entry points serve a gradient harness.  They
+ * differentiate Solver::initialize and Solver::integrate (src/solver.cpp:392-474) with
+ * PreInteraction (src/pre_interaction.cpp:39-169, smoothing length as the root of the Newton
+ * equation, grad-h term, Balsara switch) and FluidForce (src/fluid_force.cpp:26-106) of the
+ * standard SPH form, with neighbour sets and the viscosity branch (v_ij . r_ij < 0) of the
+ * forward pass.  Supported: sph_type ssph, cubic spline or Wendland C4, no gravity, no
+ * time-dependent viscosity, no artificial conductivity, iterative smoothing length, the fixed
+ * time step (tuning knob 18), a single run.  Anything else returns SPHGPU_ERR_ARG.
+ *
+ * State vector (device pointer, caller's particle order, doubles):
+ *   [x (n*dim) | v (n*dim) | u (n) | a (n*dim) | du/dt (n) | rho (n)]  = n * (3 dim + 3)
+ * x, v, a interleaved per particle.  rho is the density the next PreInteraction starts its
+ * smoothing-length guess from.  Adjoint vector (device pointer, caller's order, doubles):
+ *   [xbar (n*dim) | vbar (n*dim) | ubar (n) | abar (n*dim) | dubar (n)]  = n * (3 dim + 2)
+ * All pointers are device pointers; the work runs on the context's stream and the calls return
+ * after it finished. */
+
+/* Copy the integrator state out of / into the context (caller order). */
+int sphgpu_get_state(sphgpu_ctx* ctx, double* state);
+int sphgpu_set_state(sphgpu_ctx* ctx, const double* state);
+
+/* Reverse one sphgpu_step.  The context must hold the state S_n the step started from
+ * (sphgpu_set_state); adj holds the adjoint of S_{n+1} on entry and that of S_n on return.
+ * dens_bar (may be NULL) is an extra adjoint of the density computed inside this step;
+ * *alpha_bar (device double) accumulates the adjoint of avAlpha.  The call recomputes the step's
+ * prediction, tree and PreInteraction, so the context holds that mid-step state afterwards. */
+int sphgpu_adjoint_step(sphgpu_ctx* ctx, double* adj, const double* dens_bar, double* alpha_bar);
+
+/* Reverse sphgpu_initialize.  The context must hold the initial fields (sphgpu_set_state with
+ * the initial x, v, u and rho; a and du/dt are ignored).  adj holds the adjoint of S_0 on entry;
+ * on return its x, v and u blocks hold the gradient with respect to the initial x, v and u, and
+ * its a and du/dt blocks are zero. */
+int sphgpu_adjoint_initialize(sphgpu_ctx* ctx, double* adj, const double* dens_bar, double* alpha_bar);
 
 /* ---- allocation-free entry point ---------------------------------------------------------- */
 

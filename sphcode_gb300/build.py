@@ -31,7 +31,7 @@ NO_FMA = {"integrate.cu", "tree.cu"}
 # every membership decision is made on products and sums only (and re-decided in FP64 inside its
 # guard band), so only the FP32 pair terms see the approximation.  FP64 arithmetic is unaffected.
 FAST_F32 = {"pre_d1.cu", "pre_d2.cu", "pre_d3.cu", "fluid_d1.cu", "fluid_d2.cu", "fluid_d3.cu",
-            "gravity.cu", "neighbors.cu"}
+            "gravity.cu", "neighbors.cu", "adjoint_d1.cu", "adjoint_d2.cu", "adjoint_d3.cu"}
 
 
 def nvcc() -> str:

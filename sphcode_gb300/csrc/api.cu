@@ -64,6 +64,23 @@ __global__ void gather_int_as_double_kernel(const int* src, const int* id, int n
     if (i < n) stage[id[i]] = (double)src[i];
 }
 
+// Integrator state in the caller's order: [x (n dim) | v (n dim) | u | a (n dim) | du/dt | rho].
+__global__ void state_io_kernel(State st, int n, int dim, double* state, int to_device)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const size_t q = (size_t)st.id[i], N = (size_t)n, nd = N * dim;
+    double* blk[6] = {state, state + nd, state + 2 * nd, state + 2 * nd + N, state + 3 * nd + N, state + 3 * nd + 2 * N};
+    const int w[6] = {dim, dim, 1, dim, 1, 1};
+    const int slot[6] = {F_POS, F_VEL, F_ENE, F_ACC, F_DENE, F_DENS};
+    for (int b = 0; b < 6; ++b)
+        for (int k = 0; k < w[b]; ++k) {
+            double* f = st.f[slot[b] + k];
+            if (to_device) f[i] = blk[b][q * w[b] + k];
+            else blk[b][q * w[b] + k] = f[i];
+        }
+}
+
 __global__ void init_ids_kernel(int* id, int* run, const int* run_begin, int R, int n)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -263,7 +280,8 @@ void free_ctx(Ctx& c)
     c.alt.run = nullptr;
     free_state(c.alt, false);
     void* ptrs[] = {c.d_run_begin, c.d_time, c.d_dt, c.d_hvs, c.d_dtmin, c.d_sums, c.d_err,
-                    c.d_newton_fail, c.d_work, c.d_ovf_list, c.d_ovf_list2, c.d_stage, c.d_aos, c.d_flush};
+                    c.d_newton_fail, c.d_work, c.d_ovf_list, c.d_ovf_list2, c.d_stage, c.d_aos, c.d_flush,
+                    c.adj_buf, c.adj_mir, c.adj_partials};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (void* p : c.mir)
@@ -541,7 +559,7 @@ void run_step(Ctx& c, bool timed)
 {
     cudaStream_t s = c.stream;
     if (timed) cudaEventRecord(c.ev[0], s);
-    launch_timestep(c);
+    if (!c.fixed_dt) launch_timestep(c);
     launch_predict(c);
     if (timed) cudaEventRecord(c.ev[1], s);
     launch_make_tree(c, false);
@@ -932,6 +950,88 @@ int sphgpu_step(sphgpu_ctx* h, int n_steps)
     return sphgpu::finish(c, "step");
 }
 
+int sphgpu_get_state(sphgpu_ctx* h, double* state)
+{
+    CTX_OR_FAIL(h);
+    if (!state) return SPHGPU_ERR_ARG;
+    sphgpu::state_io_kernel<<<sphgpu::ceil_div(c.n, 256), 256, 0, c.stream>>>(c.st, c.n, c.dim, state, 0);
+    return sphgpu::finish(c, "get_state");
+}
+
+int sphgpu_set_state(sphgpu_ctx* h, const double* state)
+{
+    CTX_OR_FAIL(h);
+    if (!state) return SPHGPU_ERR_ARG;
+    sphgpu::state_io_kernel<<<sphgpu::ceil_div(c.n, 256), 256, 0, c.stream>>>(c.st, c.n, c.dim,
+                                                                            const_cast<double*>(state), 1);
+    c.tree_valid = false;
+    return sphgpu::finish(c, "set_state");
+}
+
+namespace sphgpu {
+namespace {
+
+// Scope of the adjoint and its scratch (allocated once per context).
+int adjoint_ready(Ctx& c, const char* what)
+{
+    std::string why;
+    if (c.p.sph_type != 0) why = "standard SPH (sph_type 0) only";
+    else if (c.p.use_gravity) why = "no gravity";
+    else if (c.p.use_tdav) why = "no time-dependent viscosity";
+    else if (c.p.use_ac) why = "no artificial conductivity";
+    else if (!c.p.iterative_sml) why = "iterative smoothing length only";
+    else if (c.R != 1) why = "a single run";
+    if (!why.empty()) { c.last_error = std::string(what) + ": the adjoint supports " + why; return SPHGPU_ERR_ARG; }
+    if (!c.adj_buf) {
+        cudaError_t e = cudaMalloc(&c.adj_buf, sizeof(double) * ADJ_SLOTS * (size_t)c.n);
+        if (e == cudaSuccess) e = cudaMalloc(&c.adj_mir, sizeof(double4_32a) * ADJ_MIRRORS * (size_t)c.n);
+        if (e == cudaSuccess) e = cudaMalloc(&c.adj_partials, sizeof(double) * ADJ_PARTIALS);
+        if (e != cudaSuccess) return cuda_status(c, e, what);
+    }
+    return SPHGPU_OK;
+}
+
+void launch_adjoint(Ctx& c, double* adj, const double* dens_bar, double* alpha_bar, bool initial)
+{
+    if (c.dim == 1) launch_adjoint_dim<1>(c, adj, dens_bar, alpha_bar, initial);
+    else if (c.dim == 2) launch_adjoint_dim<2>(c, adj, dens_bar, alpha_bar, initial);
+    else launch_adjoint_dim<3>(c, adj, dens_bar, alpha_bar, initial);
+}
+
+}  // namespace
+}  // namespace sphgpu
+
+int sphgpu_adjoint_step(sphgpu_ctx* h, double* adj, const double* dens_bar, double* alpha_bar)
+{
+    CTX_OR_FAIL(h);
+    if (!adj || !alpha_bar) return SPHGPU_ERR_ARG;
+    if (!c.fixed_dt) { c.last_error = "adjoint_step: needs the fixed time step (tuning knob 18)"; return SPHGPU_ERR_STATE; }
+    if (c.first_pre) { c.last_error = "adjoint_step: before initialize"; return SPHGPU_ERR_STATE; }
+    int rc = sphgpu::adjoint_ready(c, "adjoint_step");
+    if (rc != SPHGPU_OK) return rc;
+    // forward quantities of the step: prediction, tree, PreInteraction
+    sphgpu::launch_predict(c);
+    sphgpu::launch_make_tree(c, false);
+    sphgpu::run_pre_stage(c);
+    sphgpu::launch_adjoint(c, adj, dens_bar, alpha_bar, false);
+    return sphgpu::finish(c, "adjoint_step");
+}
+
+int sphgpu_adjoint_initialize(sphgpu_ctx* h, double* adj, const double* dens_bar, double* alpha_bar)
+{
+    CTX_OR_FAIL(h);
+    if (!adj || !alpha_bar) return SPHGPU_ERR_ARG;
+    int rc = sphgpu::adjoint_ready(c, "adjoint_initialize");
+    if (rc != SPHGPU_OK) return rc;
+    // forward quantities of Solver::initialize: start-up fields, tree, first PreInteraction
+    sphgpu::launch_init_fields(c);
+    sphgpu::launch_make_tree(c, true);
+    c.first_pre = true;
+    sphgpu::run_pre_stage(c);
+    sphgpu::launch_adjoint(c, adj, dens_bar, alpha_bar, true);
+    return sphgpu::finish(c, "adjoint_initialize");
+}
+
 int sphgpu_synchronize(sphgpu_ctx* h)
 {
     CTX_OR_FAIL(h);
@@ -1049,6 +1149,7 @@ int sphgpu_set_tuning(sphgpu_ctx* h, int which, int value)
         c.pass2_scale = value;
         break;
     case 4: c.autotune = value != 0; break;
+    case 18: c.fixed_dt = value != 0; break;
     case 5: c.timing = value != 0; break;
     case 6: c.use_graph = value != 0; break;
     default: return SPHGPU_ERR_ARG;
@@ -1076,6 +1177,7 @@ int sphgpu_get_tuning(sphgpu_ctx* h, int which, int* value)
     case 10: *value = c.tile_cap_pre; break;
     case 11: *value = (int)c.tune_rejects; break;
     case 12: *value = c.pass2_scale; break;
+    case 18: *value = c.fixed_dt ? 1 : 0; break;
     case 13: case 14: case 15: case 16: case 17: {
         cudaStreamSynchronize(c.stream);
         cudaMemcpy(value, c.d_work + sphgpu::FAIL_INFO_SLOT + (which - 13), sizeof(int), cudaMemcpyDeviceToHost);

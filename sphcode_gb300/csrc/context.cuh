@@ -119,6 +119,12 @@ struct Ctx {
     int stage_ovf[2] = {0, 0};      // groups sent to the overflow pass by Pre / Fluid (timing mode)
     int tile_cap_pre = 0;           // per-stage source tile capacities (0 = automatic)
     int pass2_scale = 2;            // tile of the second pair pass, in multiples of the first
+    bool fixed_dt = false;          // steps keep the dt set by the caller (no TimeStep)
+
+    // adjoint scratch (allocated on the first adjoint call)
+    double* adj_buf = nullptr;      // ADJ_SLOTS x n doubles
+    void* adj_mir = nullptr;        // ADJ_MIRRORS x n four-vectors of the pair type
+    double* adj_partials = nullptr; // block partials of the avAlpha adjoint
 
     std::string last_error;
 };
@@ -143,6 +149,20 @@ void launch_fluid(Ctx& c);
 void launch_gravity(Ctx& c);
 void launch_gravity_mirror(Ctx& c);
 void launch_neighbors(Ctx& c, int is_ij, int* d_counts, int* d_list, int cap);
+
+// ---- adjoint_dD.cu
+// Scratch slots of n doubles each (key order) of the adjoint passes.
+enum AdjSlot : int {
+    AS_RHOH = 0, AS_RHOHH = 1, AS_DV = 2, AS_DVH = 3, AS_RT = 4, AS_RTH = 7,
+    AL_X = 10, AL_V = 13, AL_RHO = 16, AL_P = 17, AL_G = 18, AL_H = 19, AL_C = 20, AL_B = 21,
+    AL_ALPHA = 22, AU_LOC = 23, AG_X = 24, AG_V = 27,
+    ADJ_SLOTS = 30
+};
+constexpr int ADJ_MIRRORS = 6;       // a0..a3, w0, w1 (one four-vector of the pair type each)
+constexpr int ADJ_PARTIALS = 1024;   // block partials of the avAlpha adjoint
+
+template <int D>
+void launch_adjoint_dim(Ctx& c, double* adj, const double* dens_bar, double* alpha_bar, bool initial);
 
 // ---- integrate.cu
 void launch_timestep(Ctx& c);

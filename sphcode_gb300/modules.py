@@ -129,7 +129,7 @@ class Output:
         dim = p["pos"].shape[1]
         int_cols = {3 * dim + 5, 3 * dim + 6}
         with open(path, "w") as f:
-            f.write("# %r\n" % sim.get_time())
+            f.write("# %r\n" % float(sim.get_time()))
             for row in table:
                 f.write(" ".join(("%d" % int(v)) if c in int_cols else repr(float(v))
                                  for c, v in enumerate(row)) + " \n")
@@ -139,7 +139,7 @@ class Output:
     def output_energy(self, sim: Simulation) -> np.ndarray:
         """``time kinetic thermal potential total`` (src/output.cpp:66-90)."""
         e = sim.gpu.energy()
-        self._energy.write("%r %r %r %r %r\n" % (sim.get_time(), e[0], e[1], e[2], e[3]))
+        self._energy.write(" ".join(repr(float(x)) for x in (sim.get_time(), e[0], e[1], e[2], e[3])) + "\n")
         self._energy.flush()
         return e
 

@@ -31,7 +31,7 @@ STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_NODE_POOL", 4: "ERR_CAPA
 
 TUNING = {"group_warps": 0, "fluid_warps": 1, "gravity_warps": 2, "tile_cap": 3, "autotune": 4,
           "timing": 5, "graph": 6, "graph_kernels": 7, "overflow_pre": 8, "overflow_fluid": 9,
-          "tile_cap_pre": 10, "tune_rejects": 11, "pass2_scale": 12}
+          "tile_cap_pre": 10, "tune_rejects": 11, "pass2_scale": 12, "fixed_dt": 18}
 
 
 class SphGpuError(RuntimeError):
@@ -85,6 +85,10 @@ _SIGS = {
     "sphgpu_bench_steps": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "sphgpu_measure_peaks": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "sphgpu_energy_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _P, _P, _P, _P, _P, _P]),
+    "sphgpu_get_state": (ctypes.c_int, [_P, _P]),
+    "sphgpu_set_state": (ctypes.c_int, [_P, _P]),
+    "sphgpu_adjoint_step": (ctypes.c_int, [_P, _P, _P, _P]),
+    "sphgpu_adjoint_initialize": (ctypes.c_int, [_P, _P, _P, _P]),
 }
 
 
@@ -190,6 +194,29 @@ class GpuSimulation:
     def set_scalar(self, which: str, value: float, run: int = 0) -> None:
         _check(self.lib.sphgpu_set_scalar(self._h, {"time": 0, "dt": 1, "h_per_v_sig": 2}[which], run,
                                           float(value)), "set_scalar", self._h)
+
+    # ---- integrator state and adjoint (device pointers, caller order) -------------------------
+    def state_size(self) -> int:
+        """Doubles of the state vector [x | v | u | a | du/dt | rho]."""
+        return self.n * (3 * self.dim + 3)
+
+    def adjoint_size(self) -> int:
+        """Doubles of the adjoint vector [xbar | vbar | ubar | abar | dubar]."""
+        return self.n * (3 * self.dim + 2)
+
+    def get_state(self, dev_ptr: int) -> None:
+        _check(self.lib.sphgpu_get_state(self._h, _P(dev_ptr)), "get_state", self._h)
+
+    def set_state(self, dev_ptr: int) -> None:
+        _check(self.lib.sphgpu_set_state(self._h, _P(dev_ptr)), "set_state", self._h)
+
+    def adjoint_step(self, adj_ptr: int, dens_bar_ptr: int, alpha_bar_ptr: int) -> None:
+        _check(self.lib.sphgpu_adjoint_step(self._h, _P(adj_ptr), _P(dens_bar_ptr or None), _P(alpha_bar_ptr)),
+               "adjoint_step", self._h)
+
+    def adjoint_initialize(self, adj_ptr: int, dens_bar_ptr: int, alpha_bar_ptr: int) -> None:
+        _check(self.lib.sphgpu_adjoint_initialize(self._h, _P(adj_ptr), _P(dens_bar_ptr or None),
+                                                  _P(alpha_bar_ptr)), "adjoint_initialize", self._h)
 
     # ---- stages -----------------------------------------------------------------------------
     def initialize(self) -> None:

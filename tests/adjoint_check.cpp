@@ -400,7 +400,45 @@ void check_single(int side, double eps, int balsara, int which, double* out)
     out[4] = gu; out[5] = (L(sh(2, eps)) - L(sh(2, -eps))) / (2 * eps);
 }
 
+// Gradient of L = sum (rho_final - 1)^2 for given initial fields (n particles of mass 1/n in the
+// periodic unit box [-0.5, 0.5)^2, gamma 5/3): gv (n*2), gu (n), *galpha, and rho_final (n).
+template <int K>
+void gradient_of(int n, int steps, double dt, double alpha, double nnb, int balsara, const double* x,
+                 const double* v, const double* u, double* gv_out, double* gu_out, double* galpha,
+                 double* rho_out)
+{
+    Run R;
+    R.K = K;
+    R.n = n;
+    R.m = 1.0 / n;
+    R.nnb = nnb;
+    R.dt = dt;
+    R.alpha = alpha;
+    R.balsara = balsara != 0;
+    St s;
+    s.x.assign(x, x + n * D);
+    s.v.assign(v, v + n * D);
+    s.u.assign(u, u + n);
+    std::vector<double> gv, gu;
+    gradient<K>(R, s, steps, alpha, gv, *galpha, gu);
+    for (int i = 0; i < n * D; ++i) gv_out[i] = gv[i];
+    for (int i = 0; i < n; ++i) gu_out[i] = gu[i];
+    St f = s;
+    Pre p;
+    initialize<K>(R, f, p, alpha);
+    for (int t = 0; t < steps; ++t) step<K>(R, f, p, alpha);
+    for (int i = 0; i < n; ++i) rho_out[i] = p.rho[i];
+}
+
 }  // namespace
+
+extern "C" void adj_gradient(int kernel, int n, int steps, double dt, double alpha, double nnb, int balsara,
+                             const double* x, const double* v, const double* u, double* gv, double* gu,
+                             double* galpha, double* rho)
+{
+    if (kernel == 0) gradient_of<0>(n, steps, dt, alpha, nnb, balsara, x, v, u, gv, gu, galpha, rho);
+    else gradient_of<1>(n, steps, dt, alpha, nnb, balsara, x, v, u, gv, gu, galpha, rho);
+}
 
 extern "C" void adj_check_single(int kernel, int side, double eps, int balsara, int which, double* out)
 {
