@@ -222,6 +222,35 @@ def run_reference_arm(args):
 
 
 # ---- GPU arm -----------------------------------------------------------------------------------
+def adjoint_report():
+    """The Gresho-Chan adjoint: 256 x 256 lattice (65,536 particles), ssph, cubic spline, 200
+    steps at the fixed CFL dt of the initial state, a checkpoint every 20 steps, loss
+    L = sum (rho_final - 1)^2, gradients in the initial velocities, the initial internal energy and
+    avAlpha.  Reports the backward/forward wall-time ratio in both precisions, central finite
+    differences of the FP64 forward pass over 20 steps, the FP32-pair gradient against FP64, and
+    how far a 1e-12 velocity perturbation grows over the 200 steps."""
+    from sphcode_gb300 import ics
+    from sphcode_gb300.adjoint import cost_and_precision, finite_difference_check, perturbation_growth
+    p, f = ics.gresho(256)
+    steps, k, fd_steps = 200, 20, 20
+    cost = cost_and_precision(p, f, steps, checkpoint_every=k)
+    dt = cost["dt"]
+    fd = finite_difference_check(p, f, fd_steps, dt, eps=1e-7)
+    prec = cost_and_precision(p, f, fd_steps, dt=dt, checkpoint_every=k, reps=1)["fp32_vs_fp64"]
+    growth = perturbation_growth(p, f, steps, dt)
+    return {"workload": "gresho-chan 256x256 (65,536), ssph cubic, periodic, gamma 5/3, fixed dt "
+                        "(initial CFL step), loss sum (rho_final - 1)^2",
+            "steps": steps, "checkpoint_every": k, "dt": dt, "n_particles": int(f["mass"].size),
+            "cost": {pr: cost[pr] for pr in ("fp32", "fp64")},
+            "fd_check": {"steps": fd_steps, "eps": fd["eps"],
+                         "directions": "dL/dv0 and dL/du0 along themselves, dL/davAlpha",
+                         "rel_err": {"v0": fd["v"], "u0": fd["u"], "alpha": fd["alpha"]},
+                         "adjoint": fd["adjoint"], "fd": fd["fd"]},
+            "fp32_vs_fp64": {"steps": fd_steps, **prec},
+            "fp32_vs_fp64_200_steps": cost["fp32_vs_fp64"],
+            "perturbation_growth": {"size": 1e-12, "every": 20, "max_abs_drho": growth}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -236,6 +265,8 @@ def main():
     ap.add_argument("--group-warps", type=int, default=0,
                     help="target-group size in warps (0 = the library's default)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true",
+                    help="skip the Gresho-Chan adjoint cost / finite-difference report")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--pass2-scale", type=int, default=0)
     ap.add_argument("--tile-pre", type=int, default=0)
@@ -431,6 +462,10 @@ def main():
         v, kind, sample, _ = cpu_reference_run(args.workload, args.ref_steps, threads)
         cpu = {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": kind, "sample": sample}
 
+    adjoint = None
+    if rank == 0 and world == 1 and not args.no_adjoint:
+        adjoint = adjoint_report()
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -448,7 +483,8 @@ def main():
                 "schedule": schedule,
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
                 "gpu_launches": launches_per_step * args.steps,
-                "peaks": {"fp32_tflops": fp32_peak, "fp64_tflops": fp64_peak}}
+                "peaks": {"fp32_tflops": fp32_peak, "fp64_tflops": fp64_peak},
+                "adjoint": adjoint}
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

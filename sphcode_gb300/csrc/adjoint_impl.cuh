@@ -139,6 +139,8 @@ __global__ void __launch_bounds__(256) adj_pass1_kernel(AdjArgs<T> a)
         const T h_i = (T)hi;
         const T m_i = (T)a.st.f[F_MASS][i];
         const sphadj::FluidSide<T> si = adj_side<D, T>(a, i, m_i, h_i);
+        const T s_i = K == 0 ? T(0.5) * h_i : h_i;
+        const T sinv_i = T(1) / s_i, hinv_i = T(1) / h_i;
         Sum<T> rho_h, rho_hh, dv, dv_h, rt[3], rt_h[3];
         Sum<T> xb[D], vb[D], rhob, pb, gb_, hb, cb, bb, ab;
         rho_h.zero(); rho_hh.zero(); dv.zero(); dv_h.zero();
@@ -160,25 +162,26 @@ __global__ void __launch_bounds__(256) adj_pass1_kernel(AdjArgs<T> a)
             T vij[3] = {T(0), T(0), T(0)};
 #pragma unroll
             for (int k = 0; k < D; ++k) vij[k] = si.v[k] - sj.v[k];
-            {
-                sphadj::PreSums<T> ps;
-                ps.zero();
-                sphadj::pre_sums_add<D, K, T>(ps, rv, vij, m_j, h_i);
-                rho_h.add(ps.rho_h);
-                rho_hh.add(ps.rho_hh);
-                dv.add(ps.Dv);
-                dv_h.add(ps.Dv_h);
-#pragma unroll
-                for (int k = 0; k < NR; ++k) { rt[k].add(ps.Rt[k]); rt_h[k].add(ps.Rt_h[k]); }
-            }
-            if (j == i || r2 == T(0)) continue;   // FluidForce skips r == 0
-            sphadj::SideAdj<T> mine, other;
+            sphadj::PreSums<T> ps;
+            ps.zero();
+            sphadj::SideAdj<T> mine;
             mine.zero();
-            other.zero();
-            T alpha_bar = T(0), unused = T(0);
-            sphadj::fluid_pair_vjp<D, K, T>(rv, si, sj, a.alpha, mine, other, alpha_bar);
-            const T rji[3] = {-rv[0], -rv[1], -rv[2]};
-            sphadj::fluid_pair_vjp<D, K, T>(rji, sj, si, a.alpha, other, mine, unused);
+            T alpha_bar = T(0);
+            if (r2 == T(0)) {
+                // the particle itself (or one at the same position): only the density-type sums;
+                // FluidForce skips r == 0
+                sphadj::pre_sums_add<D, K, T>(ps, rv, vij, m_j, h_i);
+            } else {
+                sphadj::pass1_pair<D, K, T>(rv, vij, r2, si, sj, s_i, sinv_i, hinv_i, T(1) / h_j, a.alpha,
+                                            ps, mine, alpha_bar);
+            }
+            rho_h.add(ps.rho_h);
+            rho_hh.add(ps.rho_hh);
+            dv.add(ps.Dv);
+            dv_h.add(ps.Dv_h);
+#pragma unroll
+            for (int k = 0; k < NR; ++k) { rt[k].add(ps.Rt[k]); rt_h[k].add(ps.Rt_h[k]); }
+            if (r2 == T(0)) continue;
 #pragma unroll
             for (int k = 0; k < D; ++k) { xb[k].add(mine.x[k]); vb[k].add(mine.v[k]); }
             rhob.add(mine.rho);
@@ -244,6 +247,8 @@ __global__ void __launch_bounds__(256) adj_pass2_kernel(AdjArgs<T> a)
 
         const T h_i = (T)hi;
         const T m_i = (T)a.st.f[F_MASS][i];
+        const T s_i = K == 0 ? T(0.5) * h_i : h_i;
+        const T sinv_i = T(1) / s_i, hinv_i = T(1) / h_i;
         const V4 q0 = a.a0[i];
         const T v_i[3] = {q0.x, q0.y, q0.z};
         sphadj::PreWeights<T> wi;
@@ -278,8 +283,16 @@ __global__ void __launch_bounds__(256) adj_pass2_kernel(AdjArgs<T> a)
                 if (D == 3) { const V4 w1 = a.w1[j]; wj.Rtbar[1] = w1.x; wj.Rtbar[2] = w1.y; }
             }
             T dx[3] = {T(0), T(0), T(0)}, dvv[3] = {T(0), T(0), T(0)};
-            sphadj::pre_pair_gather<D, K, T>(rv, vij, m_j, h_i, wi, dx, dvv);
-            sphadj::pre_pair_gather<D, K, T>(rv, vij, m_i, h_j, wj, dx, dvv);
+            const T rinv = T(1) / sqrt(r2);
+            const T r = r2 * rinv;
+            const T hinv_j = T(1) / h_j;
+            const T s_j = K == 0 ? T(0.5) * h_j : h_j;
+            const T sinv_j = K == 0 ? T(2) * hinv_j : hinv_j;
+            sphadj::KVals<T> ki, kj;
+            sphadj::kvals<D, K, T, true>(r, rinv, s_i, sinv_i, hinv_i, ki);
+            sphadj::kvals<D, K, T, true>(r, rinv, s_j, sinv_j, hinv_j, kj);
+            sphadj::pre_pair_gather_k<D, T>(rv, vij, rinv, m_j, ki, wi, dx, dvv);
+            sphadj::pre_pair_gather_k<D, T>(rv, vij, rinv, m_i, kj, wj, dx, dvv);
 #pragma unroll
             for (int k = 0; k < D; ++k) { xb[k].add(dx[k]); vb[k].add(dvv[k]); }
         }

@@ -269,4 +269,146 @@ SPH_HD void pre_pair_gather(const T* rv, const T* vij, T mb, T ha, const PreWeig
     }
 }
 
+// ---- fused forms for the device passes ----------------------------------------------------------
+
+// Kernel values of one side of a pair (r > 0) from a single evaluation of the kernel shape:
+// F = dW/dr / r, F_r = dF/dr, F_h = dF/dh, W_h = dW/dh, W_hh = d2W/dh2 (kderiv.cuh).
+// s = scale(h) (h / 2 for the cubic spline, h for C4), sinv = 1 / s, hinv = 1 / h.
+template <typename T>
+struct KVals {
+    T F, Fr, Fh, Wh, Whh;
+};
+
+template <int D, int K, typename T, bool WITH_H>
+SPH_HD void kvals(T r, T rinv, T s, T sinv, T hinv, KVals<T>& o)
+{
+    using KF = sphkd::KD<D, K, T>;
+    const T q = r * sinv;
+    T w0, w1, w2;
+    sphkd::shape<K, T>(q, w0, w1, w2);
+    const T cD = KF::sig() * sphkd::ipow<D>(sinv);   // sigma / s^D
+    const T c2 = cD * sinv * sinv;                     // sigma / s^(D+2)
+    const T qinv = s * rinv;
+    const T g = w1 * qinv;                             // omega' / q
+    o.F = c2 * g;
+    o.Fr = c2 * sinv * (w2 - g) * qinv;
+    if (WITH_H) {
+        o.Fh = -c2 * (T(D + 1) * g + w2) * hinv;
+        const T chi = T(D) * w0 + q * w1;
+        const T chi1 = T(D + 1) * w1 + q * w2;
+        o.Wh = -cD * chi * hinv;
+        o.Whh = cD * (T(D + 1) * chi + q * chi1) * hinv * hinv;
+    } else {
+        o.Fh = o.Wh = o.Whh = T(0);
+    }
+}
+
+// One pair (i, j), r_ij != 0, as seen from particle i in the first device pass: adds to i's
+// density-type sums (kernel at h_i) and to i's adjoints the part of the two pair terms
+// T1 = (target i, source j) and T2 = (target j, source i) of a and du/dt that depends on i's
+// inputs.  T1 and T2 share Q = -(F_i A_i + F_j A_j + Pi (F_i + F_j) / 2), so
+//   L = cQ Q + c1 S1 + c2 S2,  cQ = (m_j abar_i - m_i abar_j) . r_ij,
+//   c1 = m_j dubar_i v_ij . r_ij,  c2 = m_i dubar_j v_ij . r_ij,
+//   S1 = A_i F_i + Pi Fsum / 4,  S2 = A_j F_j + Pi Fsum / 4,
+// plus the explicit r_ij of the acceleration terms.  Every r_ij and v_ij dependence belongs to
+// x_i and v_i; of Pi's symmetric inputs i takes its own half.  alpha_bar gets half of the pair's
+// avAlpha adjoint (j's visit adds the other half).  hinv_j is 1 / h_j.
+template <int D, int K, typename T>
+SPH_HD void pass1_pair(const T* rv, const T* vij, T r2, const FluidSide<T>& si, const FluidSide<T>& sj,
+                       T s_i, T sinv_i, T hinv_i, T hinv_j, T alpha,
+                       PreSums<T>& ps, SideAdj<T>& mine, T& alpha_bar)
+{
+    const T rinv = T(1) / sqrt(r2);
+    const T r = r2 * rinv;
+    KVals<T> ki, kj;
+    kvals<D, K, T, true>(r, rinv, s_i, sinv_i, hinv_i, ki);
+    const T sinv_j = K == 0 ? T(2) * hinv_j : hinv_j;
+    kvals<D, K, T, false>(r, rinv, T(1) / sinv_j, sinv_j, hinv_j, kj);
+    T vr = T(0);
+    for (int k = 0; k < D; ++k) vr += vij[k] * rv[k];
+    // density-type sums of i
+    ps.rho_h += sj.m * ki.Wh;
+    ps.rho_hh += sj.m * ki.Whh;
+    ps.Dv += sj.m * vr * ki.F;
+    ps.Dv_h += sj.m * vr * ki.Fh;
+    {
+        T cr[3];
+        cross_of<D, T>(vij, rv, cr);
+        for (int k = 0; k < 3; ++k) { ps.Rt[k] += sj.m * ki.F * cr[k]; ps.Rt_h[k] += sj.m * ki.Fh * cr[k]; }
+    }
+    // fluid pair terms
+    const T rho2i = T(1) / (si.rho * si.rho), rho2j = T(1) / (sj.rho * sj.rho);
+    const T Ai = si.P * si.g * rho2i, Aj = sj.P * sj.g * rho2j;
+    T Pi = T(0), w = T(0), Bb = T(0), vs = T(0), Rr = T(0);
+    const bool visc = vr < T(0);
+    if (visc) {
+        w = vr * rinv;
+        Bb = T(0.5) * (si.B + sj.B);
+        vs = si.c + sj.c - T(3) * w;
+        Rr = T(2) / (si.rho + sj.rho);
+        Pi = T(-0.5) * Bb * alpha * vs * w * Rr;
+    }
+    const T Fsum = ki.F + kj.F;
+    const T Q = -(ki.F * Ai + kj.F * Aj + T(0.5) * Pi * Fsum);
+    T dab[3] = {T(0), T(0), T(0)};
+    T cQ = T(0);
+    for (int k = 0; k < D; ++k) { dab[k] = sj.m * si.abar[k] - si.m * sj.abar[k]; cQ += dab[k] * rv[k]; }
+    const T c1 = sj.m * si.dubar * vr, c2 = si.m * sj.dubar * vr;
+    const T S1 = Ai * ki.F + T(0.25) * Pi * Fsum;
+    const T S2 = Aj * kj.F + T(0.25) * Pi * Fsum;
+    const T Fbi = -cQ * (Ai + T(0.5) * Pi) + c1 * (Ai + T(0.25) * Pi) + c2 * (T(0.25) * Pi);
+    const T Fbj = -cQ * (Aj + T(0.5) * Pi) + c1 * (T(0.25) * Pi) + c2 * (Aj + T(0.25) * Pi);
+    const T Abi = (c1 - cQ) * ki.F;
+    const T Pib = (T(-0.5) * cQ + T(0.25) * (c1 + c2)) * Fsum;
+    T vrbar = sj.m * si.dubar * S1 + si.m * sj.dubar * S2;
+    T rbar = Fbi * ki.Fr + Fbj * kj.Fr;
+    mine.h += Fbi * ki.Fh;
+    if (visc) {
+        const T wbar = Pib * (T(-0.5) * Bb * alpha * Rr * (vs - T(3) * w));
+        mine.B += T(0.5) * Pib * (T(-0.5) * alpha * vs * w * Rr);
+        alpha_bar += T(0.5) * Pib * (T(-0.5) * Bb * vs * w * Rr);
+        const T Rrbar = Pib * (T(-0.5) * Bb * alpha * vs * w);
+        mine.c += Pib * (T(-0.5) * Bb * alpha * w * Rr);
+        mine.rho += Rrbar * (T(-0.5) * Rr * Rr);
+        vrbar += wbar * rinv;
+        rbar -= wbar * vr * rinv * rinv;
+    }
+    mine.P += Abi * si.g * rho2i;
+    mine.g += Abi * si.P * rho2i;
+    mine.rho += Abi * (T(-2) * Ai / si.rho);
+    for (int k = 0; k < D; ++k) {
+        mine.x[k] += Q * dab[k] + vrbar * vij[k] + rbar * rv[k] * rinv;
+        mine.v[k] += vrbar * rv[k];
+    }
+}
+
+// pre_pair_gather with the kernel values of side a already evaluated (kvals with WITH_H).
+template <int D, typename T>
+SPH_HD void pre_pair_gather_k(const T* rv, const T* vij, T rinv, T mb, const KVals<T>& ka,
+                              const PreWeights<T>& wa, T* xbar, T* vbar)
+{
+    T vr = T(0);
+    for (int k = 0; k < D; ++k) vr += vij[k] * rv[k];
+    const T F = ka.F, Fr = ka.Fr, Fh = ka.Fh;
+    const T cw = mb * (wa.w_rho * F + wa.w_rhoh * Fh);
+    const T cd = wa.Dbar * mb;
+    T cr[3];
+    cross_of<D, T>(vij, rv, cr);
+    T rt = T(0);
+    for (int k = 0; k < 3; ++k) rt += wa.Rtbar[k] * cr[k];
+    T rbv[3] = {T(0), T(0), T(0)}, rvb[3] = {T(0), T(0), T(0)};
+    if (D == 2) {
+        rbv[0] = -wa.Rtbar[0] * vij[1]; rbv[1] = wa.Rtbar[0] * vij[0];
+        rvb[0] = wa.Rtbar[0] * rv[1];   rvb[1] = -wa.Rtbar[0] * rv[0];
+    } else if (D == 3) {
+        cross_of<D, T>(wa.Rtbar, vij, rbv);
+        cross_of<D, T>(rv, wa.Rtbar, rvb);
+    }
+    const T cx = cd * vr * Fr * rinv + mb * Fr * rinv * rt;
+    for (int k = 0; k < D; ++k) {
+        xbar[k] += cw * rv[k] + cd * vij[k] * F + cx * rv[k] + mb * F * rbv[k];
+        vbar[k] += cd * F * rv[k] + mb * F * rvb[k];
+    }
+}
+
 }  // namespace sphadj

@@ -162,7 +162,7 @@ double loss(const Run& R, St s, int steps, double alpha)
 // Backward through Pre and Fluid at (x, v, u): abar / dubar are the adjoints of the fluid outputs,
 // rhobar_ext an extra adjoint of the density.  Adds the results to xbar, vbar, ubar; returns the
 // alpha adjoint.
-template <int K>
+template <int K, bool FUSED = true>
 double pre_fluid_backward(const Run& R, const std::vector<double>& x, const std::vector<double>& v,
                           const std::vector<double>& u, const Pre& p, double alpha,
                           const std::vector<double>& abar, const std::vector<double>& dubar,
@@ -189,6 +189,13 @@ double pre_fluid_backward(const Run& R, const std::vector<double>& x, const std:
             double r[3] = {0, 0, 0}, vij[3] = {0, 0, 0};
             rvec(x, i, j, r);
             for (int k = 0; k < D; ++k) vij[k] = v[i * D + k] - v[j * D + k];
+            if (FUSED && j != i) {
+                const sphadj::FluidSide<double> sj = side(j);
+                const double s_i = K == 0 ? 0.5 * p.h[i] : p.h[i];
+                sphadj::pass1_pair<D, K, double>(r, vij, r[0] * r[0] + r[1] * r[1], si, sj, s_i, 1.0 / s_i,
+                                                 1.0 / p.h[i], 1.0 / p.h[j], alpha, sums[i], loc[i], alpha_bar);
+                continue;
+            }
             sphadj::pre_sums_add<D, K, double>(sums[i], r, vij, R.m, p.h[i]);
             if (j == i) continue;
             const sphadj::FluidSide<double> sj = side(j);
@@ -218,6 +225,16 @@ double pre_fluid_backward(const Run& R, const std::vector<double>& x, const std:
             double r[3] = {0, 0, 0}, vij[3] = {0, 0, 0};
             rvec(x, i, j, r);
             for (int k = 0; k < D; ++k) vij[k] = v[i * D + k] - v[j * D + k];
+            if (FUSED) {
+                const double rr = sqrt(r[0] * r[0] + r[1] * r[1]), rinv = 1.0 / rr;
+                sphadj::KVals<double> ki, kj;
+                const double si_ = K == 0 ? 0.5 * p.h[i] : p.h[i], sj_ = K == 0 ? 0.5 * p.h[j] : p.h[j];
+                sphadj::kvals<D, K, double, true>(rr, rinv, si_, 1.0 / si_, 1.0 / p.h[i], ki);
+                sphadj::kvals<D, K, double, true>(rr, rinv, sj_, 1.0 / sj_, 1.0 / p.h[j], kj);
+                sphadj::pre_pair_gather_k<D, double>(r, vij, rinv, R.m, ki, W[i], xb, vb);
+                sphadj::pre_pair_gather_k<D, double>(r, vij, rinv, R.m, kj, W[j], xb, vb);
+                continue;
+            }
             sphadj::pre_pair_gather<D, K, double>(r, vij, R.m, p.h[i], W[i], xb, vb);
             sphadj::pre_pair_gather<D, K, double>(r, vij, R.m, p.h[j], W[j], xb, vb);
         }
@@ -380,7 +397,18 @@ void check_single(int side, double eps, int balsara, int which, double* out)
     Pre p;
     pre_pass<K>(R, s.x, s.v, s.u, p);
     std::vector<double> xb(R.n * D, 0), vb(R.n * D, 0), ub(R.n, 0);
-    pre_fluid_backward<K>(R, s.x, s.v, s.u, p, R.alpha, ca, cdu, crho, xb, vb, ub);
+    const double ab = pre_fluid_backward<K>(R, s.x, s.v, s.u, p, R.alpha, ca, cdu, crho, xb, vb, ub);
+    {
+        // the fused device forms against the two-call forms
+        std::vector<double> xb2(R.n * D, 0), vb2(R.n * D, 0), ub2(R.n, 0);
+        const double ab2 = pre_fluid_backward<K, false>(R, s.x, s.v, s.u, p, R.alpha, ca, cdu, crho, xb2, vb2, ub2);
+        double d = fabs(ab - ab2) / (fabs(ab2) + 1e-300), mx = 0, mv = 0, mu = 0;
+        for (int i = 0; i < R.n * D; ++i) { mx = fmax(mx, fabs(xb2[i])); mv = fmax(mv, fabs(vb2[i])); }
+        for (int i = 0; i < R.n; ++i) mu = fmax(mu, fabs(ub2[i]));
+        for (int i = 0; i < R.n * D; ++i) { d = fmax(d, fabs(xb[i] - xb2[i]) / mx); d = fmax(d, fabs(vb[i] - vb2[i]) / mv); }
+        for (int i = 0; i < R.n; ++i) d = fmax(d, fabs(ub[i] - ub2[i]) / (mu + 1e-300));
+        out[6] = d;
+    }
     std::vector<double> dx(R.n * D), dv(R.n * D), du(R.n);
     for (auto& q : dx) q = rnd() - 0.5;
     for (auto& q : dv) q = rnd() - 0.5;

@@ -39,8 +39,10 @@ def rel(a, b):
 @pytest.mark.parametrize("balsara", [0, 1])
 @pytest.mark.parametrize("which", [1, 2, 4])
 def test_single_evaluation(lib, kernel, balsara, which):
-    out = (ctypes.c_double * 6)()
+    out = (ctypes.c_double * 7)()
     lib.adj_check_single(kernel, 10, 1e-6, balsara, which, out)
+    # the fused forms of the device passes equal the two-call forms
+    assert out[6] <= 1e-12, out[6]
     for k, name in enumerate(("x", "v", "u")):
         adj, fd = out[2 * k], out[2 * k + 1]
         if fd == 0.0:
