@@ -274,9 +274,27 @@ def main():
     ap.add_argument("--profile-run", action="store_true",
                     help="initialize + --steps eager steps and exit (a short, fixed launch sequence "
                          "for ncu: no timing, graphs, CPU baseline or e2e)")
+    ap.add_argument("--profile-adjoint", action="store_true",
+                    help="Gresho 256x256: --steps steps forward and backward through the adjoint, then exit "
+                         "(a short, fixed launch sequence for ncu)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference_arm(args)
+        return
+    if args.profile_adjoint:
+        # a fixed, short launch sequence of the adjoint for ncu: the Gresho vortex (256 x 256),
+        # initialize + --steps steps forward and their reversal, FP32-pair form
+        import __graft_entry__ as g
+        g.build()
+        import torch
+        from sphcode_gb300 import ics
+        from sphcode_gb300.adjoint import SphRun
+        p, f = ics.gresho(256)
+        run = SphRun(p, f, args.steps, dt=5.915e-4, precision=args.precision, checkpoint_every=args.steps)
+        rho = run.forward(torch.tensor(f["vel"], device="cuda"), torch.tensor(f["ene"], device="cuda"), p.av_alpha)
+        run.backward(2 * (rho - 1))
+        print(json.dumps({"profile_adjoint": "gresho 256x256", "steps": args.steps, "precision": args.precision}))
+        run.close()
         return
     if args.profile_run:
         import __graft_entry__ as g
@@ -287,6 +305,12 @@ def main():
             sim.set_tuning("graph", 0)
             if args.no_autotune:
                 sim.set_tuning("autotune", 0)
+            if args.group_warps:
+                sim.set_tuning("group_warps", args.group_warps)
+            if args.tile_pre:
+                sim.set_tuning("tile_cap_pre", args.tile_pre)
+            if args.tile_fluid:
+                sim.set_tuning("tile_cap", args.tile_fluid)
             sim.initialize()
             sim.step(args.steps)
             print(json.dumps({"profile_run": desc, "n": sim.n, "steps": args.steps,
@@ -454,6 +478,18 @@ def main():
                         "algorithmic_bytes_per_launch": fluid_bytes,
                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}}
     roofline["frac"] = roofline["achieved"] / fp32_peak if fp32_peak > 0 else None
+    if args.workload == "khi":
+        # DRAM bytes of one fluid_kernel launch from the committed ncu capture of this workload
+        import re
+        try:
+            prof = open(os.path.join(ROOT, "profiles", "pair_kernels_khi_786k_fp32.md")).read()
+            m = re.search(r"traffic_bytes_per_launch fluid_kernel: (\d+)", prof)
+            if m:
+                roofline["traffic"] = int(m.group(1))
+                roofline["traffic_source"] = "ncu dram__bytes_read.sum + dram__bytes_write.sum, " \
+                                             "profiles/pair_kernels_khi_786k_fp32.md"
+        except OSError:
+            pass
 
     # ---- CPU baseline (rank 0, N = 1) -------------------------------------------------------------
     cpu = None

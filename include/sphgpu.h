@@ -221,14 +221,15 @@ int sphgpu_bench_steps(sphgpu_ctx* ctx, int n_steps, int flush_l2, double* ms);
  * device in TFLOP/s, the denominators of the pair kernels' compute rooflines. */
 int sphgpu_measure_peaks(double* fp32_tflops, double* fp64_tflops);
 
-/* ---- adjoint (reverse mode) of the standard-SPH step ---------------------------------------
+/* ---- adjoint (reverse mode) of the SPH step (ssph, disph) -----------------------------------
  *
  * No counterpart in the reference: these entry points serve a gradient harness.  They
  * differentiate Solver::initialize and Solver::integrate (src/solver.cpp:392-474) with
  * PreInteraction (src/pre_interaction.cpp:39-169, smoothing length as the root of the Newton
- * equation, grad-h term, Balsara switch) and FluidForce (src/fluid_force.cpp:26-106) of the
- * standard SPH form, with neighbour sets and the viscosity branch (v_ij . r_ij < 0) of the
- * forward pass.  Supported: sph_type ssph, cubic spline or Wendland C4, no gravity, no
+ * equation, grad-h term, Balsara switch) and FluidForce (src/fluid_force.cpp:26-106), with
+ * neighbour sets and the viscosity branch (v_ij . r_ij < 0) of the
+ * forward pass.  Supported: sph_type ssph or disph (src/disph/d_pre_interaction.cpp:21-230,
+ * src/disph/d_fluid_force.cpp:26-86), cubic spline or Wendland C4, no gravity, no
  * time-dependent viscosity, no artificial conductivity, iterative smoothing length, the fixed
  * time step (tuning knob 18), a single run.  Anything else returns SPHGPU_ERR_ARG.
  *

@@ -1,5 +1,6 @@
-// Reverse mode of one standard-SPH PreInteraction + FluidForce on the device, and the leapfrog
-// around it (Solver::predict / correct, src/solver.cpp:431-474).
+// Reverse mode of one PreInteraction + FluidForce on the device, standard form (TYPE 0) or
+// pressure-energy form (TYPE 1), and the leapfrog around it (Solver::predict / correct,
+// src/solver.cpp:431-474).
 //
 // After the forward quantities of a step have been recomputed (prediction, tree, PreInteraction
 // with its Newton smoothing lengths), five launches run the backward pass in key order:
@@ -41,12 +42,14 @@ struct AdjArgs {
     const V4* a0;     // {v_0, v_1, v_2, h}
     const V4* a1;     // {rho, P, c, grad-h}
     const V4* a2;     // {Balsara, dubar, abar_0, abar_1}
-    const V4* a3;     // {abar_2, 0, 0, 0}
+    const V4* a3;     // {abar_2, u, 0, 0}
     const V4* w0;     // {w_rho, w_rhoh, Dbar, Rtbar_0}
-    const V4* w1;     // {Rtbar_1, Rtbar_2, 0, 0}
+    const V4* w1;     // {Rtbar_1, Rtbar_2, w_n, w_nh}
+    const V4* w2;     // {w_Y, w_Yh, 0, 0}
     double* buf;
     int n;
     T alpha;
+    T gamma;
 };
 
 // Walk and staging of the pair set of a target group; fills the per-target candidate masks and
@@ -94,7 +97,7 @@ __device__ int adj_stage(unsigned char* smem, const AdjArgs<T>& a, GroupMisc* gm
     return nw;
 }
 
-template <int D, typename T>
+template <int D, typename T, int TYPE>
 __device__ __forceinline__ sphadj::FluidSide<T> adj_side(const AdjArgs<T>& a, int j, T m, T h)
 {
     using V4 = typename Vec4<T>::type;
@@ -104,13 +107,39 @@ __device__ __forceinline__ sphadj::FluidSide<T> adj_side(const AdjArgs<T>& a, in
     s.rho = q1.x; s.P = q1.y; s.c = q1.z; s.g = q1.w;
     s.B = q2.x; s.dubar = q2.y;
     s.abar[0] = q2.z; s.abar[1] = q2.w; s.abar[2] = T(0);
-    if (D == 3) s.abar[2] = a.a3[j].x;
+    s.u = T(0);
+    if (D == 3 || TYPE == 1) {
+        const V4 q3 = a.a3[j];
+        if (D == 3) s.abar[2] = q3.x;
+        s.u = q3.y;
+    }
     s.h = h;
     s.m = m;
     return s;
 }
 
-template <int D, typename T, int K>
+template <int D, typename T, int TYPE>
+__device__ __forceinline__ sphadj::PreWeights<T> adj_weights(const AdjArgs<T>& a, int j)
+{
+    using V4 = typename Vec4<T>::type;
+    sphadj::PreWeights<T> w;
+    const V4 p0 = a.w0[j];
+    w.w_rho = p0.x; w.w_rhoh = p0.y; w.Dbar = p0.z;
+    w.Rtbar[0] = p0.w; w.Rtbar[1] = T(0); w.Rtbar[2] = T(0);
+    w.w_n = w.w_nh = w.w_Y = w.w_Yh = T(0);
+    if (D == 3 || TYPE == 1) {
+        const V4 p1 = a.w1[j];
+        w.Rtbar[1] = p1.x; w.Rtbar[2] = p1.y;
+        w.w_n = p1.z; w.w_nh = p1.w;
+    }
+    if (TYPE == 1) {
+        const V4 p2 = a.w2[j];
+        w.w_Y = p2.x; w.w_Yh = p2.y;
+    }
+    return w;
+}
+
+template <int D, typename T, int K, int TYPE>
 __global__ void __launch_bounds__(256) adj_pass1_kernel(AdjArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -138,12 +167,14 @@ __global__ void __launch_bounds__(256) adj_pass1_kernel(AdjArgs<T> a)
 
         const T h_i = (T)hi;
         const T m_i = (T)a.st.f[F_MASS][i];
-        const sphadj::FluidSide<T> si = adj_side<D, T>(a, i, m_i, h_i);
+        const sphadj::FluidSide<T> si = adj_side<D, T, TYPE>(a, i, m_i, h_i);
         const T s_i = K == 0 ? T(0.5) * h_i : h_i;
         const T sinv_i = T(1) / s_i, hinv_i = T(1) / h_i;
         Sum<T> rho_h, rho_hh, dv, dv_h, rt[3], rt_h[3];
         Sum<T> xb[D], vb[D], rhob, pb, gb_, hb, cb, bb, ab;
+        Sum<T> nd, nd_h, nd_hh, y_h, y_hh, ub;   // pressure-energy form
         rho_h.zero(); rho_hh.zero(); dv.zero(); dv_h.zero();
+        nd.zero(); nd_h.zero(); nd_hh.zero(); y_h.zero(); y_hh.zero(); ub.zero();
 #pragma unroll
         for (int k = 0; k < 3; ++k) { rt[k].zero(); rt_h[k].zero(); }
 #pragma unroll
@@ -158,7 +189,7 @@ __global__ void __launch_bounds__(256) adj_pass1_kernel(AdjArgs<T> a)
             const int j = tile.idx[s];
             const T h_j = tile.aux[s];
             const T m_j = tile.pm[s].w;
-            const sphadj::FluidSide<T> sj = adj_side<D, T>(a, j, m_j, h_j);
+            const sphadj::FluidSide<T> sj = adj_side<D, T, TYPE>(a, j, m_j, h_j);
             T vij[3] = {T(0), T(0), T(0)};
 #pragma unroll
             for (int k = 0; k < D; ++k) vij[k] = si.v[k] - sj.v[k];
@@ -170,13 +201,21 @@ __global__ void __launch_bounds__(256) adj_pass1_kernel(AdjArgs<T> a)
             if (r2 == T(0)) {
                 // the particle itself (or one at the same position): only the density-type sums;
                 // FluidForce skips r == 0
-                sphadj::pre_sums_add<D, K, T>(ps, rv, vij, m_j, h_i);
+                sphadj::pre_sums_self<D, K, T, TYPE>(ps, m_j, sj.u, h_i);
             } else {
-                sphadj::pass1_pair<D, K, T>(rv, vij, r2, si, sj, s_i, sinv_i, hinv_i, T(1) / h_j, a.alpha,
-                                            ps, mine, alpha_bar);
+                sphadj::pass1_pair<D, K, T, TYPE>(rv, vij, r2, si, sj, s_i, sinv_i, hinv_i, T(1) / h_j, a.alpha,
+                                                  a.gamma, ps, mine, alpha_bar);
             }
             rho_h.add(ps.rho_h);
-            rho_hh.add(ps.rho_hh);
+            if (TYPE == 0) {
+                rho_hh.add(ps.rho_hh);
+            } else {
+                nd.add(ps.n);
+                nd_h.add(ps.n_h);
+                nd_hh.add(ps.n_hh);
+                y_h.add(ps.Y_h);
+                y_hh.add(ps.Y_hh);
+            }
             dv.add(ps.Dv);
             dv_h.add(ps.Dv_h);
 #pragma unroll
@@ -191,6 +230,7 @@ __global__ void __launch_bounds__(256) adj_pass1_kernel(AdjArgs<T> a)
             cb.add(mine.c);
             bb.add(mine.B);
             ab.add(alpha_bar);
+            if (TYPE == 1) ub.add(mine.u);
         }
         if (active) {
             double* B = a.buf;
@@ -215,11 +255,19 @@ __global__ void __launch_bounds__(256) adj_pass1_kernel(AdjArgs<T> a)
             B[AL_C * n + i] = (double)cb.get();
             B[AL_B * n + i] = (double)bb.get();
             B[AL_ALPHA * n + i] = (double)ab.get();
+            if (TYPE == 1) {
+                B[AS_N * n + i] = (double)nd.get();
+                B[AS_NH * n + i] = (double)nd_h.get();
+                B[AS_NHH * n + i] = (double)nd_hh.get();
+                B[AS_YH * n + i] = (double)y_h.get();
+                B[AS_YHH * n + i] = (double)y_hh.get();
+                B[AL_U * n + i] = (double)ub.get();
+            }
         }
     }
 }
 
-template <int D, typename T, int K>
+template <int D, typename T, int K, int TYPE>
 __global__ void __launch_bounds__(256) adj_pass2_kernel(AdjArgs<T> a)
 {
     using V4 = typename Vec4<T>::type;
@@ -251,16 +299,12 @@ __global__ void __launch_bounds__(256) adj_pass2_kernel(AdjArgs<T> a)
         const T sinv_i = T(1) / s_i, hinv_i = T(1) / h_i;
         const V4 q0 = a.a0[i];
         const T v_i[3] = {q0.x, q0.y, q0.z};
-        sphadj::PreWeights<T> wi;
-        {
-            const V4 p0 = a.w0[i];
-            wi.w_rho = p0.x; wi.w_rhoh = p0.y; wi.Dbar = p0.z;
-            wi.Rtbar[0] = p0.w; wi.Rtbar[1] = T(0); wi.Rtbar[2] = T(0);
-            if (D == 3) { const V4 p1 = a.w1[i]; wi.Rtbar[1] = p1.x; wi.Rtbar[2] = p1.y; }
-        }
-        Sum<T> xb[D], vb[D];
+        const T u_i = TYPE == 1 ? a.a3[i].y : T(0);
+        const sphadj::PreWeights<T> wi = adj_weights<D, T, TYPE>(a, i);
+        Sum<T> xb[D], vb[D], ub;
 #pragma unroll
         for (int k = 0; k < D; ++k) { xb[k].zero(); vb[k].zero(); }
+        ub.zero();
 
         MaskIter it(tile.mask, GT, t, nw);
         int s;
@@ -275,13 +319,7 @@ __global__ void __launch_bounds__(256) adj_pass2_kernel(AdjArgs<T> a)
             T vij[3] = {v_i[0] - p0.x, v_i[1] - p0.y, v_i[2] - p0.z};
             if (D < 3) vij[2] = T(0);
             if (D < 2) vij[1] = T(0);
-            sphadj::PreWeights<T> wj;
-            {
-                const V4 w = a.w0[j];
-                wj.w_rho = w.x; wj.w_rhoh = w.y; wj.Dbar = w.z;
-                wj.Rtbar[0] = w.w; wj.Rtbar[1] = T(0); wj.Rtbar[2] = T(0);
-                if (D == 3) { const V4 w1 = a.w1[j]; wj.Rtbar[1] = w1.x; wj.Rtbar[2] = w1.y; }
-            }
+            const sphadj::PreWeights<T> wj = adj_weights<D, T, TYPE>(a, j);
             T dx[3] = {T(0), T(0), T(0)}, dvv[3] = {T(0), T(0), T(0)};
             const T rinv = T(1) / sqrt(r2);
             const T r = r2 * rinv;
@@ -291,8 +329,17 @@ __global__ void __launch_bounds__(256) adj_pass2_kernel(AdjArgs<T> a)
             sphadj::KVals<T> ki, kj;
             sphadj::kvals<D, K, T, true>(r, rinv, s_i, sinv_i, hinv_i, ki);
             sphadj::kvals<D, K, T, true>(r, rinv, s_j, sinv_j, hinv_j, kj);
-            sphadj::pre_pair_gather_k<D, T>(rv, vij, rinv, m_j, ki, wi, dx, dvv);
-            sphadj::pre_pair_gather_k<D, T>(rv, vij, rinv, m_i, kj, wj, dx, dvv);
+            if (TYPE == 0) {
+                sphadj::pre_pair_gather_k<D, T>(rv, vij, rinv, m_j, ki, wi, dx, dvv);
+                sphadj::pre_pair_gather_k<D, T>(rv, vij, rinv, m_i, kj, wj, dx, dvv);
+            } else {
+                // i's sums hold j (its u adjoint is j's), j's sums hold i
+                T u_other = T(0), u_mine = T(0);
+                const T u_j = a.a3[j].y;
+                sphadj::pre_pair_gather_disph_k<D, T>(rv, vij, rinv, m_j, u_j, ki, wi, dx, dvv, u_other);
+                sphadj::pre_pair_gather_disph_k<D, T>(rv, vij, rinv, m_i, u_i, kj, wj, dx, dvv, u_mine);
+                ub.add(u_mine);
+            }
 #pragma unroll
             for (int k = 0; k < D; ++k) { xb[k].add(dx[k]); vb[k].add(dvv[k]); }
         }
@@ -302,6 +349,7 @@ __global__ void __launch_bounds__(256) adj_pass2_kernel(AdjArgs<T> a)
                 a.buf[(AG_X + k) * n + i] = k < D ? (double)xb[k < D ? k : 0].get() : 0.0;
                 a.buf[(AG_V + k) * n + i] = k < D ? (double)vb[k < D ? k : 0].get() : 0.0;
             }
+            a.buf[AG_U * n + i] = (double)ub.get();
         }
     }
 }
@@ -350,13 +398,15 @@ __global__ void adj_prep_kernel(State st, int n, AdjLayout lay, const double* ad
     v.w = (T)abar[1];
     a2[i] = v;
     v.x = (T)abar[2];
-    v.y = v.z = v.w = T(0);
+    v.y = (T)st.f[F_ENE][i];
+    v.z = v.w = T(0);
     a3[i] = v;
 }
 
-template <int D, typename T>
+template <int D, typename T, int K, int TYPE>
 __global__ void adj_local_kernel(State st, int n, double gamma, int balsara, const double* dens_bar, double* buf,
-                                 typename Vec4<T>::type* w0, typename Vec4<T>::type* w1)
+                                 typename Vec4<T>::type* w0, typename Vec4<T>::type* w1,
+                                 typename Vec4<T>::type* w2)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -372,9 +422,22 @@ __global__ void adj_local_kernel(State st, int n, double gamma, int balsara, con
     if (dens_bar) rhobar += dens_bar[st.id[i]];
     sphadj::PreWeights<double> W;
     double ub = 0.0;
-    sphadj::pre_local_backward<D, double>(st.f[F_DENS][i], st.f[F_SML][i], st.f[F_SOUND][i], st.f[F_ENE][i], gamma,
-                                          balsara != 0, ps, rhobar, buf[AL_P * N + i], buf[AL_G * N + i],
-                                          buf[AL_H * N + i], buf[AL_C * N + i], buf[AL_B * N + i], W, ub);
+    if (TYPE == 0) {
+        sphadj::pre_local_backward<D, double>(st.f[F_DENS][i], st.f[F_SML][i], st.f[F_SOUND][i], st.f[F_ENE][i],
+                                              gamma, balsara != 0, ps, rhobar, buf[AL_P * N + i], buf[AL_G * N + i],
+                                              buf[AL_H * N + i], buf[AL_C * N + i], buf[AL_B * N + i], W, ub);
+    } else {
+        ps.n = buf[AS_N * N + i];
+        ps.n_h = buf[AS_NH * N + i];
+        ps.n_hh = buf[AS_NHH * N + i];
+        ps.Y_h = buf[AS_YH * N + i];
+        ps.Y_hh = buf[AS_YHH * N + i];
+        ub = buf[AL_U * N + i];
+        sphadj::pre_local_backward_disph<D, K, double>(
+            st.f[F_DENS][i], st.f[F_SML][i], st.f[F_SOUND][i], st.f[F_ENE][i], st.f[F_PRES][i], st.f[F_MASS][i],
+            gamma, balsara != 0, ps, rhobar, buf[AL_P * N + i], buf[AL_G * N + i], buf[AL_H * N + i],
+            buf[AL_C * N + i], buf[AL_B * N + i], W, ub);
+    }
     buf[AU_LOC * N + i] = ub;
     typename Vec4<T>::type v;
     v.x = (T)W.w_rho;
@@ -384,8 +447,13 @@ __global__ void adj_local_kernel(State st, int n, double gamma, int balsara, con
     w0[i] = v;
     v.x = (T)W.Rtbar[1];
     v.y = (T)W.Rtbar[2];
-    v.z = v.w = T(0);
+    v.z = (T)W.w_n;
+    v.w = (T)W.w_nh;
     w1[i] = v;
+    v.x = (T)W.w_Y;
+    v.y = (T)W.w_Yh;
+    v.z = v.w = T(0);
+    w2[i] = v;
 }
 
 // Leapfrog backward and scatter to the caller's order.  Step: x' = x + vp dt, v' = v + a dt,
@@ -402,7 +470,7 @@ __global__ void adj_final_kernel(State st, int n, AdjLayout lay, double* adj, co
         const size_t q = (size_t)st.id[i];
         const double dt = dt_run[st.run[i]];
         my_alpha += buf[AL_ALPHA * N + i];
-        const double u1b = buf[AU_LOC * N + i];
+        const double u1b = buf[AU_LOC * N + i] + buf[AG_U * N + i];
         if (initial) {
 #pragma unroll
             for (int k = 0; k < D; ++k) {
@@ -450,7 +518,7 @@ __global__ inline void adj_alpha_sum_kernel(const double* partials, int nparts, 
 
 // ---- launcher ----------------------------------------------------------------------------------
 
-template <int D, typename T, int K>
+template <int D, typename T, int K, int TYPE>
 void run_adjoint(Ctx& c, double* adj, const double* dens_bar, double* alpha_bar, bool initial)
 {
     using V4 = typename Vec4<T>::type;
@@ -458,7 +526,7 @@ void run_adjoint(Ctx& c, double* adj, const double* dens_bar, double* alpha_bar,
     const int n = c.n;
     V4* mir = reinterpret_cast<V4*>(c.adj_mir);
     V4 *a0 = mir, *a1 = mir + n, *a2 = mir + 2 * (size_t)n, *a3 = mir + 3 * (size_t)n;
-    V4 *w0 = mir + 4 * (size_t)n, *w1 = mir + 5 * (size_t)n;
+    V4 *w0 = mir + 4 * (size_t)n, *w1 = mir + 5 * (size_t)n, *w2 = mir + 6 * (size_t)n;
     const AdjLayout lay = adj_layout(n, D);
     adj_prep_kernel<D, T><<<ceil_div(n, 256), 256, 0, s>>>(c.st, n, lay, adj, c.d_dt, initial ? 1 : 0, a0, a1, a2, a3);
 
@@ -468,20 +536,23 @@ void run_adjoint(Ctx& c, double* adj, const double* dens_bar, double* alpha_bar,
     a.pb = c.pb;
     a.xrel = (const V4*)c.mir[6];
     a.hmir = (const T*)c.mir[7];
-    a.a0 = a0; a.a1 = a1; a.a2 = a2; a.a3 = a3; a.w0 = w0; a.w1 = w1;
+    a.a0 = a0; a.a1 = a1; a.a2 = a2; a.a3 = a3; a.w0 = w0; a.w1 = w1; a.w2 = w2;
     a.buf = c.adj_buf;
     a.n = n;
     a.alpha = (T)c.p.av_alpha;
+    a.gamma = (T)c.p.gamma;
     const int tcap = c.tile_cap ? c.tile_cap : (D == 1 ? 128 : D == 2 ? 384 : 1024);
     auto launcher = [](const void* k, int grid, int block, size_t smem, cudaStream_t st, AdjArgs<T>& args) {
         reinterpret_cast<void (*)(AdjArgs<T>)>(const_cast<void*>(k))<<<grid, block, smem, st>>>(args);
     };
     reset_work_counters(c);
-    launch_pair_passes<AdjArgs<T>>(c, (const void*)adj_pass1_kernel<D, T, K>, a, tcap, sizeof(V4), sizeof(T), launcher);
-    adj_local_kernel<D, T><<<ceil_div(n, 256), 256, 0, s>>>(c.st, n, c.p.gamma, c.p.use_balsara && D > 1, dens_bar,
-                                                           c.adj_buf, w0, w1);
+    launch_pair_passes<AdjArgs<T>>(c, (const void*)adj_pass1_kernel<D, T, K, TYPE>, a, tcap, sizeof(V4), sizeof(T),
+                                   launcher);
+    adj_local_kernel<D, T, K, TYPE><<<ceil_div(n, 256), 256, 0, s>>>(c.st, n, c.p.gamma, c.p.use_balsara && D > 1,
+                                                                    dens_bar, c.adj_buf, w0, w1, w2);
     reset_work_counters(c);
-    launch_pair_passes<AdjArgs<T>>(c, (const void*)adj_pass2_kernel<D, T, K>, a, tcap, sizeof(V4), sizeof(T), launcher);
+    launch_pair_passes<AdjArgs<T>>(c, (const void*)adj_pass2_kernel<D, T, K, TYPE>, a, tcap, sizeof(V4), sizeof(T),
+                                   launcher);
     const int grid = std::min(ADJ_PARTIALS, ceil_div(n, 256));
     adj_final_kernel<D><<<grid, 256, 0, s>>>(c.st, n, lay, adj, c.d_dt, initial ? 1 : 0, c.adj_buf, c.adj_partials);
     adj_alpha_sum_kernel<<<1, 1024, 0, s>>>(c.adj_partials, grid, alpha_bar);
@@ -490,13 +561,17 @@ void run_adjoint(Ctx& c, double* adj, const double* dens_bar, double* alpha_bar,
 template <int D>
 void adjoint_dispatch(Ctx& c, double* adj, const double* dens_bar, double* alpha_bar, bool initial)
 {
-    if (c.precision == SPHGPU_FP32_PAIR) {
-        if (c.p.kernel == 0) run_adjoint<D, float, 0>(c, adj, dens_bar, alpha_bar, initial);
-        else run_adjoint<D, float, 1>(c, adj, dens_bar, alpha_bar, initial);
+    const bool f32 = c.precision == SPHGPU_FP32_PAIR;
+    const int k = c.p.kernel, ty = c.p.sph_type;
+#define SPHGPU_ADJ(T, K, TY) run_adjoint<D, T, K, TY>(c, adj, dens_bar, alpha_bar, initial)
+    if (f32) {
+        if (k == 0) { if (ty == 0) SPHGPU_ADJ(float, 0, 0); else SPHGPU_ADJ(float, 0, 1); }
+        else { if (ty == 0) SPHGPU_ADJ(float, 1, 0); else SPHGPU_ADJ(float, 1, 1); }
     } else {
-        if (c.p.kernel == 0) run_adjoint<D, double, 0>(c, adj, dens_bar, alpha_bar, initial);
-        else run_adjoint<D, double, 1>(c, adj, dens_bar, alpha_bar, initial);
+        if (k == 0) { if (ty == 0) SPHGPU_ADJ(double, 0, 0); else SPHGPU_ADJ(double, 0, 1); }
+        else { if (ty == 0) SPHGPU_ADJ(double, 1, 0); else SPHGPU_ADJ(double, 1, 1); }
     }
+#undef SPHGPU_ADJ
 }
 
 }  // namespace sphgpu

@@ -975,7 +975,7 @@ namespace {
 int adjoint_ready(Ctx& c, const char* what)
 {
     std::string why;
-    if (c.p.sph_type != 0) why = "standard SPH (sph_type 0) only";
+    if (c.p.sph_type == 2) why = "standard SPH and the pressure-energy form (sph_type 0, 1) only";
     else if (c.p.use_gravity) why = "no gravity";
     else if (c.p.use_tdav) why = "no time-dependent viscosity";
     else if (c.p.use_ac) why = "no artificial conductivity";

@@ -156,9 +156,10 @@ enum AdjSlot : int {
     AS_RHOH = 0, AS_RHOHH = 1, AS_DV = 2, AS_DVH = 3, AS_RT = 4, AS_RTH = 7,
     AL_X = 10, AL_V = 13, AL_RHO = 16, AL_P = 17, AL_G = 18, AL_H = 19, AL_C = 20, AL_B = 21,
     AL_ALPHA = 22, AU_LOC = 23, AG_X = 24, AG_V = 27,
-    ADJ_SLOTS = 30
+    AS_N = 30, AS_NH = 31, AS_NHH = 32, AS_YH = 33, AS_YHH = 34, AL_U = 35, AG_U = 36,   // pressure-energy form
+    ADJ_SLOTS = 37
 };
-constexpr int ADJ_MIRRORS = 6;       // a0..a3, w0, w1 (one four-vector of the pair type each)
+constexpr int ADJ_MIRRORS = 7;       // a0..a3, w0..w2 (one four-vector of the pair type each)
 constexpr int ADJ_PARTIALS = 1024;   // block partials of the avAlpha adjoint
 
 template <int D>

@@ -25,6 +25,7 @@ struct Run {
     int K = 0;
     double m = 0, gamma = 5.0 / 3.0, nnb = 32, dt = 1e-3, alpha = 1.0;
     bool balsara = true;
+    int type = 0;   // 0 standard SPH, 1 pressure-energy form
 };
 
 struct Pre {
@@ -45,7 +46,9 @@ void pre_pass(const Run& R, const std::vector<double>& x, const std::vector<doub
     using KF = sphkd::KD<D, K, double>;
     const int n = R.n;
     o.h.assign(n, 0); o.rho.assign(n, 0); o.P.assign(n, 0); o.g.assign(n, 0); o.B.assign(n, 1); o.c.assign(n, 0);
-    const double b = R.m * R.nnb / M_PI;
+    // mass density (standard form) or number density (pressure-energy form) times h^D = b
+    const double mw = R.type == 1 ? 1.0 : R.m;
+    const double b = mw * R.nnb / M_PI;
     for (int i = 0; i < n; ++i) {
         o.c[i] = sqrt(R.gamma * (R.gamma - 1.0) * u[i]);
         double h = sqrt(R.nnb * R.m / M_PI);
@@ -55,8 +58,8 @@ void pre_pass(const Run& R, const std::vector<double>& x, const std::vector<doub
                 double r[D];
                 rvec(x, i, j, r);
                 const double rr = sqrt(r[0] * r[0] + r[1] * r[1]);
-                rho += R.m * KF::w(rr, h);
-                rh += R.m * KF::w_h(rr, h);
+                rho += mw * KF::w(rr, h);
+                rh += mw * KF::w_h(rr, h);
             }
             const double f = rho * h * h - b, df = rh * h * h + 2.0 * rho * h;
             const double dh = f / df;
@@ -75,18 +78,45 @@ void pre_pass(const Run& R, const std::vector<double>& x, const std::vector<doub
         }
         o.h[i] = h;
         o.rho[i] = rho;
-        o.P[i] = (R.gamma - 1.0) * rho * u[i];
-        o.g[i] = 1.0 / (1.0 + h * ps.rho_h / (D * rho));
+        if (R.type == 0) {
+            o.P[i] = (R.gamma - 1.0) * rho * u[i];
+            o.g[i] = 1.0 / (1.0 + h * ps.rho_h / (D * rho));
+            if (R.balsara) {
+                const double div = -ps.Dv / rho, rot = ps.Rt[0] / rho;
+                o.B[i] = fabs(div) / (fabs(div) + fabs(rot) + 1e-4 * o.c[i] / h);
+            }
+            continue;
+        }
+        // pressure-energy form (src/disph/d_pre_interaction.cpp:60-154)
+        double nd = 0, Ys = 0, Yh = 0, nh = 0, dv = 0, rt = 0;
+        for (int j = 0; j < n; ++j) {
+            double r[D];
+            rvec(x, i, j, r);
+            const double rr = sqrt(r[0] * r[0] + r[1] * r[1]);
+            const double w = KF::w(rr, h), wh = KF::w_h(rr, h);
+            nd += w;
+            nh += wh;
+            Ys += R.m * u[j] * w;
+            Yh += R.m * u[j] * wh;
+            if (j == i) continue;
+            const double F = KF::F(rr, h);
+            const double vx = v[i * D] - v[j * D], vy = v[i * D + 1] - v[j * D + 1];
+            dv += R.m * u[j] * (vx * r[0] + vy * r[1]) * F;
+            rt += R.m * u[j] * (vx * r[1] - vy * r[0]) * F;
+        }
+        o.P[i] = (R.gamma - 1.0) * Ys;
+        o.g[i] = h / (D * nd) * Yh / (1.0 + h / (D * nd) * nh);
         if (R.balsara) {
-            const double div = -ps.Dv / rho, rot = ps.Rt[0] / rho;
+            const double div = -dv / Ys, rot = rt / Ys;
             o.B[i] = fabs(div) / (fabs(div) + fabs(rot) + 1e-4 * o.c[i] / h);
         }
     }
 }
 
 template <int K>
-void fluid_pass(const Run& R, const std::vector<double>& x, const std::vector<double>& v, const Pre& p,
-                double alpha, std::vector<double>& a, std::vector<double>& du)
+void fluid_pass(const Run& R, const std::vector<double>& x, const std::vector<double>& v,
+                const std::vector<double>& u, const Pre& p, double alpha, std::vector<double>& a,
+                std::vector<double>& du)
 {
     using KF = sphkd::KD<D, K, double>;
     const int n = R.n;
@@ -109,9 +139,16 @@ void fluid_pass(const Run& R, const std::vector<double>& x, const std::vector<do
                 const double w = vr / rr;
                 Pi = -0.5 * 0.5 * (p.B[i] + p.B[j]) * alpha * (p.c[i] + p.c[j] - 3 * w) * w * 2.0 / (p.rho[i] + p.rho[j]);
             }
-            const double Q = -(Fi * Ai + Fj * Aj + 0.5 * Pi * (Fi + Fj));
+            double Xi = Ai, Yj = Aj;
+            if (R.type == 1) {
+                // src/disph/d_fluid_force.cpp:60-80
+                const double g2 = (R.gamma - 1.0) * (R.gamma - 1.0);
+                Xi = g2 * u[i] * u[j] * (1.0 - p.g[i] / (R.m * u[j])) / p.P[i];
+                Yj = g2 * u[i] * u[j] * (1.0 - p.g[j] / (R.m * u[i])) / p.P[j];
+            }
+            const double Q = -(Fi * Xi + Fj * Yj + 0.5 * Pi * (Fi + Fj));
             for (int k = 0; k < D; ++k) a[i * D + k] += R.m * r[k] * Q;
-            du[i] += R.m * vr * (Ai * Fi + 0.25 * Pi * (Fi + Fj));
+            du[i] += R.m * vr * (Xi * Fi + 0.25 * Pi * (Fi + Fj));
         }
     }
 }
@@ -124,7 +161,7 @@ template <int K>
 void initialize(const Run& R, St& s, Pre& p, double alpha)
 {
     pre_pass<K>(R, s.x, s.v, s.u, p);
-    fluid_pass<K>(R, s.x, s.v, p, alpha, s.a, s.du);
+    fluid_pass<K>(R, s.x, s.v, s.u, p, alpha, s.a, s.du);
 }
 
 template <int K>
@@ -143,7 +180,7 @@ void step(const Run& R, St& s, Pre& p, double alpha)
         s.u[i] += s.du[i] * dt;
     }
     pre_pass<K>(R, s.x, s.v, s.u, p);
-    fluid_pass<K>(R, s.x, s.v, p, alpha, s.a, s.du);
+    fluid_pass<K>(R, s.x, s.v, s.u, p, alpha, s.a, s.du);
     for (int i = 0; i < n * D; ++i) s.v[i] = vp[i] + s.a[i] * 0.5 * dt;
     for (int i = 0; i < n; ++i) s.u[i] = up[i] + s.du[i] * 0.5 * dt;
 }
@@ -177,6 +214,7 @@ double pre_fluid_backward(const Run& R, const std::vector<double>& x, const std:
         sphadj::FluidSide<double> s;
         for (int k = 0; k < 3; ++k) { s.v[k] = k < D ? v[i * D + k] : 0; s.abar[k] = k < D ? abar[i * D + k] : 0; }
         s.rho = p.rho[i]; s.P = p.P[i]; s.g = p.g[i]; s.B = p.B[i]; s.c = p.c[i]; s.h = p.h[i]; s.m = R.m;
+        s.u = u[i];
         s.dubar = dubar[i];
         return s;
     };
@@ -189,11 +227,21 @@ double pre_fluid_backward(const Run& R, const std::vector<double>& x, const std:
             double r[3] = {0, 0, 0}, vij[3] = {0, 0, 0};
             rvec(x, i, j, r);
             for (int k = 0; k < D; ++k) vij[k] = v[i * D + k] - v[j * D + k];
-            if (FUSED && j != i) {
+            if (FUSED && j == i) {
+                if (R.type == 0) sphadj::pre_sums_self<D, K, double, 0>(sums[i], R.m, u[i], p.h[i]);
+                else sphadj::pre_sums_self<D, K, double, 1>(sums[i], R.m, u[i], p.h[i]);
+                continue;
+            }
+            if (FUSED) {
                 const sphadj::FluidSide<double> sj = side(j);
                 const double s_i = K == 0 ? 0.5 * p.h[i] : p.h[i];
-                sphadj::pass1_pair<D, K, double>(r, vij, r[0] * r[0] + r[1] * r[1], si, sj, s_i, 1.0 / s_i,
-                                                 1.0 / p.h[i], 1.0 / p.h[j], alpha, sums[i], loc[i], alpha_bar);
+                const double r2 = r[0] * r[0] + r[1] * r[1];
+                if (R.type == 0)
+                    sphadj::pass1_pair<D, K, double, 0>(r, vij, r2, si, sj, s_i, 1.0 / s_i, 1.0 / p.h[i],
+                                                        1.0 / p.h[j], alpha, R.gamma, sums[i], loc[i], alpha_bar);
+                else
+                    sphadj::pass1_pair<D, K, double, 1>(r, vij, r2, si, sj, s_i, 1.0 / s_i, 1.0 / p.h[i],
+                                                        1.0 / p.h[j], alpha, R.gamma, sums[i], loc[i], alpha_bar);
                 continue;
             }
             sphadj::pre_sums_add<D, K, double>(sums[i], r, vij, R.m, p.h[i]);
@@ -210,10 +258,16 @@ double pre_fluid_backward(const Run& R, const std::vector<double>& x, const std:
     // local backward
     std::vector<sphadj::PreWeights<double>> W(n);
     for (int i = 0; i < n; ++i) {
-        double ub = 0;
-        sphadj::pre_local_backward<D, double>(p.rho[i], p.h[i], p.c[i], u[i], R.gamma, R.balsara, sums[i],
-                                              loc[i].rho + rhobar_ext[i], loc[i].P, loc[i].g, loc[i].h,
-                                              loc[i].c, loc[i].B, W[i], ub);
+        double ub = loc[i].u;
+        if (R.type == 0)
+            sphadj::pre_local_backward<D, double>(p.rho[i], p.h[i], p.c[i], u[i], R.gamma, R.balsara, sums[i],
+                                                  loc[i].rho + rhobar_ext[i], loc[i].P, loc[i].g, loc[i].h,
+                                                  loc[i].c, loc[i].B, W[i], ub);
+        else
+            sphadj::pre_local_backward_disph<D, K, double>(p.rho[i], p.h[i], p.c[i], u[i], p.P[i], R.m, R.gamma,
+                                                           R.balsara, sums[i], loc[i].rho + rhobar_ext[i],
+                                                           loc[i].P, loc[i].g, loc[i].h, loc[i].c, loc[i].B,
+                                                           W[i], ub);
         ubar[i] += ub;
         for (int k = 0; k < D; ++k) { xbar[i * D + k] += loc[i].x[k]; vbar[i * D + k] += loc[i].v[k]; }
     }
@@ -231,8 +285,14 @@ double pre_fluid_backward(const Run& R, const std::vector<double>& x, const std:
                 const double si_ = K == 0 ? 0.5 * p.h[i] : p.h[i], sj_ = K == 0 ? 0.5 * p.h[j] : p.h[j];
                 sphadj::kvals<D, K, double, true>(rr, rinv, si_, 1.0 / si_, 1.0 / p.h[i], ki);
                 sphadj::kvals<D, K, double, true>(rr, rinv, sj_, 1.0 / sj_, 1.0 / p.h[j], kj);
-                sphadj::pre_pair_gather_k<D, double>(r, vij, rinv, R.m, ki, W[i], xb, vb);
-                sphadj::pre_pair_gather_k<D, double>(r, vij, rinv, R.m, kj, W[j], xb, vb);
+                if (R.type == 0) {
+                    sphadj::pre_pair_gather_k<D, double>(r, vij, rinv, R.m, ki, W[i], xb, vb);
+                    sphadj::pre_pair_gather_k<D, double>(r, vij, rinv, R.m, kj, W[j], xb, vb);
+                } else {
+                    double u_unused = 0;
+                    sphadj::pre_pair_gather_disph_k<D, double>(r, vij, rinv, R.m, u[j], ki, W[i], xb, vb, u_unused);
+                    sphadj::pre_pair_gather_disph_k<D, double>(r, vij, rinv, R.m, u[i], kj, W[j], xb, vb, ubar[i]);
+                }
                 continue;
             }
             sphadj::pre_pair_gather<D, K, double>(r, vij, R.m, p.h[i], W[i], xb, vb);
@@ -306,9 +366,10 @@ void gradient(const Run& R, const St& s0, int steps, double alpha, std::vector<d
 }
 
 template <int K>
-void check(int side, int steps, double eps, int balsara, double vnoise, double* out)
+void check(int side, int steps, double eps, int balsara, double vnoise, int type, double* out)
 {
     Run R;
+    R.type = type;
     R.balsara = balsara != 0;
     R.K = K;
     R.n = side * side;
@@ -359,10 +420,11 @@ void check(int side, int steps, double eps, int balsara, double vnoise, double* 
 // One Pre + Fluid evaluation: L = ca . a + cdu . du + crho . rho, gradient in x, v, u along
 // random directions by the adjoint and by central differences.
 template <int K>
-void check_single(int side, double eps, int balsara, int which, double* out)
+void check_single(int side, double eps, int balsara, int which, int type, double* out)
 {
     Run R;
     R.K = K;
+    R.type = type;
     R.balsara = balsara != 0;
     R.n = side * side;
     R.m = 1.0 / R.n;
@@ -388,7 +450,7 @@ void check_single(int side, double eps, int balsara, int which, double* out)
         Pre p;
         std::vector<double> a, du;
         pre_pass<K>(R, t.x, t.v, t.u, p);
-        fluid_pass<K>(R, t.x, t.v, p, R.alpha, a, du);
+        fluid_pass<K>(R, t.x, t.v, t.u, p, R.alpha, a, du);
         double l = 0;
         for (int i = 0; i < R.n * D; ++i) l += ca[i] * a[i];
         for (int i = 0; i < R.n; ++i) l += cdu[i] * du[i] + crho[i] * p.rho[i];
@@ -401,7 +463,10 @@ void check_single(int side, double eps, int balsara, int which, double* out)
     {
         // the fused device forms against the two-call forms
         std::vector<double> xb2(R.n * D, 0), vb2(R.n * D, 0), ub2(R.n, 0);
-        const double ab2 = pre_fluid_backward<K, false>(R, s.x, s.v, s.u, p, R.alpha, ca, cdu, crho, xb2, vb2, ub2);
+        // the two-call forms exist for the standard form only
+        const double ab2 = R.type != 0 ? ab : pre_fluid_backward<K, false>(R, s.x, s.v, s.u, p, R.alpha, ca, cdu,
+                                                                           crho, xb2, vb2, ub2);
+        if (R.type != 0) { xb2 = xb; vb2 = vb; ub2 = ub; }
         double d = fabs(ab - ab2) / (fabs(ab2) + 1e-300), mx = 0, mv = 0, mu = 0;
         for (int i = 0; i < R.n * D; ++i) { mx = fmax(mx, fabs(xb2[i])); mv = fmax(mv, fabs(vb2[i])); }
         for (int i = 0; i < R.n; ++i) mu = fmax(mu, fabs(ub2[i]));
@@ -431,11 +496,12 @@ void check_single(int side, double eps, int balsara, int which, double* out)
 // Gradient of L = sum (rho_final - 1)^2 for given initial fields (n particles of mass 1/n in the
 // periodic unit box [-0.5, 0.5)^2, gamma 5/3): gv (n*2), gu (n), *galpha, and rho_final (n).
 template <int K>
-void gradient_of(int n, int steps, double dt, double alpha, double nnb, int balsara, const double* x,
+void gradient_of(int n, int steps, double dt, double alpha, double nnb, int balsara, int type, const double* x,
                  const double* v, const double* u, double* gv_out, double* gu_out, double* galpha,
                  double* rho_out)
 {
     Run R;
+    R.type = type;
     R.K = K;
     R.n = n;
     R.m = 1.0 / n;
@@ -460,24 +526,25 @@ void gradient_of(int n, int steps, double dt, double alpha, double nnb, int bals
 
 }  // namespace
 
-extern "C" void adj_gradient(int kernel, int n, int steps, double dt, double alpha, double nnb, int balsara,
-                             const double* x, const double* v, const double* u, double* gv, double* gu,
-                             double* galpha, double* rho)
+extern "C" void adj_gradient(int kernel, int type, int n, int steps, double dt, double alpha, double nnb,
+                             int balsara, const double* x, const double* v, const double* u, double* gv,
+                             double* gu, double* galpha, double* rho)
 {
-    if (kernel == 0) gradient_of<0>(n, steps, dt, alpha, nnb, balsara, x, v, u, gv, gu, galpha, rho);
-    else gradient_of<1>(n, steps, dt, alpha, nnb, balsara, x, v, u, gv, gu, galpha, rho);
+    if (kernel == 0) gradient_of<0>(n, steps, dt, alpha, nnb, balsara, type, x, v, u, gv, gu, galpha, rho);
+    else gradient_of<1>(n, steps, dt, alpha, nnb, balsara, type, x, v, u, gv, gu, galpha, rho);
 }
 
-extern "C" void adj_check_single(int kernel, int side, double eps, int balsara, int which, double* out)
+extern "C" void adj_check_single(int kernel, int type, int side, double eps, int balsara, int which, double* out)
 {
-    if (kernel == 0) check_single<0>(side, eps, balsara, which, out);
-    else check_single<1>(side, eps, balsara, which, out);
+    if (kernel == 0) check_single<0>(side, eps, balsara, which, type, out);
+    else check_single<1>(side, eps, balsara, which, type, out);
 }
 
 // out[7]: adjoint / finite-difference pairs for a velocity direction, an energy direction and
 // avAlpha, then the loss.  kernel 0 cubic spline, 1 Wendland C4.
-extern "C" void adj_check(int kernel, int side, int steps, double eps, int balsara, double vnoise, double* out)
+extern "C" void adj_check(int kernel, int type, int side, int steps, double eps, int balsara, double vnoise,
+                          double* out)
 {
-    if (kernel == 0) check<0>(side, steps, eps, balsara, vnoise, out);
-    else check<1>(side, steps, eps, balsara, vnoise, out);
+    if (kernel == 0) check<0>(side, steps, eps, balsara, vnoise, type, out);
+    else check<1>(side, steps, eps, balsara, vnoise, type, out);
 }

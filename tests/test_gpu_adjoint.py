@@ -1,6 +1,7 @@
 """The device adjoint (sphgpu_adjoint_step / sphgpu_adjoint_initialize behind
-sphcode_gb300.adjoint.SphRunFunction) on the Gresho-Chan vortex (ssph, cubic spline, periodic
-[-0.5, 0.5]^2, gamma 5/3), loss L = sum (rho_final - 1)^2.
+sphcode_gb300.adjoint.SphRunFunction) on the Gresho-Chan vortex (standard SPH and the
+pressure-energy form, cubic spline, periodic [-0.5, 0.5]^2, gamma 5/3), loss
+L = sum (rho_final - 1)^2.
 
 - against an independent host adjoint (tests/adjoint_check.cpp: all pairs, Newton to round-off)
   on a 16 x 16 lattice;
@@ -29,9 +30,10 @@ FP32_DIR_TOL = 2e-2       # directional derivative along a random direction
 FP32_ALPHA_TOL = 1e-3
 
 
-def gresho(n_side, noise=0.0, seed=3):
+def gresho(n_side, noise=0.0, seed=3, sph_type="ssph"):
     from sphcode_gb300 import ics
     p, f = ics.gresho(n_side)
+    p.sph_type = sph_type
     if noise:
         rng = np.random.default_rng(seed)
         f["vel"] = f["vel"] + noise * rng.standard_normal(f["vel"].shape)
@@ -63,17 +65,18 @@ def host_adjoint(tmp_path_factory):
                            os.path.join(HERE, "adjoint_check.cpp"), "-o", out])
     lib = ctypes.CDLL(out)
     P = ctypes.c_void_p
-    lib.adj_gradient.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
-                                 ctypes.c_double, ctypes.c_int, P, P, P, P, P, P, P]
+    lib.adj_gradient.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                 ctypes.c_double, ctypes.c_double, ctypes.c_int, P, P, P, P, P, P, P]
     return lib
 
 
+@pytest.mark.parametrize("sph_type", ["ssph", "disph"])
 @pytest.mark.parametrize("noise", [0.01, 0.05])
-def test_adjoint_matches_host(gpu_lib, host_adjoint, noise):
+def test_adjoint_matches_host(gpu_lib, host_adjoint, noise, sph_type):
     """Velocity noise keeps every pair off v_ij . r_ij = 0 (see the module docstring), where the
     two sides may legitimately take different branches on round-off."""
     from sphcode_gb300.adjoint import SphRun
-    p, f = gresho(16, noise)
+    p, f = gresho(16, noise, sph_type=sph_type)
     steps = 5
     run = SphRun(p, f, steps, precision="fp64", checkpoint_every=2)
     L, gv, gu, ga = gradients(run, f, p)
@@ -84,7 +87,8 @@ def test_adjoint_matches_host(gpu_lib, host_adjoint, noise):
     u = np.ascontiguousarray(f["ene"])
     hv, hu, hr = np.zeros(2 * n), np.zeros(n), np.zeros(n)
     ha = ctypes.c_double()
-    host_adjoint.adj_gradient(0, n, steps, run.dt, p.av_alpha, float(p.neighbor_number), 1,
+    host_adjoint.adj_gradient(0, 0 if sph_type == "ssph" else 1, n, steps, run.dt, p.av_alpha,
+                              float(p.neighbor_number), 1,
                               x.ctypes.data, v.ctypes.data, u.ctypes.data, hv.ctypes.data, hu.ctypes.data,
                               ctypes.addressof(ha), hr.ctypes.data)
     # the device smoothing lengths are the reference's Newton iterates (converged to a relative
@@ -100,10 +104,10 @@ def test_adjoint_matches_host(gpu_lib, host_adjoint, noise):
     assert errs["alpha_bar"] <= 1e-5 or abs(ga - ha.value) <= 1e-9 * np.abs(hv).max(), errs
 
 
-@pytest.fixture(scope="module")
-def fd_case(gpu_lib):
+@pytest.fixture(scope="module", params=["ssph", "disph"])
+def fd_case(gpu_lib, request):
     from sphcode_gb300.adjoint import SphRun
-    p, f = gresho(64, 0.05)
+    p, f = gresho(64, 0.05, sph_type=request.param)
     run = SphRun(p, f, 30, precision="fp64", checkpoint_every=20)
     res = gradients(run, f, p)
     yield p, f, run, res
