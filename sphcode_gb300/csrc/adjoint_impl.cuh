@@ -83,14 +83,18 @@ __device__ int adj_stage(unsigned char* smem, const AdjArgs<T>& a, GroupMisc* gm
     const int t = threadIdx.x, GT = blockDim.x;
     for (int w = 0; w < nw; ++w) {
         unsigned bits = 0;
-        const int smax = min(32, ntile - w * 32);
-        for (int b = 0; b < smax; ++b) {
-            const int s = w * 32 + b;
-            T r[D];
-            const T r2 = tile_r2<D, T>(xo, tile.pm[s], r);
-            const T hj = tile.aux[s];
-            const T H = (h_i > hj ? h_i : hj) * grow;
-            if (r2 < H * H) bits |= 1u << b;
+        const T wmax = D == 3 ? tile.wbox[2 * w + 1].w : h_i;   // largest h_j of the word
+        const T Hw = (h_i > wmax ? h_i : wmax) * grow;
+        if (word_box_r2<D, T>(xo, tile, w) < Hw * Hw) {
+            const int smax = min(32, ntile - w * 32);
+            for (int b = 0; b < smax; ++b) {
+                const int s = w * 32 + b;
+                T r[D];
+                const T r2 = tile_r2<D, T>(xo, tile.pm[s], r);
+                const T hj = tile.aux[s];
+                const T H = (h_i > hj ? h_i : hj) * grow;
+                if (r2 < H * H) bits |= 1u << b;
+            }
         }
         tile.mask[w * GT + t] = active ? bits : 0u;
     }

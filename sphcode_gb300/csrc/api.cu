@@ -519,7 +519,7 @@ int autotune_impl(Ctx& c)
         if (32 * gw > 32 * 8) break;
         c.gw_pre = gw;
         if (build_groups(c) != SPHGPU_OK) break;
-        launch_make_tree(c, true);   // same positions: an identity reorder, new group split
+        launch_make_tree(c, true, true);   // same positions: an identity reorder, new group split
         float bp = 1e30f, bf = 1e30f;
         int tp = base_pre, tf = base_fluid;
         for (double f : fr) {
@@ -549,7 +549,7 @@ int autotune_impl(Ctx& c)
     c.tile_cap = best_tf;
     int rc = build_groups(c);
     if (rc != SPHGPU_OK) return rc;
-    launch_make_tree(c, true);
+    launch_make_tree(c, true, true);
     pre_inputs(c, 1);
     c.tuned = true;
     return SPHGPU_OK;
@@ -610,6 +610,22 @@ int kernel_occupancy(const void* kern, int threads, size_t smem)
 }
 
 void reset_work_counters(Ctx& c) { cudaMemsetAsync(c.d_work, 0, sizeof(int) * 48, c.stream); }
+
+// After a capped tree build left a node unsplit that the full build would split, the following
+// builds split four more levels (the step graph is captured again).
+void check_tree_cap(Ctx& c)
+{
+    if (c.p.use_gravity || c.depth_cap <= 0) return;
+    int t = 0;
+    cudaMemcpyAsync(&t, c.d_work + TREE_TRUNC_SLOT, sizeof(int), cudaMemcpyDeviceToHost, c.stream);
+    cudaStreamSynchronize(c.stream);
+    if (!t) return;
+    cudaMemsetAsync(c.d_work + TREE_TRUNC_SLOT, 0, sizeof(int), c.stream);
+    cudaStreamSynchronize(c.stream);
+    c.depth_cap = std::min(c.key_levels, c.tree_levels + 4);
+    c.graph_valid = false;
+    c.warm = false;
+}
 
 void set_global_error(const std::string& text)
 {
@@ -818,7 +834,9 @@ int sphgpu_make_tree(sphgpu_ctx* h)
 {
     CTX_OR_FAIL(h);
     sphgpu::launch_make_tree(c, true);
-    return sphgpu::finish(c, "make_tree");
+    const int rc = sphgpu::finish(c, "make_tree");
+    if (rc == SPHGPU_OK) sphgpu::check_tree_cap(c);
+    return rc;
 }
 
 int sphgpu_pre_interaction(sphgpu_ctx* h)
@@ -874,7 +892,8 @@ int sphgpu_initialize(sphgpu_ctx* h)
 {
     CTX_OR_FAIL(h);
     sphgpu::launch_init_fields(c);
-    sphgpu::launch_make_tree(c, true);
+    cudaMemsetAsync(c.d_work + sphgpu::TREE_TRUNC_SLOT, 0, sizeof(int), c.stream);
+    sphgpu::launch_make_tree(c, true, true);
     c.first_pre = true;
     if (c.autotune && !c.tuned) {
         sphgpu::launch_pre(c, true);   // initial smoothing once; the tuner's trials start after it
@@ -886,7 +905,10 @@ int sphgpu_initialize(sphgpu_ctx* h)
     sphgpu::launch_fluid(c);
     if (c.p.use_gravity) sphgpu::launch_gravity(c);
     c.graph_valid = false;
-    return sphgpu::finish(c, "initialize");
+    const int rc = sphgpu::finish(c, "initialize");
+    // later builds split two levels deeper than the initial tree (without gravity)
+    if (rc == SPHGPU_OK && !c.p.use_gravity) c.depth_cap = std::min(c.key_levels, sphgpu::tree_depth(c) + 1);
+    return rc;
 }
 
 int sphgpu_step(sphgpu_ctx* h, int n_steps)
@@ -947,7 +969,9 @@ int sphgpu_step(sphgpu_ctx* h, int n_steps)
         if (e != cudaSuccess) return sphgpu::cuda_status(c, e, "step launch");
     }
     sphgpu::nonfinite_kernel<<<sphgpu::ceil_div(c.n, 256), 256, 0, c.stream>>>(c.st, c.n, c.dim, c.d_err);
-    return sphgpu::finish(c, "step");
+    const int rc = sphgpu::finish(c, "step");
+    if (rc == SPHGPU_OK) sphgpu::check_tree_cap(c);
+    return rc;
 }
 
 int sphgpu_get_state(sphgpu_ctx* h, double* state)
@@ -1014,7 +1038,9 @@ int sphgpu_adjoint_step(sphgpu_ctx* h, double* adj, const double* dens_bar, doub
     sphgpu::launch_make_tree(c, false);
     sphgpu::run_pre_stage(c);
     sphgpu::launch_adjoint(c, adj, dens_bar, alpha_bar, false);
-    return sphgpu::finish(c, "adjoint_step");
+    rc = sphgpu::finish(c, "adjoint_step");
+    if (rc == SPHGPU_OK) sphgpu::check_tree_cap(c);
+    return rc;
 }
 
 int sphgpu_adjoint_initialize(sphgpu_ctx* h, double* adj, const double* dens_bar, double* alpha_bar)
@@ -1025,7 +1051,7 @@ int sphgpu_adjoint_initialize(sphgpu_ctx* h, double* adj, const double* dens_bar
     if (rc != SPHGPU_OK) return rc;
     // forward quantities of Solver::initialize: start-up fields, tree, first PreInteraction
     sphgpu::launch_init_fields(c);
-    sphgpu::launch_make_tree(c, true);
+    sphgpu::launch_make_tree(c, true, true);
     c.first_pre = true;
     sphgpu::run_pre_stage(c);
     sphgpu::launch_adjoint(c, adj, dens_bar, alpha_bar, true);
@@ -1224,7 +1250,9 @@ int sphgpu_bench_steps(sphgpu_ctx* h, int n_steps, int flush_l2, double* ms)
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     *ms = total;
-    return sphgpu::finish(c, "bench");
+    const int rc = sphgpu::finish(c, "bench");
+    if (rc == SPHGPU_OK) sphgpu::check_tree_cap(c);
+    return rc;
 }
 
 int sphgpu_stage_times(sphgpu_ctx* h, double* out)

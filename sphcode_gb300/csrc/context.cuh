@@ -120,6 +120,12 @@ struct Ctx {
     int tile_cap_pre = 0;           // per-stage source tile capacities (0 = automatic)
     int pass2_scale = 2;            // tile of the second pair pass, in multiples of the first
     bool fixed_dt = false;          // steps keep the dt set by the caller (no TimeStep)
+    // octree levels split in a step's tree build (0: all key levels).  Without gravity the tree
+    // only serves the neighbour walks, whose sets do not depend on where the splitting stops;
+    // sphgpu_initialize sets it two levels below the initial tree's depth, and a build that had
+    // to stop splitting early raises it (TREE_TRUNC_SLOT).
+    int depth_cap = 0;
+    int tree_levels = 0;            // split levels of the last build
 
     // adjoint scratch (allocated on the first adjoint call)
     double* adj_buf = nullptr;      // ADJ_SLOTS x n doubles
@@ -132,7 +138,8 @@ struct Ctx {
 // ---- tree.cu
 int tree_alloc(Ctx& c);
 void tree_free(Ctx& c);
-void launch_make_tree(Ctx& c, bool reorder_all);
+void launch_make_tree(Ctx& c, bool reorder_all, bool full_depth = false);
+int tree_depth(Ctx& c);            // deepest level holding nodes in the last build (synchronises)
 void launch_set_kernel_size(Ctx& c);
 void launch_node_moments(Ctx& c);
 TreeView tree_view(const Ctx& c);
@@ -178,6 +185,7 @@ inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 int max_optin_smem(const Ctx& c);
 int kernel_occupancy(const void* kern, int threads, size_t smem);
 void reset_work_counters(Ctx& c);
+void check_tree_cap(Ctx& c);
 void set_global_error(const std::string& text);   // text of sphgpu_last_error(NULL)
 
 // Passes of a CTA-per-group pair kernel.  Pass 1 runs every group with the tuned capacities at
@@ -190,6 +198,7 @@ void set_global_error(const std::string& text);   // text of sphgpu_last_error(N
 // `L` (SmemLayout) and `work` (GroupWork).
 constexpr int MAX_PAIR_PASSES = 14;
 constexpr int FAIL_INFO_SLOT = 48;   // d_work[48..52]: the last failing range
+constexpr int TREE_TRUNC_SLOT = 60;  // d_work[60]: a capped tree build left a splittable node
 template <class Args>
 void launch_pair_passes(Ctx& c, const void* kern, Args& a, int tcap, int elt4, int eltT,
                         void (*launch)(const void*, int, int, size_t, cudaStream_t, Args&));
@@ -199,7 +208,7 @@ void launch_pair_passes(Ctx& c, const void* kern, Args& a, int tcap, int elt4, i
 inline int big_tile_cap(const Ctx& c, int gt, int elt4, int eltT, int stack_cap, int leaf_cap)
 {
     const SmemLayout L0 = make_layout(gt, 0, elt4, eltT, stack_cap, leaf_cap);
-    const size_t per = (size_t)elt4 + (size_t)eltT + sizeof(int) + (size_t)gt / 8;
+    const size_t per = (size_t)elt4 + (size_t)eltT + sizeof(int) + (size_t)gt / 8 + (size_t)elt4 / 16;
     size_t cap = ((size_t)max_optin_smem(c) - L0.total - 64) / per;
     cap = cap / 32 * 32;
     if (cap > 16384) cap = 16384;

@@ -129,14 +129,19 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
         // ---- pair candidates: r^2 < max(h_i, h_j)^2 (1 + delta), j != i ----
         for (int w = 0; w < nw; ++w) {
             unsigned bits = 0;
-            const int smax = min(32, ntile - w * 32);
-            for (int b = 0; b < smax; ++b) {
-                const int s = w * 32 + b;
-                T r[D];
-                const T r2 = tile_r2<D, T>(xo, tile.pm[s], r);
-                const T hinv_j = tile.aux[s];
-                const T Hinv = hinv_i < hinv_j ? hinv_i : hinv_j;   // 1 / max(h_i, h_j)
-                if (r2 * (Hinv * Hinv) < dhi) bits |= 1u << b;
+            // the word's smallest 1/h_j bounds every source's 1/max(h_i, h_j) from below
+            const T wmin = D == 3 ? tile.wbox[2 * w].w : hinv_i;
+            const T Hw = hinv_i < wmin ? hinv_i : wmin;
+            if (word_box_r2<D, T>(xo, tile, w) * (Hw * Hw) < dhi) {
+                const int smax = min(32, ntile - w * 32);
+                for (int b = 0; b < smax; ++b) {
+                    const int s = w * 32 + b;
+                    T r[D];
+                    const T r2 = tile_r2<D, T>(xo, tile.pm[s], r);
+                    const T hinv_j = tile.aux[s];
+                    const T Hinv = hinv_i < hinv_j ? hinv_i : hinv_j;   // 1 / max(h_i, h_j)
+                    if (r2 * (Hinv * Hinv) < dhi) bits |= 1u << b;
+                }
             }
             tile.mask[w * GT + t] = active ? bits : 0u;
         }

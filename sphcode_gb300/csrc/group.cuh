@@ -62,7 +62,7 @@ struct SmemLayout {
     int stack_cap;  // walk stack entries
     int leaf_cap;   // leaf ranges
     size_t off_stack, off_leaves, off_loff, off_lpre, off_misc, off_tpos, off_taux, off_tidx,
-        off_mask, total;
+        off_mask, off_wbox, total;
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -101,6 +101,7 @@ __host__ __device__ inline SmemLayout make_layout(int gt, int tcap, int elt4, in
     L.off_taux = o; o = align16(o + (size_t)eltT * tcap);
     L.off_tidx = o; o = align16(o + sizeof(int) * tcap);
     L.off_mask = o; o = align16(o + sizeof(unsigned) * (size_t)(tcap / 32) * gt);
+    L.off_wbox = o; o = align16(o + (size_t)elt4 * 2 * (size_t)(tcap / 32));
     L.total = o;
     return L;
 }
@@ -111,6 +112,9 @@ struct Tile {
     T* aux;                       // one auxiliary value per source (stage-defined)
     int* idx;                     // key-order slot of each staged source
     unsigned* mask;               // word w of target t at mask[w * gt + t]
+    // bounding box of the offsets of the 32 sources of mask word w: wbox[2 w] = {min x, min y,
+    // min z, min aux}, wbox[2 w + 1] = {max x, max y, max z, max aux}
+    typename Vec4<T>::type* wbox;
     int gt;
 };
 
@@ -122,8 +126,33 @@ __device__ __forceinline__ Tile<T> tile_of(unsigned char* smem, const SmemLayout
     v.aux = reinterpret_cast<T*>(smem + L.off_taux);
     v.idx = reinterpret_cast<int*>(smem + L.off_tidx);
     v.mask = reinterpret_cast<unsigned*>(smem + L.off_mask);
+    v.wbox = reinterpret_cast<typename Vec4<T>::type*>(smem + L.off_wbox);
     v.gt = L.gt;
     return v;
+}
+
+// Squared distance in T from a target offset to the box of mask word w (3D tiles; 0 otherwise,
+// i.e. no word is skipped).  It is formed with the
+// operations of tile_r2 on per-axis distances that are never larger than the word's sources'
+// (rounding is monotonic), so it never exceeds tile_r2 of any source of the word: a word whose
+// box distance already fails a target's test holds no source that passes it.
+template <int D, typename T>
+__device__ __forceinline__ T word_box_r2(const T* xo, const Tile<T>& tile, int w)
+{
+    if (D != 3) return T(0);
+    const typename Vec4<T>::type lo = tile.wbox[2 * w], hi = tile.wbox[2 * w + 1];
+    const T l[3] = {lo.x, lo.y, lo.z}, h[3] = {hi.x, hi.y, hi.z};
+    T d[3];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        const T a = l[k] - xo[k], b = xo[k] - h[k];
+        const T m = a > b ? a : b;
+        d[k] = m > T(0) ? m : T(0);
+    }
+    T r2 = d[0] * d[0];
+    if (D > 1) r2 = fma(d[D > 1 ? 1 : 0], d[D > 1 ? 1 : 0], r2);
+    if (D > 2) r2 = fma(d[D > 2 ? 2 : 0], d[D > 2 ? 2 : 0], r2);
+    return r2;
 }
 
 // The set bits of one target's candidate mask, visited across all words in one loop, so that a
@@ -494,8 +523,44 @@ __device__ int stage_sources(unsigned char* smem, const SmemLayout& L, GroupMisc
         base += tot;
     }
     __syncthreads();
-    if (base > L.tcap && threadIdx.x == 0) gm->overflow = 1000000 + base;   // diagnostic: sources needed
-    return base > L.tcap ? -1 : base;
+    if (base > L.tcap) {
+        if (threadIdx.x == 0) gm->overflow = 1000000 + base;   // diagnostic: sources needed
+        return -1;
+    }
+    // bounding boxes of the mask words (warp w reduces words w, w + nw, ...).  Built in 3D only:
+    // a warp skips a word only when none of its 32 targets needs it, which the 2D tiles rarely
+    // allow, while in 3D the tile volume outside the targets' spheres is large.
+    if (D != 3) return base;
+    const T big = sizeof(T) == 4 ? T(3.0e38f) : T(1.0e300);
+    for (int wd = w; wd < ((base + 31) >> 5); wd += nw) {
+        const int sidx = wd * 32 + lane;
+        V4 lo, hi;
+        if (sidx < base) {
+            lo = tile.pm[sidx];
+            lo.w = tile.aux[sidx];
+            hi = lo;
+        } else {
+            lo.x = lo.y = lo.z = lo.w = big;
+            hi.x = hi.y = hi.z = hi.w = -big;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            lo.x = fmin(lo.x, __shfl_xor_sync(FULL, lo.x, o));
+            lo.y = fmin(lo.y, __shfl_xor_sync(FULL, lo.y, o));
+            lo.z = fmin(lo.z, __shfl_xor_sync(FULL, lo.z, o));
+            lo.w = fmin(lo.w, __shfl_xor_sync(FULL, lo.w, o));
+            hi.x = fmax(hi.x, __shfl_xor_sync(FULL, hi.x, o));
+            hi.y = fmax(hi.y, __shfl_xor_sync(FULL, hi.y, o));
+            hi.z = fmax(hi.z, __shfl_xor_sync(FULL, hi.z, o));
+            hi.w = fmax(hi.w, __shfl_xor_sync(FULL, hi.w, o));
+        }
+        if (lane == 0) {
+            tile.wbox[2 * wd] = lo;
+            tile.wbox[2 * wd + 1] = hi;
+        }
+    }
+    __syncthreads();
+    return base;
 }
 
 // ---- exact FP64 decisions for the guard band ---------------------------------------------------

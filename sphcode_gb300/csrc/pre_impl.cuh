@@ -104,14 +104,16 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
             const T lo_t = to_T_down<T>(hs2 - band), hi_t = to_T_up<T>(hs2 + band);
             for (int w = 0; w < nw; ++w) {
                 unsigned bits = 0;
-                const int smax = min(32, ntile - w * 32);
-                for (int b = 0; b < smax; ++b) {
-                    const int s = w * 32 + b;
-                    T r[D];
-                    const T r2 = tile_r2<D, T>(xo, tile.pm[s], r);
-                    bool in = r2 < lo_t;
-                    if (!in && r2 <= hi_t) in = exact_r2<D>(st, xi, tile.idx[s], a.pb) < hs2;
-                    if (in) bits |= 1u << b;
+                if (word_box_r2<D, T>(xo, tile, w) <= hi_t) {   // else no source of the word is in
+                    const int smax = min(32, ntile - w * 32);
+                    for (int b = 0; b < smax; ++b) {
+                        const int s = w * 32 + b;
+                        T r[D];
+                        const T r2 = tile_r2<D, T>(xo, tile.pm[s], r);
+                        bool in = r2 < lo_t;
+                        if (!in && r2 <= hi_t) in = exact_r2<D>(st, xi, tile.idx[s], a.pb) < hs2;
+                        if (in) bits |= 1u << b;
+                    }
                 }
                 tile.mask[w * GT + t] = active ? bits : 0u;
             }
@@ -171,6 +173,12 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
         }
         Sum<T> sd, sdh, sn, sp, sdp, sdn;
         sd.zero(); sdh.zero(); sn.zero(); sp.zero(); sdp.zero(); sdn.zero();
+        // the Balsara / time-dependent-alpha sums over the same set {r < h}, accumulated in the
+        // same pass (src/pre_interaction.cpp:115-161 normalise them only afterwards)
+        const bool bal = a.use_balsara && D != 1;
+        const bool avsum = TYPE != 2 && !a.initial && (bal || a.use_tdav);
+        Sum<T> sdiv, srot[3];
+        sdiv.zero(); srot[0].zero(); srot[1].zero(); srot[2].zero();
         T vsig = T(2) * ciT;
         int nnb = 0;
         {
@@ -205,11 +213,36 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
                 }
                 if (!a.initial && j != i) {
                     const V4 vj = a.mvel[j];
-                    T rv = r[0] * (vi[0] - vj.x);
-                    if (D > 1) rv += r[D > 1 ? 1 : 0] * (vi[1] - vj.y);
-                    if (D > 2) rv += r[D > 2 ? 2 : 0] * (vi[2] - vj.z);
+                    T vij[3] = {T(0), T(0), T(0)};
+                    vij[0] = vi[0] - vj.x;
+                    if (D > 1) vij[1] = vi[1] - vj.y;
+                    if (D > 2) vij[2] = vi[2] - vj.z;
+                    T rv = r[0] * vij[0];
+                    if (D > 1) rv += r[D > 1 ? 1 : 0] * vij[1];
+                    if (D > 2) rv += r[D > 2 ? 2 : 0] * vij[2];
                     const T vs = ciT + vj.w - T(3) * rv * (T(1) / rr);
                     vsig = vs > vsig ? vs : vsig;
+                    if (avsum) {
+                        // grad W = r_ij cf; the particle itself contributes dW = 0
+                        const T cf = KF::dw_coef(rr, rr > T(0) ? T(1) / rr : T(0), hinvT);
+                        const T wj = (TYPE == 1) ? p.w * tile.aux[s] : p.w;
+                        T dw[3] = {T(0), T(0), T(0)};
+#pragma unroll
+                        for (int k = 0; k < D; ++k) dw[k] = r[k] * cf;
+                        T vd = vij[0] * dw[0];
+                        if (D > 1) vd += vij[1] * dw[1];
+                        if (D > 2) vd += vij[2] * dw[2];
+                        sdiv.add(-wj * vd);
+                        if (bal) {
+                            if (D == 2) {
+                                srot[0].add((vij[0] * dw[1] - vij[1] * dw[0]) * wj);
+                            } else if (D == 3) {
+                                srot[0].add((vij[1] * dw[2] - vij[2] * dw[1]) * wj);
+                                srot[1].add((vij[2] * dw[0] - vij[0] * dw[2]) * wj);
+                                srot[2].add((vij[0] * dw[1] - vij[1] * dw[0]) * wj);
+                            }
+                        }
+                    }
                 }
             }
         }
@@ -306,42 +339,7 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
         T balsara = (T)st.f[F_BALSARA][i];
         double alpha_out = st.f[F_ALPHA][i], balsara_out = st.f[F_BALSARA][i];
         const T dt = (T)a.dt_run[run];
-        const bool bal = a.use_balsara && D != 1;
-        if (bal || a.use_tdav) {
-            Sum<T> sdiv, srot[3];
-            sdiv.zero(); srot[0].zero(); srot[1].zero(); srot[2].zero();
-            MaskIter it(tile.mask, GT, t, nw);
-            int s;
-            while (it.next(s)) {
-                {
-                    const V4 p = tile.pm[s];
-                    const int j = tile.idx[s];
-                    T r[D];
-                    const T rr = sqrt(tile_r2<D, T>(xo, p, r));
-                    const T cf = KF::dw_coef(rr, rr > T(0) ? T(1) / rr : T(0), hinvT);
-                    const V4 vj = a.mvel[j];
-                    const T wj = (TYPE == 1) ? p.w * tile.aux[s] : p.w;
-                    T dw[3] = {T(0), T(0), T(0)}, vij[3] = {T(0), T(0), T(0)};
-#pragma unroll
-                    for (int k = 0; k < D; ++k) dw[k] = r[k] * cf;
-                    vij[0] = vi[0] - vj.x;
-                    if (D > 1) vij[1] = vi[1] - vj.y;
-                    if (D > 2) vij[2] = vi[2] - vj.z;
-                    T vd = vij[0] * dw[0];
-                    if (D > 1) vd += vij[1] * dw[1];
-                    if (D > 2) vd += vij[2] * dw[2];
-                    sdiv.add(-wj * vd);
-                    if (bal) {
-                        if (D == 2) {
-                            srot[0].add((vij[0] * dw[1] - vij[1] * dw[0]) * wj);
-                        } else if (D == 3) {
-                            srot[0].add((vij[1] * dw[2] - vij[2] * dw[1]) * wj);
-                            srot[1].add((vij[2] * dw[0] - vij[0] * dw[2]) * wj);
-                            srot[2].add((vij[0] * dw[1] - vij[1] * dw[0]) * wj);
-                        }
-                    }
-                }
-            }
+        if (avsum) {
             T div = (T)sdiv.get();
             T rot[3] = {(T)srot[0].get(), (T)srot[1].get(), (T)srot[2].get()};
             if (TYPE == 1) {

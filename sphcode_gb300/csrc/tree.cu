@@ -102,7 +102,7 @@ __global__ void roots_kernel(TreeView tv, double* center0, double* center1, doub
 // The path of a particle through the reference's recursive split, one D-bit digit per level,
 // most significant first, with the run index above the digits.
 template <int D>
-__global__ void keys_kernel(State st, int n, TreeView tv, int levels, int run_shift,
+__global__ void keys_kernel(State st, int n, TreeView tv, int levels, int nd, int run_shift,
                             unsigned long long* keys, int* perm)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -113,7 +113,8 @@ __global__ void keys_kernel(State st, int n, TreeView tv, int levels, int run_sh
     for (int k = 0; k < D; ++k) { x[k] = st.f[F_POS + k][i]; c[k] = tv.center[k][r]; }
     double e = tv.edge[r];
     unsigned long long key = 0;
-    for (int l = 0; l < levels; ++l) {
+    // the first nd digits (the levels a capped build splits); deeper digits stay 0
+    for (int l = 0; l < nd; ++l) {
         unsigned digit = 0;
 #pragma unroll
         for (int k = 0; k < D; ++k) {
@@ -125,6 +126,7 @@ __global__ void keys_kernel(State st, int n, TreeView tv, int levels, int run_sh
         key = (key << D) | digit;
         e = e * 0.5;
     }
+    if (nd < levels) key <<= D * (levels - nd);
     if (run_shift < 64) key |= (unsigned long long)r << run_shift;
     keys[i] = key;
     perm[i] = i;
@@ -279,8 +281,8 @@ __device__ __forceinline__ void child_bounds(const unsigned long long* keys, int
 
 template <int D>
 __global__ void level_count_kernel(NodeArrays na, const unsigned long long* keys,
-                                   const int* lvl_start, int l, int levels, int leaf_num,
-                                   int* lvl_tmp, int* chunk_sum)
+                                   const int* lvl_start, int l, int levels, int lv, int leaf_num,
+                                   int* lvl_tmp, int* chunk_sum, int* trunc)
 {
     constexpr int NC = 1 << D;
     __shared__ int red[32];
@@ -291,7 +293,9 @@ __global__ void level_count_kernel(NodeArrays na, const unsigned long long* keys
         int nc = 0;
         if (node < e) {
             const int cnt = na.count[node];
-            const bool split = (l == 1) || (cnt > leaf_num && l <= levels);
+            const bool split = (l == 1) || (cnt > leaf_num && l <= lv);
+            // a node the full build would split, left a leaf by the cap
+            if (!split && cnt > leaf_num && l <= levels) atomicOr(trunc, 1);
             if (split && cnt > 0) {
                 int bnd[NC + 1];
                 child_bounds<D>(keys, na.begin[node], cnt, D * (levels - l), bnd);
@@ -785,7 +789,7 @@ void launch_reorder_fields(Ctx& c, bool all)
 }
 
 template <int D>
-static void make_tree_d(Ctx& c, bool reorder_all)
+static void make_tree_d(Ctx& c, bool reorder_all, bool full_depth)
 {
     const int n = c.n, R = c.R;
     cudaStream_t s = c.stream;
@@ -800,12 +804,17 @@ static void make_tree_d(Ctx& c, bool reorder_all)
         c.nd_com[1], c.nd_com[2], c.bbox, c.d_run_begin, R, c.pb, c.lvl_start);
     const int levels = c.key_levels;
     const int run_shift = D * levels;
-    keys_kernel<D><<<ceil_div(n, 256), 256, 0, s>>>(c.st, n, tv, levels, run_shift, c.keys, c.perm);
-    // radix sort on the significant bits
-    const int bits = D * levels + c.run_bits;
+    // levels split in this build: all of them with gravity (its node sets are the reference's),
+    // at most depth_cap otherwise
+    const int lv = (full_depth || c.p.use_gravity || c.depth_cap <= 0) ? levels : std::min(levels, c.depth_cap);
+    c.tree_levels = lv;
+    keys_kernel<D><<<ceil_div(n, 256), 256, 0, s>>>(c.st, n, tv, levels, lv, run_shift, c.keys, c.perm);
+    // radix sort on the significant bits: the lv digits computed and the run index
+    const int shift0 = D * (levels - lv);
+    const int bits = D * lv + c.run_bits;
     const int passes = (bits + 7) / 8;
     for (int p = 0; p < passes; ++p) {
-        const int shift = 8 * p;
+        const int shift = shift0 + 8 * p;
         radix_hist_kernel<<<c.radix_blocks, RADIX_THREADS, 0, s>>>(c.keys, n, shift, c.radix_hist, c.radix_blocks);
         radix_scan_columns_kernel<<<256, 1024, 0, s>>>(c.radix_hist, c.radix_blocks, c.radix_dtot);
         radix_scatter_kernel<<<c.radix_blocks, RADIX_THREADS, 0, s>>>(
@@ -821,15 +830,16 @@ static void make_tree_d(Ctx& c, bool reorder_all)
     for (int k = 0; k < 3; ++k) na.center[k] = c.nd_center[k];
     na.edge = c.nd_edge;
     const int grid = std::max(1, std::min(c.num_sms * 4, ceil_div(c.node_cap, LEVEL_CHUNK)));
-    for (int l = 1; l <= levels + 1; ++l) {
-        level_count_kernel<D><<<grid, LEVEL_CHUNK, 0, s>>>(na, c.keys, c.lvl_start, l, levels,
-                                                         c.p.leaf_num, c.lvl_tmp, c.chunk_sum);
+    for (int l = 1; l <= lv + 1; ++l) {
+        level_count_kernel<D><<<grid, LEVEL_CHUNK, 0, s>>>(na, c.keys, c.lvl_start, l, levels, lv,
+                                                         c.p.leaf_num, c.lvl_tmp, c.chunk_sum,
+                                                         c.d_work + TREE_TRUNC_SLOT);
         level_scan_kernel<<<1, 1024, 0, s>>>(c.lvl_start, l, c.chunk_sum, c.node_cap, c.d_err);
         level_emit_kernel<D><<<grid, LEVEL_CHUNK, 0, s>>>(na, c.keys, c.lvl_start, l, levels,
                                                         c.p.leaf_num, c.lvl_tmp, c.chunk_sum,
                                                         c.node_cap, c.d_err);
     }
-    cudaMemcpyAsync(c.node_total, c.lvl_start + levels + 2, sizeof(int), cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(c.node_total, c.lvl_start + lv + 2, sizeof(int), cudaMemcpyDeviceToDevice, s);
     launch_node_moments(c);
     split_groups_kernel<D><<<ceil_div(c.num_chunks, 128), 128, 0, s>>>(c.st, c.keys, c.ck_begin, c.ck_count,
                                                                    c.num_chunks, c.part_begin, c.part_count,
@@ -854,17 +864,29 @@ static void make_tree_d(Ctx& c, bool reorder_all)
     c.kernel_size_valid = false;
 }
 
-void launch_make_tree(Ctx& c, bool reorder_all)
+void launch_make_tree(Ctx& c, bool reorder_all, bool full_depth)
 {
-    if (c.dim == 1) make_tree_d<1>(c, reorder_all);
-    else if (c.dim == 2) make_tree_d<2>(c, reorder_all);
-    else make_tree_d<3>(c, reorder_all);
+    if (c.dim == 1) make_tree_d<1>(c, reorder_all, full_depth);
+    else if (c.dim == 2) make_tree_d<2>(c, reorder_all, full_depth);
+    else make_tree_d<3>(c, reorder_all, full_depth);
+}
+
+int tree_depth(Ctx& c)
+{
+    int ls[MAX_LEVELS + 2];
+    const int nl = c.tree_levels + 3;
+    cudaMemcpyAsync(ls, c.lvl_start, sizeof(int) * nl, cudaMemcpyDeviceToHost, c.stream);
+    cudaStreamSynchronize(c.stream);
+    int depth = 1;
+    for (int l = 1; l + 1 < nl; ++l)
+        if (ls[l + 1] > ls[l]) depth = l;
+    return depth;
 }
 
 void launch_node_moments(Ctx& c)
 {
     const int grid = c.num_sms * 8;
-    for (int l = c.key_levels + 1; l >= 2; --l) {
+    for (int l = c.tree_levels + 1; l >= 2; --l) {
         if (c.dim == 1)
             moments_level_kernel<1><<<grid, 256, 0, c.stream>>>(c.st, c.lvl_start, l, c.R, c.nd_begin, c.nd_count, c.nd_first, c.nd_nchild, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
         else if (c.dim == 2)
@@ -879,7 +901,7 @@ void launch_node_moments(Ctx& c)
 
 void launch_set_kernel_size(Ctx& c)
 {
-    for (int l = c.key_levels + 1; l >= 1; --l)
+    for (int l = c.tree_levels + 1; l >= 1; --l)
         ksize_level_kernel<<<c.num_sms * 8, 256, 0, c.stream>>>(c.st.f[F_SML], c.lvl_start, l, c.nd_begin,
                                                                c.nd_count, c.nd_first, c.nd_nchild,
                                                                c.nd_ksize);
