@@ -840,7 +840,7 @@ static void make_tree_d(Ctx& c, bool reorder_all, bool full_depth)
                                                         c.node_cap, c.d_err);
     }
     cudaMemcpyAsync(c.node_total, c.lvl_start + lv + 2, sizeof(int), cudaMemcpyDeviceToDevice, s);
-    launch_node_moments(c);
+    if (c.p.use_gravity) launch_node_moments(c);   // node masses and centres of mass serve gravity only
     split_groups_kernel<D><<<ceil_div(c.num_chunks, 128), 128, 0, s>>>(c.st, c.keys, c.ck_begin, c.ck_count,
                                                                    c.num_chunks, c.part_begin, c.part_count,
                                                                    c.part_n);
