@@ -203,7 +203,11 @@ const char* sphgpu_last_error(const sphgpu_ctx* ctx);
  * first (1..8, default 2); 13..17 (read only) the last target range no pair-kernel pass could
  * fit: {first particle (key order), count, search radius x 1e9, leaves, overflow code};
  * 18 fixed time step on/off: with 1, sphgpu_step skips TimeStep and advances every run by the
- * dt last set with sphgpu_set_scalar(SPHGPU_SCALAR_DT) (the adjoint requires it). */
+ * dt last set with sphgpu_set_scalar(SPHGPU_SCALAR_DT) (the adjoint requires it);
+ * 19 AoS record reuse on/off: with 1, sphgpu_download_aos takes the record members outside the
+ * layout from the records of the last sphgpu_upload_aos (same stride) instead of copying the
+ * caller's buffer to the device first — valid when the caller has not changed those members on
+ * the host since that upload (the upload, calculate, download pattern of a Module). */
 int sphgpu_set_tuning(sphgpu_ctx* ctx, int which, int value);
 int sphgpu_get_tuning(sphgpu_ctx* ctx, int which, int* value);
 

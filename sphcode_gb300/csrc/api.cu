@@ -275,6 +275,7 @@ void free_state(State& s, bool primary)
 void free_ctx(Ctx& c)
 {
     if (c.graph) cudaGraphExecDestroy(c.graph);
+    if (c.adj_graph) cudaGraphExecDestroy(c.adj_graph);
     tree_free(c);
     free_state(c.st, true);
     c.alt.run = nullptr;
@@ -624,6 +625,7 @@ void check_tree_cap(Ctx& c)
     cudaStreamSynchronize(c.stream);
     c.depth_cap = std::min(c.key_levels, c.tree_levels + 4);
     c.graph_valid = false;
+    ++c.graph_epoch;
     c.warm = false;
 }
 
@@ -772,6 +774,7 @@ int sphgpu_upload_aos(sphgpu_ctx* h, const void* base, const sphgpu_aos_layout* 
     const int rc = sphgpu::ensure_aos_stage(c, bytes, "upload_aos");
     if (rc != SPHGPU_OK) return rc;
     cudaMemcpyAsync(c.d_aos, base, bytes, cudaMemcpyHostToDevice, c.stream);
+    c.aos_stage_stride = layout->stride;
     sphgpu::aos_upload_kernel<<<sphgpu::ceil_div(c.n, 256), 256, 0, c.stream>>>(c.st, m, c.d_aos, c.n);
     c.tree_valid = false;
     c.kernel_size_valid = false;
@@ -784,10 +787,13 @@ int sphgpu_download_aos(sphgpu_ctx* h, void* base, const sphgpu_aos_layout* layo
     if (!base || !layout || layout->stride == 0) return SPHGPU_ERR_ARG;
     const size_t bytes = layout->stride * (size_t)c.n;
     const sphgpu::AosMap m = sphgpu::aos_map(c, layout);
+    const bool reuse = c.aos_reuse && c.aos_stage_stride == layout->stride && bytes <= c.aos_bytes;
     const int rc = sphgpu::ensure_aos_stage(c, bytes, "download_aos");
     if (rc != SPHGPU_OK) return rc;
-    // the members outside the layout keep the caller's values
-    cudaMemcpyAsync(c.d_aos, base, bytes, cudaMemcpyHostToDevice, c.stream);
+    // the members outside the layout keep the caller's values: read them again, or (knob 19)
+    // take them from the records of the last upload, which the caller has not changed since
+    if (!reuse) cudaMemcpyAsync(c.d_aos, base, bytes, cudaMemcpyHostToDevice, c.stream);
+    c.aos_stage_stride = layout->stride;
     sphgpu::aos_download_kernel<<<sphgpu::ceil_div(c.n, 256), 256, 0, c.stream>>>(c.st, m, c.d_aos, c.n);
     cudaMemcpyAsync(base, c.d_aos, bytes, cudaMemcpyDeviceToHost, c.stream);
     return sphgpu::finish(c, "download_aos");
@@ -901,6 +907,7 @@ int sphgpu_initialize(sphgpu_ctx* h)
     sphgpu::launch_fluid(c);
     if (c.p.use_gravity) sphgpu::launch_gravity(c);
     c.graph_valid = false;
+    ++c.graph_epoch;
     const int rc = sphgpu::finish(c, "initialize");
     // later builds split two levels deeper than the initial tree (without gravity)
     if (rc == SPHGPU_OK && !c.p.use_gravity) c.depth_cap = std::min(c.key_levels, sphgpu::tree_depth(c) + 1);
@@ -1029,11 +1036,40 @@ int sphgpu_adjoint_step(sphgpu_ctx* h, double* adj, const double* dens_bar, doub
     if (c.first_pre) { c.last_error = "adjoint_step: before initialize"; return SPHGPU_ERR_STATE; }
     int rc = sphgpu::adjoint_ready(c, "adjoint_step");
     if (rc != SPHGPU_OK) return rc;
-    // forward quantities of the step: prediction, tree, PreInteraction
-    sphgpu::launch_predict(c);
-    sphgpu::launch_make_tree(c, false);
-    sphgpu::run_pre_stage(c);
-    sphgpu::launch_adjoint(c, adj, dens_bar, alpha_bar, false);
+    // forward quantities of the step (prediction, tree, PreInteraction), then the backward passes;
+    // replayed as a CUDA graph once the same buffers come back (first call eager, second captured)
+    auto body = [&]() {
+        sphgpu::launch_predict(c);
+        sphgpu::launch_make_tree(c, false);
+        sphgpu::run_pre_stage(c);
+        sphgpu::launch_adjoint(c, adj, dens_bar, alpha_bar, false);
+    };
+    const void* key[3] = {adj, dens_bar, alpha_bar};
+    auto same = [&](const void* const* k) { return k[0] == key[0] && k[1] == key[1] && k[2] == key[2]; };
+    if (!c.use_graph || c.timing) {
+        body();
+    } else if (c.adj_graph && c.adj_epoch == c.graph_epoch && same(c.adj_key)) {
+        cudaError_t e = cudaGraphLaunch(c.adj_graph, c.stream);
+        if (e != cudaSuccess) return sphgpu::cuda_status(c, e, "adjoint_step launch");
+    } else if (!same(c.adj_warm_key)) {
+        body();
+        for (int q = 0; q < 3; ++q) c.adj_warm_key[q] = key[q];
+    } else {
+        if (c.adj_graph) { cudaGraphExecDestroy(c.adj_graph); c.adj_graph = nullptr; }
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return sphgpu::cuda_status(c, e, "adjoint_step capture");
+        body();
+        e = cudaStreamEndCapture(c.stream, &g);
+        if (e != cudaSuccess) return sphgpu::cuda_status(c, e, "adjoint_step capture");
+        e = cudaGraphInstantiate(&c.adj_graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) { c.adj_graph = nullptr; return sphgpu::cuda_status(c, e, "adjoint_step instantiate"); }
+        for (int q = 0; q < 3; ++q) c.adj_key[q] = key[q];
+        c.adj_epoch = c.graph_epoch;
+        e = cudaGraphLaunch(c.adj_graph, c.stream);
+        if (e != cudaSuccess) return sphgpu::cuda_status(c, e, "adjoint_step launch");
+    }
     rc = sphgpu::finish(c, "adjoint_step");
     if (rc == SPHGPU_OK) sphgpu::check_tree_cap(c);
     return rc;
@@ -1172,11 +1208,13 @@ int sphgpu_set_tuning(sphgpu_ctx* h, int which, int value)
         break;
     case 4: c.autotune = value != 0; break;
     case 18: c.fixed_dt = value != 0; break;
+    case 19: c.aos_reuse = value != 0; break;
     case 5: c.timing = value != 0; break;
     case 6: c.use_graph = value != 0; break;
     default: return SPHGPU_ERR_ARG;
     }
     c.graph_valid = false;
+    ++c.graph_epoch;
     c.warm = false;
     return SPHGPU_OK;
 }
@@ -1200,6 +1238,7 @@ int sphgpu_get_tuning(sphgpu_ctx* h, int which, int* value)
     case 11: *value = (int)c.tune_rejects; break;
     case 12: *value = c.pass2_scale; break;
     case 18: *value = c.fixed_dt ? 1 : 0; break;
+    case 19: *value = c.aos_reuse ? 1 : 0; break;
     case 13: case 14: case 15: case 16: case 17: {
         cudaStreamSynchronize(c.stream);
         cudaMemcpy(value, c.d_work + sphgpu::FAIL_INFO_SLOT + (which - 13), sizeof(int), cudaMemcpyDeviceToHost);

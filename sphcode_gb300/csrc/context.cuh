@@ -90,6 +90,9 @@ struct Ctx {
     size_t stage_bytes = 0;
     unsigned char* d_aos = nullptr;
     size_t aos_bytes = 0;
+    size_t aos_stage_stride = 0;    // stride of the records the staging buffer holds (0: none)
+    bool aos_reuse = false;         // knob 19: downloads take the members outside the layout from
+                                    // the last upload's records instead of reading them again
     unsigned char* d_flush = nullptr;   // L2 flush buffer of the benchmark helper
     size_t flush_bytes = 0;
 
@@ -111,6 +114,12 @@ struct Ctx {
     bool use_graph = true;
     bool warm = false;
     int graph_kernels = 0;          // kernel nodes of the captured step
+    int graph_epoch = 0;            // bumped whenever captured graphs go stale
+    // graph of one reversed step, keyed by the adjoint buffers it was captured with
+    cudaGraphExec_t adj_graph = nullptr;
+    const void* adj_key[3] = {nullptr, nullptr, nullptr};
+    const void* adj_warm_key[3] = {nullptr, nullptr, nullptr};
+    int adj_epoch = -1;
 
     // stage timing
     cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};

@@ -67,3 +67,26 @@ def test_aos_round_trip(gpu_lib, pinned):
         assert np.all(rec["next"] == 0xABCDEF0123456789)
         sim.step(1)
     del keep
+
+
+def test_download_reuses_uploaded_records(gpu_lib):
+    """Knob 19: the download takes the members outside the layout from the last upload."""
+    import ctypes
+    from sphcode_gb300 import ics, sphgpu
+    p, f = ics.gresho(32)
+    n = f["mass"].size
+    dt = particle_dtype(2)
+    lay = layout(dt)
+    rec = np.zeros(n, dtype=dt)
+    rec["id"] = np.arange(n)
+    rec["next"] = 7
+    with sphgpu.GpuSimulation(p, f, precision="fp64") as sim:
+        sim.set_tuning("aos_reuse", 1)
+        sim.initialize()
+        assert sim.lib.sphgpu_download_aos(sim._h, rec.ctypes.data, ctypes.byref(lay)) == 0
+        assert sim.lib.sphgpu_upload_aos(sim._h, rec.ctypes.data, ctypes.byref(lay)) == 0
+        sim.step(1)
+        out = np.zeros(n, dtype=dt)      # a different buffer: its own members are not read
+        assert sim.lib.sphgpu_download_aos(sim._h, out.ctypes.data, ctypes.byref(lay)) == 0
+        assert np.all(out["next"] == 7) and np.array_equal(out["id"], np.arange(n))
+        assert np.array_equal(out["dens"], sim.get("dens"))
