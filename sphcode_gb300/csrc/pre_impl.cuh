@@ -132,17 +132,31 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
                     Sum<T> s0, s1;
                     s0.zero();
                     s1.zero();
+                    // two candidates per trip: independent dependency chains, one compensated
+                    // add per pair
                     MaskIter it(tile.mask, GT, t, nw);
-                    int s;
-                    while (it.next(s)) {
-                        const V4 p = tile.pm[s];
-                        T r[D];
-                        const T rr = sqrt(tile_r2<D, T>(xo, p, r));
-                        if (rr < hT) {
+                    int sa, sb;
+                    while (it.next(sa)) {
+                        const bool two = it.next(sb);
+                        T w = T(0), dw = T(0);
+                        {
+                            const V4 p = tile.pm[sa];
+                            T r[D];
+                            const T rr = sqrt(tile_r2<D, T>(xo, p, r));
+                            const T m = TYPE == 1 ? T(1) : p.w;
                             const T W = KF::w(rr, hinvT), dW = KF::dhw(rr, hinvT);
-                            if (TYPE == 1) { s0.add(W); s1.add(dW); }
-                            else { s0.add(p.w * W); s1.add(p.w * dW); }
+                            if (rr < hT) { w = m * W; dw = m * dW; }
                         }
+                        if (two) {
+                            const V4 p = tile.pm[sb];
+                            T r[D];
+                            const T rr = sqrt(tile_r2<D, T>(xo, p, r));
+                            const T m = TYPE == 1 ? T(1) : p.w;
+                            const T W = KF::w(rr, hinvT), dW = KF::dhw(rr, hinvT);
+                            if (rr < hT) { w += m * W; dw += m * dW; }
+                        }
+                        s0.add(w);
+                        s1.add(dw);
                     }
                     const T dens = (T)s0.get(), ddens = (T)s1.get();
                     const T hd = powD<D>(hT);
