@@ -318,52 +318,51 @@ __global__ void level_count_kernel(NodeArrays na, const unsigned long long* keys
     }
 }
 
-__global__ void level_scan_kernel(int* lvl_start, int l, int* chunk_sum, int node_cap,
-                                  unsigned* err)
-{
-    __shared__ int part[1024];
-    const int s = lvl_start[l], e = lvl_start[l + 1];
-    const int m = (e - s + LEVEL_CHUNK - 1) / LEVEL_CHUNK;
-    const int t = threadIdx.x;
-    const int per = (m + 1023) / 1024;
-    const int b = t * per, en = min(m, b + per);
-    int sum = 0;
-    for (int i = b; i < en; ++i) sum += chunk_sum[i];
-    part[t] = sum;
-    __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {
-        const int v = t >= o ? part[t - o] : 0;
-        __syncthreads();
-        part[t] += v;
-        __syncthreads();
-    }
-    int run = t > 0 ? part[t - 1] : 0;
-    for (int i = b; i < en; ++i) {
-        const int v = chunk_sum[i];
-        chunk_sum[i] = run;
-        run += v;
-    }
-    if (t == 1023) {
-        int next = lvl_start[l + 1] + part[1023];
-        if (next > node_cap) { atomicOr(err, (unsigned)ERR_NODE_POOL); next = node_cap; }
-        lvl_start[l + 2] = next;
-    }
-}
 
+// One launch per level: emits the children of the level-l nodes (level l + 1: begin, count,
+// centre, edge, parent) and, for each child, its own split decision and child count, so that the
+// next launch can place the grandchildren.  tmp_cur / cs_cur hold the child counts of the level-l
+// nodes and their per-chunk totals (accumulated by the previous launch); this launch accumulates
+// tmp_next / cs_next for level l + 1 and clears cs_clear, the totals the launch after it fills.
+// Node indices are breadth-first and, within a level, in key order.
 template <int D>
-__global__ void level_emit_kernel(NodeArrays na, const unsigned long long* keys,
-                                  const int* lvl_start, int l, int levels, int leaf_num,
-                                  const int* lvl_tmp, const int* chunk_off, int node_cap,
-                                  unsigned* err)
+__global__ void level_build_kernel(NodeArrays na, const unsigned long long* keys, int n, int* lvl_start, int l,
+                                   int levels, int lv, int leaf_num, const int* tmp_cur, int* tmp_next,
+                                   const int* cs_cur, int* cs_next, int* cs_clear, int cs_cap, int node_cap,
+                                   unsigned* err, int* trunc)
 {
     constexpr int NC = 1 << D;
     __shared__ int sc[LEVEL_CHUNK];
+    __shared__ int red[32];
+    __shared__ int agg[NC + 2];   // child totals per next-level chunk touched by this chunk's children
     const int s = lvl_start[l], e = lvl_start[l + 1];
-    const int cbase = lvl_start[l + 1];
     const int nchunks = (e - s + LEVEL_CHUNK - 1) / LEVEL_CHUNK;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < cs_cap; q += gridDim.x * blockDim.x) cs_clear[q] = 0;
+    // block sum of cs_cur[0, m)
+    auto prefix = [&](int m) {
+        int v = 0;
+        for (int q = threadIdx.x; q < m; q += blockDim.x) v += cs_cur[q];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+        __syncthreads();
+        int u = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) u += red[w];
+        __syncthreads();
+        return u;
+    };
+    const int cbase = e;   // level l + 1 starts where level l ends
+    if (blockIdx.x == 0) {
+        const int total = prefix(nchunks);
+        if (threadIdx.x == 0) {
+            int next = cbase + total;
+            if (next > node_cap) { atomicOr(err, (unsigned)ERR_NODE_POOL); next = node_cap; }
+            lvl_start[l + 2] = next;
+        }
+    }
     for (int chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
+        const int chunk_off = prefix(chunk);
         const int node = s + chunk * LEVEL_CHUNK + threadIdx.x;
-        const int nc = node < e ? lvl_tmp[node - s] : 0;
+        const int nc = node < e ? tmp_cur[node - s] : 0;
         sc[threadIdx.x] = nc;
         __syncthreads();
         for (int o = 1; o < LEVEL_CHUNK; o <<= 1) {
@@ -372,7 +371,8 @@ __global__ void level_emit_kernel(NodeArrays na, const unsigned long long* keys,
             sc[threadIdx.x] += v;
             __syncthreads();
         }
-        const int off = sc[threadIdx.x] - nc + chunk_off[chunk];
+        const int off = sc[threadIdx.x] - nc + chunk_off;
+        const int chunk_children = sc[LEVEL_CHUNK - 1];
         __syncthreads();
         if (node < e && nc > 0) {
             const int b = na.begin[node], cnt = na.count[node];
@@ -409,13 +409,61 @@ __global__ void level_emit_kernel(NodeArrays na, const unsigned long long* keys,
             }
         }
         __syncthreads();
+        // the children of this chunk's nodes are consecutive: one thread per child for its split
+        // decision (src/bhtree.cpp:154-158) and child count
+        const int lc = l + 1;
+        const int c0 = cbase + chunk_off, c1 = min(c0 + chunk_children, node_cap);
+        const int q0 = (c0 - cbase) / LEVEL_CHUNK;   // first next-level chunk touched
+        if (threadIdx.x < NC + 2) agg[threadIdx.x] = 0;
+        __syncthreads();
+        for (int ci = c0 + threadIdx.x; ci < c1; ci += blockDim.x) {
+            const int cb = na.begin[ci], ccnt = na.count[ci];
+            int ncc = 0;
+            // slots of a parent the node pool could not hold were not written (the error bit is set)
+            if (cb < 0 || ccnt < 0 || cb + ccnt > n) { tmp_next[ci - cbase] = 0; continue; }
+            const bool split = ccnt > leaf_num && lc <= lv;
+            if (!split && ccnt > leaf_num && lc <= levels) atomicOr(trunc, 1);
+            if (split) {
+                int cbnd[NC + 1];
+                child_bounds<D>(keys, cb, ccnt, D * (levels - lc), cbnd);
+                for (int g = 0; g < NC; ++g) ncc += cbnd[g + 1] > cbnd[g];
+            }
+            tmp_next[ci - cbase] = ncc;
+            if (ncc) atomicAdd(&agg[(ci - cbase) / LEVEL_CHUNK - q0], ncc);
+        }
+        __syncthreads();
+        // at most NC * LEVEL_CHUNK children from one chunk: they touch at most NC + 1 chunks
+        if (threadIdx.x < NC + 2 && agg[threadIdx.x]) atomicAdd(&cs_next[q0 + threadIdx.x], agg[threadIdx.x]);
+        __syncthreads();
     }
 }
+
+
 
 // ---- bottom-up reductions, one tree level per launch -------------------------------------------
 // Level l occupies the node range [lvl_start[l], lvl_start[l + 1]) of the breadth-first arrays;
 // deeper levels are done first, so a node reads its finished children (no atomics, and the sums
 // do not depend on scheduling).
+
+// Kernel size (BHTree::set_kernel, src/bhtree.cpp:206-232): leaves take the maximum h of their
+// particles, inner nodes the maximum of their children.
+__global__ void ksize_level_kernel(const double* sml, const int* lvl_start, int l, const int* begin,
+                                   const int* count, const int* first, const int* nchild, double* ksize)
+{
+    const int s = lvl_start[l], e = lvl_start[l + 1];
+    for (int i = s + blockIdx.x * blockDim.x + threadIdx.x; i < e; i += gridDim.x * blockDim.x) {
+        double h = 0.0;
+        const int fc = first[i];
+        if (fc < 0) {
+            const int b = begin[i], en = b + count[i];
+            for (int j = b; j < en; ++j) h = fmax(h, sml[j]);
+        } else {
+            const int nc = nchild[i];
+            for (int c = 0; c < nc; ++c) h = fmax(h, ksize[fc + c]);
+        }
+        ksize[i] = h;
+    }
+}
 
 // Mass and sum of m x per node: leaves sum their particles, inner nodes their children.  The roots
 // keep zero mass and centre, as in the reference, whose root never receives them.
@@ -468,23 +516,6 @@ __global__ void com_finalize_kernel(const int* node_total_p, int R, const double
 }
 
 // Per-node maximum smoothing length (BHNode::set_kernel, src/bhtree.cpp:206-232).
-__global__ void ksize_level_kernel(const double* sml, const int* lvl_start, int l, const int* begin,
-                                   const int* count, const int* first, const int* nchild, double* ksize)
-{
-    const int s = lvl_start[l], e = lvl_start[l + 1];
-    for (int i = s + blockIdx.x * blockDim.x + threadIdx.x; i < e; i += gridDim.x * blockDim.x) {
-        double h = 0.0;
-        const int fc = first[i];
-        if (fc < 0) {
-            const int b = begin[i], en = b + count[i];
-            for (int j = b; j < en; ++j) h = fmax(h, sml[j]);
-        } else {
-            const int nc = nchild[i];
-            for (int c = 0; c < nc; ++c) h = fmax(h, ksize[fc + c]);
-        }
-        ksize[i] = h;
-    }
-}
 
 // ---- target groups ----------------------------------------------------------------------------
 // Each fixed chunk of key-consecutive particles is split at the highest key bit in which its
@@ -719,8 +750,8 @@ int tree_alloc(Ctx& c)
     A((void**)&c.nd_mass, sizeof(double) * nc);
     A((void**)&c.nd_ksize, sizeof(double) * nc);
     A((void**)&c.lvl_start, sizeof(int) * (MAX_LEVELS + 2));
-    A((void**)&c.lvl_tmp, sizeof(int) * nc);
-    A((void**)&c.chunk_sum, sizeof(int) * (ceil_div(nc, LEVEL_CHUNK) + 1));
+    A((void**)&c.lvl_tmp, sizeof(int) * 2 * (size_t)nc);
+    A((void**)&c.chunk_sum, sizeof(int) * 3 * (size_t)(ceil_div(nc, LEVEL_CHUNK) + 1));
     A((void**)&c.bbox, sizeof(long long) * 2 * 3 * c.R);
     A((void**)&c.node_total, sizeof(int));
     const int max_chunks = n / 32 + c.R + 1;
@@ -830,14 +861,19 @@ static void make_tree_d(Ctx& c, bool reorder_all, bool full_depth)
     for (int k = 0; k < 3; ++k) na.center[k] = c.nd_center[k];
     na.edge = c.nd_edge;
     const int grid = std::max(1, std::min(c.num_sms * 4, ceil_div(c.node_cap, LEVEL_CHUNK)));
-    for (int l = 1; l <= lv + 1; ++l) {
-        level_count_kernel<D><<<grid, LEVEL_CHUNK, 0, s>>>(na, c.keys, c.lvl_start, l, levels, lv,
-                                                         c.p.leaf_num, c.lvl_tmp, c.chunk_sum,
-                                                         c.d_work + TREE_TRUNC_SLOT);
-        level_scan_kernel<<<1, 1024, 0, s>>>(c.lvl_start, l, c.chunk_sum, c.node_cap, c.d_err);
-        level_emit_kernel<D><<<grid, LEVEL_CHUNK, 0, s>>>(na, c.keys, c.lvl_start, l, levels,
-                                                        c.p.leaf_num, c.lvl_tmp, c.chunk_sum,
-                                                        c.node_cap, c.d_err);
+    {
+        // child counts of the roots, then one launch per level (children of level l and their counts)
+        const int cs_cap = ceil_div(c.node_cap, LEVEL_CHUNK) + 1;
+        int* tmp[2] = {c.lvl_tmp, c.lvl_tmp + c.node_cap};
+        int* cs[3] = {c.chunk_sum, c.chunk_sum + cs_cap, c.chunk_sum + 2 * cs_cap};
+        cudaMemsetAsync(c.chunk_sum, 0, sizeof(int) * 3 * (size_t)cs_cap, s);
+        level_count_kernel<D><<<grid, LEVEL_CHUNK, 0, s>>>(na, c.keys, c.lvl_start, 1, levels, lv,
+                                                         c.p.leaf_num, tmp[1], cs[1], c.d_work + TREE_TRUNC_SLOT);
+        for (int l = 1; l <= lv; ++l)
+            level_build_kernel<D><<<grid, LEVEL_CHUNK, 0, s>>>(
+                na, c.keys, n, c.lvl_start, l, levels, lv, c.p.leaf_num, tmp[l & 1], tmp[(l + 1) & 1],
+                cs[l % 3], cs[(l + 1) % 3], cs[(l + 2) % 3], cs_cap, c.node_cap, c.d_err,
+                c.d_work + TREE_TRUNC_SLOT);
     }
     cudaMemcpyAsync(c.node_total, c.lvl_start + lv + 2, sizeof(int), cudaMemcpyDeviceToDevice, s);
     if (c.p.use_gravity) launch_node_moments(c);   // node masses and centres of mass serve gravity only
