@@ -110,21 +110,31 @@ __global__ void keys_kernel(State st, int n, TreeView tv, int levels, int nd, in
     const int r = st.run[i];
     double x[D], c[D];
 #pragma unroll
-    for (int k = 0; k < D; ++k) { x[k] = st.f[F_POS + k][i]; c[k] = tv.center[k][r]; }
-    double e = tv.edge[r];
+    // + 0.0 turns -0.0 into +0.0, so that the ordered-integer comparison below equals x > c
+    for (int k = 0; k < D; ++k) { x[k] = st.f[F_POS + k][i] + 0.0; c[k] = tv.center[k][r] + 0.0; }
+    // edge / 4 of level l is the root edge scaled by 2^-(l+2): exact, so it is formed on the
+    // exponent bits; only the centre update needs FP64 arithmetic, and the comparison x > c runs on
+    // the ordered-integer images of the doubles
+    const double e0 = tv.edge[r];
+    const bool scale = e0 > 0.0;   // a zero-extent root keeps every centre (edge * 0.25 = 0)
+    long long q = scale ? __double_as_longlong(e0) - (2LL << 52) : 0;
+    long long xo[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) xo[k] = dbl_to_ord(x[k]);
     unsigned long long key = 0;
     // the first nd digits (the levels a capped build splits); deeper digits stay 0
     for (int l = 0; l < nd; ++l) {
         unsigned digit = 0;
+        const double qd = scale ? __longlong_as_double(q) : 0.0;
 #pragma unroll
         for (int k = 0; k < D; ++k) {
-            const bool up = x[k] > c[k];
+            const bool up = xo[k] > dbl_to_ord(c[k]);
             digit |= (up ? 1u : 0u) << k;
             // child center: center + (+/-1 * edge) * 0.25, one rounding (src/bhtree.cpp:190-196)
-            c[k] = __dadd_rn(c[k], (up ? e : -e) * 0.25);
+            c[k] = __dadd_rn(c[k], up ? qd : -qd);
         }
         key = (key << D) | digit;
-        e = e * 0.5;
+        q -= 1LL << 52;
     }
     if (nd < levels) key <<= D * (levels - nd);
     if (run_shift < 64) key |= (unsigned long long)r << run_shift;
