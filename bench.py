@@ -388,7 +388,8 @@ def main():
             stages[k] += v / reps
     overflow = {"pre": sim.get_tuning("overflow_pre"), "fluid": sim.get_tuning("overflow_fluid")}
     schedule = {"group_warps": sim.get_tuning("group_warps"), "tile_pre": sim.get_tuning("tile_cap_pre"),
-                "tile_fluid": sim.get_tuning("tile_cap"), "autotuned": bool(sim.get_tuning("autotune")),
+                "tile_fluid": sim.get_tuning("tile_cap"), "pass2_scale": sim.get_tuning("pass2_scale"),
+                "autotuned": bool(sim.get_tuning("autotune")),
                 "rejected_candidate_status_bits": sim.get_tuning("tune_rejects")}
     sim.set_tuning("timing", 0)
     pairs = sim.neighbor_counts(True).astype(np.int64) - 1   # r = 0 (self) is skipped
