@@ -476,55 +476,77 @@ __device__ int stage_sources(unsigned char* smem, const SmemLayout& L, GroupMisc
     const int total = lpre[nl];
     int* wcnt = reinterpret_cast<int*>(&gm->wred[0][0]);
     int base = 0;
-    for (int f0 = 0; f0 < total; f0 += blockDim.x) {
-        const int f = f0 + threadIdx.x;
-        bool ok = false;
-        int j = -1;
-        T off[D];
-        T m = T(0);
-        if (f < total) {
-            int lo = 0, hi = nl;   // last r with lpre[r] <= f
-            while (hi - lo > 1) {
-                const int mid = (lo + hi) >> 1;
-                if (lpre[mid] <= f) lo = mid; else hi = mid;
+    // U sources per thread between barriers: their loads overlap, and the slot order (by f) is the
+    // same as one source per thread per barrier
+    constexpr int U = 4;
+    for (int f0 = 0; f0 < total; f0 += U * blockDim.x) {
+        bool ok[U];
+        int jj[U];
+        T off[U][D];
+        T mm[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int f = f0 + u * blockDim.x + threadIdx.x;
+            ok[u] = false;
+            jj[u] = -1;
+            mm[u] = T(0);
+#pragma unroll
+            for (int k = 0; k < D; ++k) off[u][k] = T(0);
+            if (f < total) {
+                int lo = 0, hi = nl;   // last r with lpre[r] <= f
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (lpre[mid] <= f) lo = mid; else hi = mid;
+                }
+                const int j = leaves[lo].x + (f - lpre[lo]);
+                const V4 a = loff[lo];
+                const V4 q = xrel[j];
+                off[u][0] = a.x + q.x;
+                if (D > 1) off[u][D > 1 ? 1 : 0] = a.y + q.y;
+                if (D > 2) off[u][D > 2 ? 2 : 0] = a.z + q.z;
+                mm[u] = q.w;
+                jj[u] = j;
+                ok[u] = accept(j, off[u]);
             }
-            j = leaves[lo].x + (f - lpre[lo]);
-            const V4 a = loff[lo];
-            const V4 q = xrel[j];
-            off[0] = a.x + q.x;
-            if (D > 1) off[D > 1 ? 1 : 0] = a.y + q.y;
-            if (D > 2) off[D > 2 ? 2 : 0] = a.z + q.z;
-            m = q.w;
-            ok = accept(j, off);
         }
-        const unsigned bal = __ballot_sync(FULL, ok);
+        unsigned bal[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) bal[u] = __ballot_sync(FULL, ok[u]);
         __syncthreads();   // previous iteration's readers of wcnt are done
-        if (lane == 0) wcnt[w] = __popc(bal);
+        if (lane == 0) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) wcnt[u * nw + w] = __popc(bal[u]);
+        }
         __syncthreads();
-        int woff = 0, tot = 0;
-        for (int ww = 0; ww < nw; ++ww) {
-            const int c = wcnt[ww];
-            if (ww < w) woff += c;
-            tot += c;
-        }
-        if (ok) {
-            const int slot = base + woff + __popc(bal & lanemask_lt());
-            if (slot < L.tcap) {
-                V4 v;
-                v.x = off[0];
-                v.y = D > 1 ? off[D > 1 ? 1 : 0] : T(0);
-                v.z = D > 2 ? off[D > 2 ? 2 : 0] : T(0);
-                v.w = m;
-                tile.pm[slot] = v;
-                tile.aux[slot] = aux(j);
-                tile.idx[slot] = j;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            int woff = 0, tot = 0;
+            for (int ww = 0; ww < nw; ++ww) {
+                const int c = wcnt[u * nw + ww];
+                if (ww < w) woff += c;
+                tot += c;
             }
+            if (ok[u]) {
+                const int slot = base + woff + __popc(bal[u] & lanemask_lt());
+                if (slot < L.tcap) {
+                    V4 v;
+                    v.x = off[u][0];
+                    v.y = D > 1 ? off[u][D > 1 ? 1 : 0] : T(0);
+                    v.z = D > 2 ? off[u][D > 2 ? 2 : 0] : T(0);
+                    v.w = mm[u];
+                    tile.pm[slot] = v;
+                    tile.aux[slot] = aux(jj[u]);
+                    tile.idx[slot] = jj[u];
+                }
+            }
+            base += tot;
         }
-        base += tot;
+        // the range goes to a later pass: no need to count the rest (base is block-uniform)
+        if (base > L.tcap) break;
     }
     __syncthreads();
     if (base > L.tcap) {
-        if (threadIdx.x == 0) gm->overflow = 1000000 + base;   // diagnostic: sources needed
+        if (threadIdx.x == 0) gm->overflow = 1000000 + base;   // diagnostic: sources needed (at least)
         return -1;
     }
     // bounding boxes of the mask words (warp w reduces words w, w + nw, ...).  Built in 3D only:
