@@ -404,6 +404,7 @@ int create_impl(const sphgpu_params* params, int dim, int n_runs, const int* run
         A(&c.mir[5], c.p.sph_type == 2 ? sizeof(double) * 16 * n : 16);   // gsph gradients
         A(&c.mir[6], sizeof(double4_32a) * n);                        // {x - leaf centre, m}
         A(&c.mir[7], sizeof(double) * n);                             // h
+        A(&c.mir[8], sizeof(double) * n);                             // Pre smoothing-length guess
         for (int q = 0; q < 7 && e == cudaSuccess; ++q) e = cudaEventCreate(&c.ev[q]);
         if (e != cudaSuccess) rc = cuda_status(c, e, "create");
     }

@@ -76,7 +76,8 @@ struct Ctx {
 
     // key-ordered mirrors of source fields in the pair type (sized for FP64):
     // 0 Pre {v, c}, 1 Pre u, 2-4 Fluid records, 5 gsph gradients,
-    // 6 {x - leaf centre, m} (tree build), 7 h (end of PreInteraction)
+    // 6 {x - leaf centre, m} (tree build), 7 h (end of PreInteraction), 8 the smoothing-length
+    // guess of the current PreInteraction (written by its first pass, read by the later ones)
     void* mir[16] = {nullptr};
     // persistent-kernel work counters and the overflow group list
     int* d_work = nullptr;          // 64 ints: pair-kernel pass p uses [2p] work, [2p+1] ranges left;

@@ -251,29 +251,33 @@ template <int D>
 __device__ void group_box(GroupMisc* gm, const double* xi, bool active, double radius, const Periodic& pb)
 {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    double lo[D], hi[D];
+    // minima and maxima on the ordered-integer images of the doubles (exact, and off the FP64
+    // pipe, which runs at 1/64 of the FP32 rate)
+    const long long top = dbl_to_ord(1.7976931348623157e308), bottom = dbl_to_ord(-1.7976931348623157e308);
+    long long lo[D], hi[D];
 #pragma unroll
     for (int k = 0; k < D; ++k) {
-        lo[k] = active ? xi[k] : 1.7976931348623157e308;
-        hi[k] = active ? xi[k] : -1.7976931348623157e308;
+        const long long o = dbl_to_ord(xi[k]);
+        lo[k] = active ? o : top;
+        hi[k] = active ? o : bottom;
     }
-    double rr = active ? radius : 0.0;
-    double rm = active ? radius : 1.7976931348623157e308;
+    long long rr = active ? dbl_to_ord(radius) : 0;
+    long long rm = active ? dbl_to_ord(radius) : top;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
 #pragma unroll
         for (int k = 0; k < D; ++k) {
-            lo[k] = fmin(lo[k], __shfl_xor_sync(FULL, lo[k], o));
-            hi[k] = fmax(hi[k], __shfl_xor_sync(FULL, hi[k], o));
+            lo[k] = min(lo[k], __shfl_xor_sync(FULL, lo[k], o));
+            hi[k] = max(hi[k], __shfl_xor_sync(FULL, hi[k], o));
         }
-        rr = fmax(rr, __shfl_xor_sync(FULL, rr, o));
-        rm = fmin(rm, __shfl_xor_sync(FULL, rm, o));
+        rr = max(rr, __shfl_xor_sync(FULL, rr, o));
+        rm = min(rm, __shfl_xor_sync(FULL, rm, o));
     }
     if (lane == 0) {
 #pragma unroll
-        for (int k = 0; k < D; ++k) { gm->wred[w][k] = lo[k]; gm->wred[w][3 + k] = hi[k]; }
-        gm->wred[w][6] = rr;
-        gm->wred[w][7] = rm;
+        for (int k = 0; k < D; ++k) { gm->wred[w][k] = ord_to_dbl(lo[k]); gm->wred[w][3 + k] = ord_to_dbl(hi[k]); }
+        gm->wred[w][6] = ord_to_dbl(rr);
+        gm->wred[w][7] = ord_to_dbl(rm);
     }
     __syncthreads();
     if (threadIdx.x == 0) {

@@ -40,6 +40,7 @@ struct PreArgs {
     const double* dt_run;
     long long* hvs;
     int* newton_fail;
+    double* hguess;   // per-particle guess: the first pass stores it, later passes reuse it
 };
 
 template <int D>
@@ -75,7 +76,15 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
 #pragma unroll
         for (int k = 0; k < D; ++k) xi[k] = st.f[F_POS + k][i];
         const double mi = st.f[F_MASS][i];
-        const double hg = h_guess<D>((double)a.nn, mi, st.f[F_DENS][i]);
+        // the guess (FP64 pow / sqrt) once per particle and stage: passes after the first take
+        // the value the first pass stored (it takes every target before any later pass runs)
+        double hg;
+        if (a.work.list == nullptr) {
+            hg = h_guess<D>((double)a.nn, mi, st.f[F_DENS][i]);
+            if (active) a.hguess[i] = hg;
+        } else {
+            hg = a.hguess[i];
+        }
         const double hs = a.initial ? hg : hg * a.ratio;
         group_box<D>(gm, xi, active, hs, a.pb);
         const int run = st.run[gb];
@@ -284,9 +293,10 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
         }
         // h / v_sig minimum of the group -> run minimum (TimeStep input)
         {
-            double hv = active ? (double)(hT / vsig) : 1.7976931348623157e308;
-            for (int o = 16; o > 0; o >>= 1) hv = fmin(hv, __shfl_xor_sync(FULL, hv, o));
-            if ((t & 31) == 0) atomicMin(&a.hvs[run], dbl_to_ord(hv));
+            // minimum over the warp in T, converted once (the minimum commutes with the conversion)
+            T hv = active ? hT / vsig : T(3.0e38f);
+            for (int o = 16; o > 0; o >>= 1) { const T u = __shfl_xor_sync(FULL, hv, o); hv = u < hv ? u : hv; }
+            if ((t & 31) == 0) atomicMin(&a.hvs[run], dbl_to_ord((double)hv));
         }
 
         if (TYPE == 2) {
@@ -454,6 +464,7 @@ void run_pre(Ctx& c, bool initial)
     a.dt_run = c.d_dt;
     a.hvs = c.d_hvs;
     a.newton_fail = c.d_newton_fail;
+    a.hguess = (double*)c.mir[8];
     const int tcap = c.tile_cap_pre ? c.tile_cap_pre : default_tile_cap<D>();
     launch_pair_passes<PreArgs<T>>(c, (const void*)kern, a, tcap, sizeof(V4), sizeof(T),
         [](const void* k, int grid, int block, size_t smem, cudaStream_t st, PreArgs<T>& args) {
