@@ -176,6 +176,8 @@ struct MaskIter {
     }
     // drop the source last returned by next() from the stored mask
     __device__ __forceinline__ void clear_current() { mask[w * gt + t] &= ~(1u << b); }
+    // drop source s (returned by an earlier next()) from the stored mask
+    __device__ __forceinline__ void clear(int s) { mask[(s >> 5) * gt + t] &= ~(1u << (s & 31)); }
 };
 
 // Work distribution.  A work item is a range of key-consecutive targets (begin, count).  The

@@ -208,15 +208,23 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
             const double hf2 = __dmul_rn(hf, hf);
             const double band = r2_band<T, D>(gm, hf);
             const T lo_t = to_T_down<T>(hf2 - band), hi_t = to_T_up<T>(hf2 + band);
+            // the next candidate's velocity record is loaded before the current one is evaluated
             MaskIter it(tile.mask, GT, t, nw);
-            int s;
-            while (it.next(s)) {
+            int snext;
+            bool have = it.next(snext);
+            V4 vq{};
+            if (have && !a.initial) vq = a.mvel[tile.idx[snext]];
+            while (have) {
+                const int s = snext;
+                const V4 vjr = vq;
+                have = it.next(snext);
+                if (have && !a.initial) vq = a.mvel[tile.idx[snext]];
                 const V4 p = tile.pm[s];
                 T r[D];
                 const T r2 = tile_r2<D, T>(xo, p, r);
                 bool in = r2 < lo_t;
                 if (!in && r2 <= hi_t) in = __dsqrt_rn(exact_r2<D>(st, xi, tile.idx[s], a.pb)) < hf;
-                if (!in) { it.clear_current(); continue; }
+                if (!in) { it.clear(s); continue; }
                 ++nnb;
                 const int j = tile.idx[s];
                 const T rr = sqrt(r2);
@@ -235,7 +243,7 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
                     }
                 }
                 if (!a.initial && j != i) {
-                    const V4 vj = a.mvel[j];
+                    const V4 vj = vjr;
                     T vij[3] = {T(0), T(0), T(0)};
                     vij[0] = vi[0] - vj.x;
                     if (D > 1) vij[1] = vi[1] - vj.y;
