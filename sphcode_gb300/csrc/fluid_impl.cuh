@@ -111,13 +111,15 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
         // Relative guard band of the T-precision test r^2 < H^2 for H = max(h_i, h_j) >= h_min
         // of the group: the component error E (comp_err) at separations ~H is below e_rel H, so
         // |r2_T - r2| < delta H^2 there.
-        double delta;
+        // (in the FP32 form formed in FP32 and widened by 0.1 %: a wider band only sends more
+        // pairs to the exact test, and an FP64 divide per target costs 1/64-rate cycles)
+        T delta;
         {
-            const double hm = gm->rmin;
-            const double e_rel = comp_err<T>(gm, hm) / hm + Unit<T>::u * 3.0;
-            delta = 2.0 * (2.0 * 1.7320508075688772 * e_rel + D * e_rel * e_rel + 8.0 * Unit<T>::u);
+            const T hm = (T)gm->rmin;
+            const T e_rel = (T)comp_err<T>(gm, gm->rmin) / hm * T(1.001) + (T)(Unit<T>::u * 3.0);
+            delta = T(2.002) * (T(2.0 * 1.7320508075688772) * e_rel + T(D) * e_rel * e_rel + (T)(8.0 * Unit<T>::u));
         }
-        const T dlo = (T)(1.0 - delta), dhi = (T)(1.0 + delta);
+        const T dlo = T(1) - delta, dhi = T(1) + delta;
 
         T xo[D];
 #pragma unroll

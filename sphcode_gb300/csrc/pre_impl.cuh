@@ -41,6 +41,7 @@ struct PreArgs {
     long long* hvs;
     int* newton_fail;
     double* hguess;   // per-particle guess: the first pass stores it, later passes reuse it
+    double nn_over_a; // neighborNumber / A_D
 };
 
 template <int D>
@@ -131,7 +132,8 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
         // ---- smoothing length: Newton-Raphson on rho h^D = b (or n h^D = b for disph) ----
         double h = hg;
         if (!a.initial && a.iterative) {
-            const T bconst = (T)((TYPE == 1) ? a.nn / A : mi * a.nn / A);
+            // N / A_D is a constant: one FP64 division per launch, not per target
+            const T bconst = (T)((TYPE == 1) ? a.nn_over_a : mi * a.nn_over_a);
             bool done = !active, conv = false;
             for (int it = 0; it < 10; ++it) {
                 if (!__any_sync(FULL, !done)) break;
@@ -186,7 +188,7 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
 
         // ---- density, pressure, grad-h, signal velocity over {r < h} ----
         const T hT = (T)hf;
-        const T hinvT = (T)(1.0 / hf);
+        const T hinvT = T(1) / hT;   // in the pair type (the FP64 divide costs 1/64-rate cycles)
         const T ciT = a.mvel[i].w;
         const T uiT = a.mu[i];
         T vi[3] = {T(0), T(0), T(0)};
@@ -375,7 +377,7 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
             T div = (T)sdiv.get();
             T rot[3] = {(T)srot[0].get(), (T)srot[1].get(), (T)srot[2].get()};
             if (TYPE == 1) {
-                const T p_inv = (T)((a.gamma - 1.0) / pres);
+                const T p_inv = (T)(a.gamma - 1.0) / (T)pres;
                 div *= p_inv;
                 for (int k = 0; k < 3; ++k) rot[k] *= p_inv;
             } else {
@@ -473,6 +475,7 @@ void run_pre(Ctx& c, bool initial)
     a.hvs = c.d_hvs;
     a.newton_fail = c.d_newton_fail;
     a.hguess = (double*)c.mir[8];
+    a.nn_over_a = (double)c.p.neighbor_number / volume_const<D>();
     const int tcap = c.tile_cap_pre ? c.tile_cap_pre : default_tile_cap<D>();
     launch_pair_passes<PreArgs<T>>(c, (const void*)kern, a, tcap, sizeof(V4), sizeof(T),
         [](const void* k, int grid, int block, size_t smem, cudaStream_t st, PreArgs<T>& args) {
