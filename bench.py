@@ -160,10 +160,12 @@ def pinned_array(nbytes):
 
 
 # ---- CPU baseline / reference arm ------------------------------------------------------------
-def cpu_reference_run(name, steps, threads):
+def cpu_reference_run(name, steps, threads, warmup=0, budget_s=None):
     """Time the reference's own modules (oracle/_ref, built from the reference sources with the
     reference Makefile's flags) or, where they are not built, the C restatement in oracle/, on
-    the host cores.  Returns (particle-steps/s, kind, sample text, seconds)."""
+    the host cores.  After initialize, `warmup` untimed steps, then up to `steps` timed steps;
+    with `budget_s` the timed loop stops once that many seconds have passed (at least one step).
+    Returns (particle-steps/s, kind, sample text, seconds, timed steps, warm-up steps)."""
     from oracle import pyoracle
     p, f, desc, runs = workload(name)
     kind = "reference" if pyoracle.reference_available("fast") else "port"
@@ -178,6 +180,8 @@ def cpu_reference_run(name, steps, threads):
             sub = {k: np.asarray(v)[begins[r]:begins[r + 1]] for k, v in f.items()}
             sim = pyoracle.OracleSim(p, sub, kind=okind, flavor="fast", threads=threads)
             sim.initialize()
+            for _ in range(warmup):
+                sim.step()
             t0 = time.perf_counter()
             for _ in range(steps):
                 sim.step()
@@ -185,21 +189,33 @@ def cpu_reference_run(name, steps, threads):
             n += sim.n
             sim.close()
         sample = (f"{desc}: the first {ntubes} tubes ({n} particles) one after another, "
-                  f"{steps} timed steps each after an untimed initialize, {threads} OpenMP threads")
-        return n * steps / dt, kind, sample, dt
+                  f"{warmup} untimed and {steps} timed steps each after an untimed initialize, "
+                  f"{threads} OpenMP threads")
+        return n * steps / dt, kind, sample, dt, steps, warmup
     sim = pyoracle.OracleSim(p, f, kind=okind, flavor="fast", threads=threads)
     t0 = time.perf_counter()
     sim.initialize()
     t_init = time.perf_counter() - t0
     t0 = time.perf_counter()
-    for _ in range(steps):
+    done_w = 0
+    for _ in range(warmup):
         sim.step()
+        done_w += 1
+        if budget_s is not None and time.perf_counter() - t0 > 0.5 * budget_s:
+            break
+    t0 = time.perf_counter()
+    done = 0
+    while done < steps:
+        sim.step()
+        done += 1
+        if budget_s is not None and time.perf_counter() - t0 > budget_s:
+            break
     dt = time.perf_counter() - t0
     n = sim.n
     sim.close()
-    sample = (f"{desc}: {n} particles, Solver::initialize ({t_init:.1f} s, untimed) then {steps} "
-              f"timed Solver::integrate steps on {threads} OpenMP threads")
-    return n * steps / dt, kind, sample, dt
+    sample = (f"{desc}: {n} particles, Solver::initialize ({t_init:.1f} s, untimed), {done_w} untimed "
+              f"and {done} timed Solver::integrate steps on {threads} OpenMP threads")
+    return n * done / dt, kind, sample, dt, done, done_w
 
 
 def run_reference_arm(args):
@@ -207,11 +223,13 @@ def run_reference_arm(args):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    steps = max(1, min(args.steps, args.ref_steps))
-    value, kind, sample, secs = cpu_reference_run(args.workload, steps, threads)
+    # --warmup untimed and --steps timed steps of the reference, bounded to about a minute of
+    # timed CPU work (the count actually run is reported)
+    value, kind, sample, secs, steps, warm = cpu_reference_run(args.workload, max(1, args.steps), threads,
+                                                              warmup=args.warmup, budget_s=60.0)
     _, _, desc, _ = workload(args.workload)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "particle-steps/s",
-            "n_gpus": args.gpus, "steps": steps, "warmup": 0, "ms_per_step": secs / steps * 1e3,
+            "n_gpus": args.gpus, "steps": steps, "warmup": warm, "ms_per_step": secs / steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": {"workload": desc},
             "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads,
@@ -500,7 +518,7 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        v, kind, sample, _ = cpu_reference_run(args.workload, args.ref_steps, threads)
+        v, kind, sample, _, _, _ = cpu_reference_run(args.workload, args.ref_steps, threads)
         cpu = {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": kind, "sample": sample}
 
     adjoint = None
