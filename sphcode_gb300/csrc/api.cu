@@ -494,8 +494,10 @@ float time_ms(Ctx& c, F fn, int reps)
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    float best = 1e30f;
-    for (int r = 0; r < reps; ++r) {
+    // minimum over at least `reps` runs and, for short stages, over enough runs to span ~3 ms
+    // (a sub-millisecond stage timed twice picks its schedule on noise)
+    float best = 1e30f, total = 0.f;
+    for (int r = 0; r < 64 && (r < reps || total < 3.0f); ++r) {
         cudaEventRecord(e0, c.stream);
         fn();
         cudaEventRecord(e1, c.stream);
@@ -503,6 +505,7 @@ float time_ms(Ctx& c, F fn, int reps)
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
         best = std::min(best, ms);
+        total += ms;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

@@ -71,8 +71,11 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
         int gb, gn;
         if (!next_group(gm, a.work, gb, gn)) break;
         if (gn == 0) continue;   // the unused half of an unsplit chunk
-        const bool active = t < gn;
-        const int i = gb + (active ? t : 0);
+        // targets interleaved over the CTA's warps (warp w takes every (GT/32)-th target), so
+        // that the warps meet at the next group's barrier with similar amounts of work
+        const int tl = (t & 31) * (GT >> 5) + (t >> 5);
+        const bool active = tl < gn;
+        const int i = gb + (active ? tl : 0);
         double xi[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) xi[k] = st.f[F_POS + k][i];
