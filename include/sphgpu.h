@@ -207,7 +207,10 @@ const char* sphgpu_last_error(const sphgpu_ctx* ctx);
  * 19 AoS record reuse on/off: with 1, sphgpu_download_aos takes the record members outside the
  * layout from the records of the last sphgpu_upload_aos (same stride) instead of copying the
  * caller's buffer to the device first — valid when the caller has not changed those members on
- * the host since that upload (the upload, calculate, download pattern of a Module). */
+ * the host since that upload (the upload, calculate, download pattern of a Module);
+ * 20, 21 (read only) the level limit of the last octree build, and the level limit of the
+ * step builds without gravity (0: all key levels; raised by four whenever a build leaves a node
+ * with more than leafParticleNumber particles unsplit at the limit). */
 int sphgpu_set_tuning(sphgpu_ctx* ctx, int which, int value);
 int sphgpu_get_tuning(sphgpu_ctx* ctx, int which, int* value);
 

@@ -1243,6 +1243,8 @@ int sphgpu_get_tuning(sphgpu_ctx* h, int which, int* value)
     case 12: *value = c.pass2_scale; break;
     case 18: *value = c.fixed_dt ? 1 : 0; break;
     case 19: *value = c.aos_reuse ? 1 : 0; break;
+    case 20: *value = c.tree_levels; break;
+    case 21: *value = c.depth_cap; break;
     case 13: case 14: case 15: case 16: case 17: {
         cudaStreamSynchronize(c.stream);
         cudaMemcpy(value, c.d_work + sphgpu::FAIL_INFO_SLOT + (which - 13), sizeof(int), cudaMemcpyDeviceToHost);

@@ -116,16 +116,21 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
             const double band = r2_band<T, D>(gm, hs);
             const T lo_t = to_T_down<T>(hs2 - band), hi_t = to_T_up<T>(hs2 + band);
             for (int w = 0; w < nw; ++w) {
-                unsigned bits = 0;
+                unsigned bits = 0, band = 0;
                 if (word_box_r2<D, T>(xo, tile, w) <= hi_t) {   // else no source of the word is in
                     const int smax = min(32, ntile - w * 32);
                     for (int b = 0; b < smax; ++b) {
-                        const int s = w * 32 + b;
                         T r[D];
-                        const T r2 = tile_r2<D, T>(xo, tile.pm[s], r);
-                        bool in = r2 < lo_t;
-                        if (!in && r2 <= hi_t) in = exact_r2<D>(st, xi, tile.idx[s], a.pb) < hs2;
-                        if (in) bits |= 1u << b;
+                        const T r2 = tile_r2<D, T>(xo, tile.pm[w * 32 + b], r);
+                        bits |= (unsigned)(r2 < lo_t) << b;
+                        band |= (unsigned)(!(r2 < lo_t) && r2 <= hi_t) << b;
+                    }
+                    // the guard band after the word, as a loop: a test inside the loop above is
+                    // if-converted, which issues the FP64 re-decision for every source
+                    while (band) {
+                        const int b = __ffs(band) - 1;
+                        band &= band - 1;
+                        if (exact_r2<D>(st, xi, tile.idx[w * 32 + b], a.pb) < hs2) bits |= 1u << b;
                     }
                 }
                 tile.mask[w * GT + t] = active ? bits : 0u;
@@ -227,9 +232,10 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
                 const V4 p = tile.pm[s];
                 T r[D];
                 const T r2 = tile_r2<D, T>(xo, p, r);
-                bool in = r2 < lo_t;
-                if (!in && r2 <= hi_t) in = __dsqrt_rn(exact_r2<D>(st, xi, tile.idx[s], a.pb)) < hf;
-                if (!in) { it.clear(s); continue; }
+                if (!(r2 < lo_t)) {
+                    if (r2 > hi_t) { it.clear(s); continue; }
+                    if (!(__dsqrt_rn(exact_r2<D>(st, xi, tile.idx[s], a.pb)) < hf)) { it.clear(s); continue; }
+                }
                 ++nnb;
                 const int j = tile.idx[s];
                 const T rr = sqrt(r2);

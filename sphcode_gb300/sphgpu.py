@@ -31,7 +31,8 @@ STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_NODE_POOL", 4: "ERR_CAPA
 
 TUNING = {"group_warps": 0, "fluid_warps": 1, "gravity_warps": 2, "tile_cap": 3, "autotune": 4,
           "timing": 5, "graph": 6, "graph_kernels": 7, "overflow_pre": 8, "overflow_fluid": 9,
-          "tile_cap_pre": 10, "tune_rejects": 11, "pass2_scale": 12, "fixed_dt": 18, "aos_reuse": 19}
+          "tile_cap_pre": 10, "tune_rejects": 11, "pass2_scale": 12, "fixed_dt": 18, "aos_reuse": 19,
+          "tree_levels": 20, "depth_cap": 21}
 
 
 class SphGpuError(RuntimeError):

@@ -125,3 +125,47 @@ def test_autotuner_picks_a_candidate_and_keeps_results(gpu_lib):
             assert rel_err(tuned.get(name), fixed.get(name)) <= FP32_TOL[name], name
         assert np.array_equal(tuned.get("neighbor"), fixed.get("neighbor")) or \
             np.mean(tuned.get("neighbor") != fixed.get("neighbor")) < 1e-3
+
+
+def test_capped_tree_deepens_on_clustering(gpu_lib):
+    """Without gravity the step builds split at most one level below the initial tree's depth.
+    A cluster that forms later leaves an over-full node at that limit: the neighbour sets stay
+    exact with the capped tree, and the next step raises the limit by four levels."""
+    from oracle import pyoracle
+    from sphcode_gb300 import ics, sphgpu
+    p, f = ics.gresho(32)
+    ref = pyoracle.OracleSim(p, f, kind="port")
+    ref.initialize()
+    pos, sml = ref.get("pos"), ref.get("sml")
+    # squeeze the particles within 0.15 of c into a disc 64 times smaller, away from the cell
+    # boundaries of the capped levels (multiples of 1/32 from -0.5), so one capped leaf holds them
+    c = np.array([0.11, 0.047])
+    inner = np.hypot(pos[:, 0] - c[0], pos[:, 1] - c[1]) < 0.15
+    assert inner.sum() > 2 * p.leaf_num
+    pos[inner, :2] = c + (pos[inner, :2] - c) / 64.0
+    sml[inner] /= 64.0
+    ref.set("pos", pos)
+    ref.set("sml", sml)
+
+    def check_sets(sim):
+        for is_ij in (0, 1):
+            cg, lg = sim.neighbors(is_ij, cap=512)
+            cr, lr = ref.neighbors(is_ij, exhaustive=True, cap=512)
+            assert np.array_equal(cg, cr), f"is_ij={is_ij}: counts differ"
+            for i in range(sim.n):
+                assert set(lg[i, :cg[i]].tolist()) == set(lr[i, :cr[i]].tolist()), i
+
+    with sphgpu.GpuSimulation(p, f, precision="fp64") as sim:
+        sim.initialize()
+        cap0 = sim.get_tuning("depth_cap")
+        assert cap0 > 0
+        sim.set("pos", pos)
+        sim.set("sml", sml)
+        check_sets(sim)
+        assert sim.get_tuning("tree_levels") == cap0
+        sim.step(1)
+        assert sim.get_tuning("depth_cap") == cap0 + 4
+        sim.set("pos", pos)
+        sim.set("sml", sml)
+        check_sets(sim)
+        assert sim.get_tuning("tree_levels") == cap0 + 4
