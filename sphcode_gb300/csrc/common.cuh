@@ -76,13 +76,19 @@ struct TreeView {
     const float* cf[3];
     const float* ef;
     const float* kf;
-    // FP32 copies for the Barnes-Hut walk: centre of mass and geometric centre as two-float
-    // pairs (hi = nearest float, lo = nearest float of the remainder), edge^2 and mass
-    const float* comf[3];
-    const float* comlo[3];
-    const float* clo[3];
-    const float* l2f;
-    const float* massf;
+    // one 64-byte record per node for the Barnes-Hut walk (built with gravity only)
+    const struct GravNode* gn;
+};
+
+// The Barnes-Hut walk's view of a node, loaded with four 16-byte loads: the centre of mass as a
+// two-float pair (hi = nearest float, lo = nearest float of the remainder), edge^2 and mass in
+// FP32, the links, and the geometric centre's offset from the centre of mass (nearest float of
+// the FP64 difference; leaf particles are stored relative to the geometric centre).
+struct __align__(16) GravNode {
+    float4 com;     // {com_hi.x, com_hi.y, com_hi.z, edge^2}
+    float4 comlo;   // {com_lo.x, com_lo.y, com_lo.z, mass}
+    int4 link;      // {first_child, nchild, begin, count}
+    float4 cc;      // {centre - com (x, y, z), 0}
 };
 
 struct Periodic {

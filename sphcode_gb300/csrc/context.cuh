@@ -44,9 +44,7 @@ struct Ctx {
     double *nd_center[3] = {nullptr, nullptr, nullptr}, *nd_edge = nullptr, *nd_mass = nullptr;
     double *nd_com[3] = {nullptr, nullptr, nullptr}, *nd_ksize = nullptr;
     float *nd_cf[3] = {nullptr, nullptr, nullptr}, *nd_ef = nullptr, *nd_kf = nullptr;
-    float *nd_comf[3] = {nullptr, nullptr, nullptr}, *nd_l2f = nullptr;
-    float *nd_comlo[3] = {nullptr, nullptr, nullptr}, *nd_clo[3] = {nullptr, nullptr, nullptr};
-    float* nd_massf = nullptr;
+    GravNode* nd_grav = nullptr;    // Barnes-Hut node records (gravity only)
     int* lvl_start = nullptr;       // device, MAX_LEVELS + 2 entries
     int* lvl_tmp = nullptr;         // per-node child counts of the frontier
     int* chunk_sum = nullptr;       // per-1024-node chunk sums

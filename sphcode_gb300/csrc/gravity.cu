@@ -12,9 +12,11 @@
 // open an inner node continue with its children.  The roots carry zero mass, as in the
 // reference, whose root never receives its mass and centre (src/bhtree.cpp:57,152).
 //
-// FP32 pair form: leaf particles are stored as offsets from their leaf's centre in T, and each
-// lane forms x_i - centre once per leaf in FP64, so pair separations are T differences of
-// small numbers.  FP64 form: separations use the reference's periodic FP64 arithmetic.
+// FP32 pair form: leaf particles are stored as offsets from their leaf's centre in T; a lane
+// forms x_i - centre once per leaf as its (two-float) x_i - com minus the record's centre - com,
+// so pair separations are T differences of small numbers, and sums a leaf's terms before adding
+// them to its compensated totals.  FP64 form: separations use the reference's periodic FP64
+// arithmetic.  Each node is one 64-byte record (GravNode), read with four 16-byte loads.
 #include "context.cuh"
 
 namespace sphgpu {
@@ -126,19 +128,30 @@ __global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
             const int node = e.x;
             const unsigned m = (unsigned)e.y;
             const bool in = (m >> lane) & 1u;
+            // the whole record at once (one latency for the node instead of one per field)
+            const GravNode* gp = tv.gn + node;
+            const int4 link = gp->link;
+            float4 gcom, gcomlo, gcc;
+            if (!exact_pairs) {
+                gcom = gp->com;
+                gcomlo = gp->comlo;
+                gcc = gp->cc;
+            }
             bool open = false;
+            float df[D];
             if (in) {
                 T dT[D];
                 bool decided = false;
                 if (!exact_pairs) {
                     // edge^2 > theta^2 |d|^2 in FP32, certain outside the margin
-                    float df[D], d2f = 0.f;
+                    const float cx[3] = {gcom.x, gcom.y, gcom.z}, cl[3] = {gcomlo.x, gcomlo.y, gcomlo.z};
+                    float d2f = 0.f;
 #pragma unroll
                     for (int k = 0; k < D; ++k) {
-                        df[k] = min_image_f((xf[k] - tv.comf[k][node]) + (xlo[k] - tv.comlo[k][node]), a.pb, k);
+                        df[k] = min_image_f((xf[k] - cx[k]) + (xlo[k] - cl[k]), a.pb, k);
                         d2f = fmaf(df[k], df[k], d2f);
                     }
-                    const float l2 = tv.l2f[node];
+                    const float l2 = gcom.w;
                     const float dabs = sqrtf(d2f);
                     const float u = 5.9604645e-08f;
                     const float margin = theta2f * (8.f * u * dabs * (xmag + dabs) + 8.f * u * d2f) + 8.f * u * l2;
@@ -162,7 +175,7 @@ __global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
                     for (int k = 0; k < D; ++k) dT[k] = (T)d[k];
                 }
                 if (!open) {
-                    const T M = exact_pairs ? (T)tv.mass[node] : (T)tv.massf[node];
+                    const T M = exact_pairs ? (T)tv.mass[node] : (T)gcomlo.w;
                     if (M != T(0)) {
                         // monopole: phi -= G M / r, acc -= d G M / r^3 (src/bhtree.cpp:327-329)
                         T r2 = T(0);
@@ -179,16 +192,24 @@ __global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
             }
             const unsigned om = __ballot_sync(FULL, open);
             if (!om) continue;
-            const int fc = tv.first_child[node];
+            const int fc = link.x;
             if (fc < 0) {
                 if (open) {
-                    const int b = tv.begin[node], cnt = tv.count[node];
+                    const int b = link.z, cnt = link.w;
                     T base[D];
                     if (!exact_pairs) {
+                        // x_i - centre = (x_i - com) - (centre - com)
+                        const float cc[3] = {gcc.x, gcc.y, gcc.z};
 #pragma unroll
-                        for (int k = 0; k < D; ++k)
-                            base[k] = (T)min_image_f((xf[k] - tv.cf[k][node]) + (xlo[k] - tv.clo[k][node]), a.pb, k);
+                        for (int k = 0; k < D; ++k) base[k] = (T)min_image_f(df[k] - cc[k], a.pb, k);
                     }
+                    // the leaf's terms summed plainly, then added to the compensated totals once
+                    T lphi = T(0), lacc[D];
+#pragma unroll
+                    for (int k = 0; k < D; ++k) lacc[k] = T(0);
+                    V4 qn{};
+                    T hn = T(0);
+                    if (!exact_pairs) { qn = a.grel[b]; hn = a.gh[b]; }
                     for (int j = b; j < b + cnt; ++j) {
                         T rv[D], mj, hj;
                         if (exact_pairs) {
@@ -197,12 +218,14 @@ __global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
                             mj = (T)st.f[F_MASS][j];
                             hj = (T)st.f[F_SML][j];
                         } else {
-                            const V4 q = a.grel[j];
+                            // the next particle's record is loaded before this one is evaluated
+                            const V4 q = qn;
+                            hj = hn;
+                            if (j + 1 < b + cnt) { qn = a.grel[j + 1]; hn = a.gh[j + 1]; }
                             rv[0] = base[0] - q.x;
                             if (D > 1) rv[D > 1 ? 1 : 0] = base[D > 1 ? 1 : 0] - q.y;
                             if (D > 2) rv[D > 2 ? 2 : 0] = base[D > 2 ? 2 : 0] - q.z;
                             mj = q.w;
-                            hj = a.gh[j];
                         }
                         T r2 = rv[0] * rv[0];
 #pragma unroll
@@ -221,14 +244,26 @@ __global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
                             gsum = hk_g(r, hiT) + hk_g(r, hj);
                         }
                         const T gm = G * mj * T(0.5);
-                        phi.add(-gm * fsum);
+                        if (exact_pairs) {
+                            phi.add(-gm * fsum);
+                        } else {
+                            lphi -= gm * fsum;
+                        }
                         const T c = gm * gsum;
 #pragma unroll
-                        for (int k = 0; k < D; ++k) acc[k].add(-rv[k] * c);
+                        for (int k = 0; k < D; ++k) {
+                            if (exact_pairs) acc[k].add(-rv[k] * c);
+                            else lacc[k] -= rv[k] * c;
+                        }
+                    }
+                    if (!exact_pairs) {
+                        phi.add(lphi);
+#pragma unroll
+                        for (int k = 0; k < D; ++k) acc[k].add(lacc[k]);
                     }
                 }
             } else {
-                const int nc = tv.nchild[node];
+                const int nc = link.y;
                 if (sp + nc > a.stack_cap) { overflow = true; break; }
                 if (lane < nc) stack[sp + nc - 1 - lane] = make_int2(fc + lane, (int)om);
                 sp += nc;
@@ -264,7 +299,8 @@ void run_gravity(Ctx& c)
     a.gh = gh;
     a.G = c.p.g_constant;
     a.theta2 = c.p.theta * c.p.theta;
-    a.stack_cap = 1024;
+    // deepest stack: 2^D - 1 siblings waiting per level below the root, plus one node's children
+    a.stack_cap = 256;
     a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 0, nullptr, nullptr, 0, nullptr,
                        nullptr, 0, 0, c.d_err, nullptr};
     const int gt = c.group_threads;

@@ -643,7 +643,8 @@ __global__ void compact_groups_kernel(const int* part_begin, const int* part_cou
 // ---- FP32 node copies and leaf-relative particle offsets ------------------------------------
 
 struct NodeMirrors {
-    float *cf[3], *ef, *comf[3], *comlo[3], *clo[3], *l2f, *massf;
+    float *cf[3], *ef;
+    GravNode* grav;
 };
 
 template <int D, typename T>
@@ -656,19 +657,25 @@ __global__ void node_mirror_kernel(State st, const int* node_total_p, TreeView t
 #pragma unroll
         for (int k = 0; k < D; ++k) {
             c[k] = tv.center[k][nd];
-            const float hi = (float)c[k];
-            nm.cf[k][nd] = hi;
-            if (nm.clo[k]) nm.clo[k][nd] = (float)(c[k] - (double)hi);
-            if (nm.comf[k]) {
-                const double cm = tv.com[k][nd];
-                const float chi = (float)cm;
-                nm.comf[k][nd] = chi;
-                nm.comlo[k][nd] = (float)(cm - (double)chi);
-            }
+            nm.cf[k][nd] = (float)c[k];
         }
         nm.ef[nd] = __double2float_ru(tv.edge[nd]);
-        if (nm.l2f) nm.l2f[nd] = (float)(tv.edge[nd] * tv.edge[nd]);
-        if (nm.massf) nm.massf[nd] = (float)tv.mass[nd];
+        if (nm.grav) {
+            GravNode g;
+            float hi[3] = {0.f, 0.f, 0.f}, lo[3] = {0.f, 0.f, 0.f}, cc[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+                const double cm = tv.com[k][nd];
+                hi[k] = (float)cm;
+                lo[k] = (float)(cm - (double)hi[k]);
+                cc[k] = (float)(c[k] - cm);
+            }
+            g.com = make_float4(hi[0], hi[1], hi[2], (float)(tv.edge[nd] * tv.edge[nd]));
+            g.comlo = make_float4(lo[0], lo[1], lo[2], (float)tv.mass[nd]);
+            g.link = make_int4(tv.first_child[nd], tv.nchild[nd], tv.begin[nd], tv.count[nd]);
+            g.cc = make_float4(cc[0], cc[1], cc[2], 0.f);
+            nm.grav[nd] = g;
+        }
         if (tv.first_child[nd] >= 0) continue;
         const int b = tv.begin[nd], e = b + tv.count[nd];
         for (int j = b; j < e; ++j) {
@@ -706,11 +713,9 @@ TreeView tree_view(const Ctx& c)
     t.first_child = c.nd_first;
     t.nchild = c.nd_nchild;
     for (int k = 0; k < 3; ++k) {
-        t.center[k] = c.nd_center[k]; t.com[k] = c.nd_com[k]; t.cf[k] = c.nd_cf[k]; t.comf[k] = c.nd_comf[k];
-        t.comlo[k] = c.nd_comlo[k]; t.clo[k] = c.nd_clo[k];
+        t.center[k] = c.nd_center[k]; t.com[k] = c.nd_com[k]; t.cf[k] = c.nd_cf[k];
     }
-    t.l2f = c.nd_l2f;
-    t.massf = c.nd_massf;
+    t.gn = c.nd_grav;
     t.ef = c.nd_ef;
     t.kf = c.nd_kf;
     t.edge = c.nd_edge;
@@ -744,16 +749,8 @@ int tree_alloc(Ctx& c)
         A((void**)&c.nd_center[k], sizeof(double) * nc);
         A((void**)&c.nd_com[k], sizeof(double) * nc);
         A((void**)&c.nd_cf[k], sizeof(float) * nc);
-        if (c.p.use_gravity) {
-            A((void**)&c.nd_comf[k], sizeof(float) * nc);
-            A((void**)&c.nd_comlo[k], sizeof(float) * nc);
-            A((void**)&c.nd_clo[k], sizeof(float) * nc);
-        }
     }
-    if (c.p.use_gravity) {
-        A((void**)&c.nd_l2f, sizeof(float) * nc);
-        A((void**)&c.nd_massf, sizeof(float) * nc);
-    }
+    if (c.p.use_gravity) A((void**)&c.nd_grav, sizeof(GravNode) * nc);
     A((void**)&c.nd_ef, sizeof(float) * nc);
     A((void**)&c.nd_kf, sizeof(float) * nc);
     A((void**)&c.nd_edge, sizeof(double) * nc);
@@ -789,9 +786,7 @@ void tree_free(Ctx& c)
                     c.nd_center[1], c.nd_center[2], c.nd_com[0], c.nd_com[1], c.nd_com[2],
                     c.nd_edge, c.nd_mass, c.nd_ksize, c.lvl_start, c.lvl_tmp, c.chunk_sum, c.bbox,
                     c.node_total, c.g_begin, c.g_count, c.n_groups, c.nd_cf[0], c.nd_cf[1],
-                    c.nd_cf[2], c.nd_ef, c.nd_kf, c.ck_begin, c.ck_count, c.radix_dtot, c.nd_comf[0], c.nd_comf[1], c.nd_comf[2],
-                    c.nd_l2f, c.nd_comlo[0], c.nd_comlo[1], c.nd_comlo[2], c.nd_clo[0], c.nd_clo[1],
-                    c.nd_clo[2], c.nd_massf, c.part_begin,
+                    c.nd_cf[2], c.nd_ef, c.nd_kf, c.ck_begin, c.ck_count, c.radix_dtot, c.nd_grav, c.part_begin,
                     c.part_count, c.part_n};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -897,11 +892,10 @@ static void make_tree_d(Ctx& c, bool reorder_all, bool full_depth)
     tv = tree_view(c);
     NodeMirrors nm{};
     for (int k = 0; k < 3; ++k) {
-        nm.cf[k] = c.nd_cf[k]; nm.comf[k] = c.nd_comf[k]; nm.comlo[k] = c.nd_comlo[k]; nm.clo[k] = c.nd_clo[k];
+        nm.cf[k] = c.nd_cf[k];
     }
     nm.ef = c.nd_ef;
-    nm.l2f = c.nd_l2f;
-    nm.massf = c.nd_massf;
+    nm.grav = c.nd_grav;
     if (c.precision == SPHGPU_FP32_PAIR)
         node_mirror_kernel<D, float><<<c.num_sms * 8, 128, 0, s>>>(c.st, c.node_total, tv, nm, (float4*)c.mir[6]);
     else
