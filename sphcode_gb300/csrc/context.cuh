@@ -47,6 +47,7 @@ struct Ctx {
     GravNode* nd_grav = nullptr;    // Barnes-Hut node records (gravity only)
     int* lvl_start = nullptr;       // device, MAX_LEVELS + 2 entries
     int* lvl_tmp = nullptr;         // per-node child counts of the frontier
+    int* nd_bnd = nullptr;          // per split node: its inner child boundaries (2^D - 1 ints)
     int* chunk_sum = nullptr;       // per-1024-node chunk sums
     long long* bbox = nullptr;      // per run: D mins then D maxs (ordered-int images)
     int* node_total = nullptr;      // device: number of nodes built

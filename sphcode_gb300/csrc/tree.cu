@@ -269,6 +269,7 @@ __global__ void copy_fields_kernel(FieldMove fm, int n)
 struct NodeArrays {
     int *begin, *count, *first, *nchild, *parent, *level, *arrive;
     double *center[3], *edge;
+    int* bnd;   // per split node, its 2^D - 1 inner child boundaries (found once, used by the next level)
 };
 
 template <int D>
@@ -289,8 +290,85 @@ __device__ __forceinline__ void child_bounds(const unsigned long long* keys, int
     }
 }
 
+// child_bounds of one range by the whole warp (b, cnt and the result are the same in every
+// lane): 32 probes per round narrow each boundary 32-fold, so a range of 2^20 particles takes
+// four rounds of loads per boundary instead of twenty dependent ones.
 template <int D>
-__global__ void level_count_kernel(NodeArrays na, const unsigned long long* keys,
+__device__ __forceinline__ void warp_child_bounds(const unsigned long long* keys, int b, int cnt,
+                                                  int shift, int* bnd)
+{
+    constexpr int NC = 1 << D;
+    const int lane = threadIdx.x & 31;
+    bnd[0] = b;
+    bnd[NC] = b + cnt;
+    int lo = b;
+#pragma unroll
+    for (int c = 1; c < NC; ++c) {
+        int hi = b + cnt;   // first index in [lo, hi) with digit >= c, or hi
+        while (hi - lo > 32) {
+            const int step = (hi - lo + 31) >> 5;
+            const int pos = lo + lane * step;
+            const bool ge = pos >= hi || (int)((keys[pos] >> shift) & (NC - 1)) >= c;
+            const unsigned m = __ballot_sync(FULL, ge);
+            if (m == 0) {
+                lo = lo + 31 * step + 1;
+            } else {
+                const int f = __ffs(m) - 1;
+                if (f == 0) { hi = lo; break; }
+                const int pf = lo + f * step;
+                lo = lo + (f - 1) * step + 1;
+                hi = pf < hi ? pf : hi;
+            }
+        }
+        if (hi > lo) {
+            const int pos = lo + lane;
+            const bool ge = pos >= hi || (int)((keys[pos] >> shift) & (NC - 1)) >= c;
+            const unsigned m = __ballot_sync(FULL, ge);
+            lo = m ? lo + __ffs(m) - 1 : hi;
+        }
+        bnd[c] = lo;
+    }
+}
+
+// Child boundaries for every lane with want set (warp-collective: all 32 lanes call it).  A warp
+// with one or two large ranges searches them together; otherwise each lane searches its own.
+constexpr int WARP_SEARCH_MIN = 4096;
+template <int D>
+__device__ __forceinline__ void find_bounds(const unsigned long long* keys, bool want, int b, int cnt,
+                                            int shift, int* bnd)
+{
+    constexpr int NC = 1 << D;
+    const int lane = threadIdx.x & 31;
+    const bool big = want && cnt > WARP_SEARCH_MIN;
+    const unsigned bm = __ballot_sync(FULL, big);
+    const bool coop = bm != 0 && __popc(bm) <= 2;
+    if (want && !(coop && big)) child_bounds<D>(keys, b, cnt, shift, bnd);
+    __syncwarp();
+    if (coop) {
+        unsigned mm = bm;
+        while (mm) {
+            const int src = __ffs(mm) - 1;
+            mm &= mm - 1;
+            int wb[NC + 1];
+            warp_child_bounds<D>(keys, __shfl_sync(FULL, b, src), __shfl_sync(FULL, cnt, src), shift, wb);
+            if (lane == src) {
+#pragma unroll
+                for (int c = 0; c <= NC; ++c) bnd[c] = wb[c];
+            }
+        }
+    }
+}
+
+template <int D>
+__device__ __forceinline__ void store_bounds(int* buf, int node, const int* bnd)
+{
+    constexpr int NC = 1 << D;
+#pragma unroll
+    for (int c = 1; c < NC; ++c) buf[(size_t)node * (NC - 1) + (c - 1)] = bnd[c];
+}
+
+template <int D>
+__global__ void __launch_bounds__(LEVEL_CHUNK) level_count_kernel(NodeArrays na, const unsigned long long* keys,
                                    const int* lvl_start, int l, int levels, int lv, int leaf_num,
                                    int* lvl_tmp, int* chunk_sum, int* trunc)
 {
@@ -301,15 +379,22 @@ __global__ void level_count_kernel(NodeArrays na, const unsigned long long* keys
     for (int chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
         const int node = s + chunk * LEVEL_CHUNK + threadIdx.x;
         int nc = 0;
+        bool split = false;
+        int b = 0, cnt = 0;
         if (node < e) {
-            const int cnt = na.count[node];
-            const bool split = (l == 1) || (cnt > leaf_num && l <= lv);
+            b = na.begin[node];
+            cnt = na.count[node];
+            split = (l == 1) || (cnt > leaf_num && l <= lv);
             // a node the full build would split, left a leaf by the cap
             if (!split && cnt > leaf_num && l <= levels) atomicOr(trunc, 1);
+        }
+        int bnd[NC + 1];
+        find_bounds<D>(keys, split && cnt > 0, b, cnt, D * (levels - l), bnd);
+        if (node < e) {
             if (split && cnt > 0) {
-                int bnd[NC + 1];
-                child_bounds<D>(keys, na.begin[node], cnt, D * (levels - l), bnd);
+#pragma unroll
                 for (int c = 0; c < NC; ++c) nc += bnd[c + 1] > bnd[c];
+                store_bounds<D>(na.bnd, node, bnd);
             }
             if (!split) { na.first[node] = -1; na.nchild[node] = 0; }
             lvl_tmp[node - s] = nc;
@@ -336,7 +421,7 @@ __global__ void level_count_kernel(NodeArrays na, const unsigned long long* keys
 // tmp_next / cs_next for level l + 1 and clears cs_clear, the totals the launch after it fills.
 // Node indices are breadth-first and, within a level, in key order.
 template <int D>
-__global__ void level_build_kernel(NodeArrays na, const unsigned long long* keys, int n, int* lvl_start, int l,
+__global__ void __launch_bounds__(LEVEL_CHUNK) level_build_kernel(NodeArrays na, const unsigned long long* keys, int n, int* lvl_start, int l,
                                    int levels, int lv, int leaf_num, const int* tmp_cur, int* tmp_next,
                                    const int* cs_cur, int* cs_next, int* cs_clear, int cs_cap, int node_cap,
                                    unsigned* err, int* trunc)
@@ -387,7 +472,10 @@ __global__ void level_build_kernel(NodeArrays na, const unsigned long long* keys
         if (node < e && nc > 0) {
             const int b = na.begin[node], cnt = na.count[node];
             int bnd[NC + 1];
-            child_bounds<D>(keys, b, cnt, D * (levels - l), bnd);
+            bnd[0] = b;
+            bnd[NC] = b + cnt;
+#pragma unroll
+            for (int c = 1; c < NC; ++c) bnd[c] = na.bnd[(size_t)node * (NC - 1) + (c - 1)];
             const int fc = cbase + off;
             if (fc + nc > node_cap) {
                 atomicOr(err, (unsigned)ERR_NODE_POOL);
@@ -426,20 +514,33 @@ __global__ void level_build_kernel(NodeArrays na, const unsigned long long* keys
         const int q0 = (c0 - cbase) / LEVEL_CHUNK;   // first next-level chunk touched
         if (threadIdx.x < NC + 2) agg[threadIdx.x] = 0;
         __syncthreads();
-        for (int ci = c0 + threadIdx.x; ci < c1; ci += blockDim.x) {
-            const int cb = na.begin[ci], ccnt = na.count[ci];
-            int ncc = 0;
-            // slots of a parent the node pool could not hold were not written (the error bit is set)
-            if (cb < 0 || ccnt < 0 || cb + ccnt > n) { tmp_next[ci - cbase] = 0; continue; }
-            const bool split = ccnt > leaf_num && lc <= lv;
-            if (!split && ccnt > leaf_num && lc <= levels) atomicOr(trunc, 1);
-            if (split) {
-                int cbnd[NC + 1];
-                child_bounds<D>(keys, cb, ccnt, D * (levels - lc), cbnd);
-                for (int g = 0; g < NC; ++g) ncc += cbnd[g + 1] > cbnd[g];
+        // children spread over the warps (the first 32 to lane 0 of each warp), so that the few
+        // large ranges of the upper levels are searched by separate warps
+        const int spread = (threadIdx.x & 31) * (blockDim.x >> 5) + (threadIdx.x >> 5);
+        for (int base = c0; base < c1; base += blockDim.x) {
+            const int ci = base + spread;
+            bool valid = ci < c1;
+            int cb = 0, ccnt = 0;
+            if (valid) {
+                cb = na.begin[ci];
+                ccnt = na.count[ci];
+                // slots of a parent the node pool could not hold were not written (the error bit is set)
+                if (cb < 0 || ccnt < 0 || cb + ccnt > n) { tmp_next[ci - cbase] = 0; valid = false; }
             }
-            tmp_next[ci - cbase] = ncc;
-            if (ncc) atomicAdd(&agg[(ci - cbase) / LEVEL_CHUNK - q0], ncc);
+            const bool split = valid && ccnt > leaf_num && lc <= lv;
+            if (valid && !split && ccnt > leaf_num && lc <= levels) atomicOr(trunc, 1);
+            int cbnd[NC + 1];
+            find_bounds<D>(keys, split, cb, ccnt, D * (levels - lc), cbnd);
+            if (valid) {
+                int ncc = 0;
+                if (split) {
+#pragma unroll
+                    for (int g = 0; g < NC; ++g) ncc += cbnd[g + 1] > cbnd[g];
+                    store_bounds<D>(na.bnd, ci, cbnd);
+                }
+                tmp_next[ci - cbase] = ncc;
+                if (ncc) atomicAdd(&agg[(ci - cbase) / LEVEL_CHUNK - q0], ncc);
+            }
         }
         __syncthreads();
         // at most NC * LEVEL_CHUNK children from one chunk: they touch at most NC + 1 chunks
@@ -529,76 +630,74 @@ __global__ void com_finalize_kernel(const int* node_total_p, int R, const double
 
 // ---- target groups ----------------------------------------------------------------------------
 // Each fixed chunk of key-consecutive particles is split at the highest key bit in which its
-// first and last particle differ whenever both halves are less than half as wide as the whole
-// (the chunk straddles an octree boundary), recursively up to GROUP_SPLIT_DEPTH times; the parts
-// are then compacted into the group list in chunk order.
-constexpr int GROUP_SPLIT_DEPTH = 1;
-constexpr int GROUP_PARTS = 1 << GROUP_SPLIT_DEPTH;
-
-template <int D>
-__device__ double range_extent(const State& st, int b, int e)
-{
-    double ext = 0.0;
-#pragma unroll
-    for (int k = 0; k < D; ++k) {
-        double lo = 1.7976931348623157e308, hi = -lo;
-        for (int i = b; i < e; ++i) {
-            const double x = st.f[F_POS + k][i];
-            lo = fmin(lo, x);
-            hi = fmax(hi, x);
-        }
-        ext = fmax(ext, hi - lo);
-    }
-    return ext;
-}
+// first and last particle differ when both halves are less than half as wide as the whole (the
+// chunk straddles an octree boundary); the parts are then compacted into the group list in chunk
+// order.  One warp per chunk: the lanes take the particles in turn and the extents are minima and
+// maxima of the ordered-integer images of the coordinates (exact, and off the FP64 pipe).
+constexpr int GROUP_PARTS = 2;
 
 template <int D>
 __global__ void split_groups_kernel(State st, const unsigned long long* keys, const int* ck_begin,
                                     const int* ck_count, int nchunks, int* part_begin, int* part_count,
                                     int* nparts)
 {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= nchunks) return;
-    int pb[GROUP_PARTS], pe[GROUP_PARTS], pd[GROUP_PARTS];
-    int np = 0, out = 0;
-    int ob[GROUP_PARTS], oc[GROUP_PARTS];
-    pb[0] = ck_begin[c];
-    pe[0] = pb[0] + ck_count[c];
-    pd[0] = 0;
-    np = 1;
-    while (np > 0) {
-        --np;
-        const int b = pb[np], e = pe[np], d = pd[np];
-        int s = e;
-        const unsigned long long diff = keys[b] ^ keys[e - 1];
-        if (diff && d < GROUP_SPLIT_DEPTH && e - b > 1) {
-            const unsigned long long bit = 1ull << (63 - __clzll((long long)diff));
-            int lo = b, hi = e - 1;   // first index with the bit set
-            while (lo < hi) {
-                const int mid = (lo + hi) >> 1;
-                if (keys[mid] & bit) hi = mid; else lo = mid + 1;
-            }
-            if (lo > b) {
-                const double ext = range_extent<D>(st, b, e);
-                const double ea = range_extent<D>(st, b, lo), eb = range_extent<D>(st, lo, e);
-                if (fmax(ea, eb) < 0.5 * ext) s = lo;
-            }
+    const int lane = threadIdx.x & 31;
+    const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (c >= nchunks) return;   // whole warps
+    const int b = ck_begin[c], e = b + ck_count[c];
+    int s = e;
+    const unsigned long long diff = e - b > 1 ? keys[b] ^ keys[e - 1] : 0ull;
+    if (diff) {
+        const unsigned long long bit = 1ull << (63 - __clzll((long long)diff));
+        int lo = b, hi = e - 1;   // first index with the bit set
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (keys[mid] & bit) hi = mid; else lo = mid + 1;
         }
+        if (lo > b) {
+            const long long top = dbl_to_ord(1.7976931348623157e308), bottom = dbl_to_ord(-1.7976931348623157e308);
+            long long mn[2][D], mx[2][D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) { mn[0][k] = mn[1][k] = top; mx[0][k] = mx[1][k] = bottom; }
+            for (int i = b + lane; i < e; i += 32) {
+                const int h = i >= lo;
+#pragma unroll
+                for (int k = 0; k < D; ++k) {
+                    const long long o = dbl_to_ord(st.f[F_POS + k][i]);
+                    mn[h][k] = min(mn[h][k], o);
+                    mx[h][k] = max(mx[h][k], o);
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+#pragma unroll
+                    for (int k = 0; k < D; ++k) {
+                        mn[h][k] = min(mn[h][k], __shfl_xor_sync(FULL, mn[h][k], o));
+                        mx[h][k] = max(mx[h][k], __shfl_xor_sync(FULL, mx[h][k], o));
+                    }
+                }
+            }
+            double ext = 0.0, ea = 0.0, eb = 0.0;
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+                ea = fmax(ea, ord_to_dbl(mx[0][k]) - ord_to_dbl(mn[0][k]));
+                eb = fmax(eb, ord_to_dbl(mx[1][k]) - ord_to_dbl(mn[1][k]));
+                ext = fmax(ext, ord_to_dbl(max(mx[0][k], mx[1][k])) - ord_to_dbl(min(mn[0][k], mn[1][k])));
+            }
+            if (fmax(ea, eb) < 0.5 * ext) s = lo;
+        }
+    }
+    if (lane == 0) {
+        part_begin[(size_t)c * GROUP_PARTS] = b;
+        part_count[(size_t)c * GROUP_PARTS] = s - b;
         if (s < e) {
-            // second half first on the stack so that parts come out in key order
-            pb[np] = s; pe[np] = e; pd[np] = d + 1; ++np;
-            pb[np] = b; pe[np] = s; pd[np] = d + 1; ++np;
-        } else {
-            ob[out] = b;
-            oc[out] = e - b;
-            ++out;
+            part_begin[(size_t)c * GROUP_PARTS + 1] = s;
+            part_count[(size_t)c * GROUP_PARTS + 1] = e - s;
         }
+        nparts[c] = s < e ? 2 : 1;
     }
-    for (int q = 0; q < out; ++q) {
-        part_begin[(size_t)c * GROUP_PARTS + q] = ob[q];
-        part_count[(size_t)c * GROUP_PARTS + q] = oc[q];
-    }
-    nparts[c] = out;
 }
 
 // Exclusive scan of the per-chunk part counts in one block; total to *n_groups.
@@ -758,6 +857,7 @@ int tree_alloc(Ctx& c)
     A((void**)&c.nd_ksize, sizeof(double) * nc);
     A((void**)&c.lvl_start, sizeof(int) * (MAX_LEVELS + 2));
     A((void**)&c.lvl_tmp, sizeof(int) * 2 * (size_t)nc);
+    A((void**)&c.nd_bnd, sizeof(int) * ((1 << c.dim) - 1) * nc);
     A((void**)&c.chunk_sum, sizeof(int) * 3 * (size_t)(ceil_div(nc, LEVEL_CHUNK) + 1));
     A((void**)&c.bbox, sizeof(long long) * 2 * 3 * c.R);
     A((void**)&c.node_total, sizeof(int));
@@ -786,7 +886,7 @@ void tree_free(Ctx& c)
                     c.nd_center[1], c.nd_center[2], c.nd_com[0], c.nd_com[1], c.nd_com[2],
                     c.nd_edge, c.nd_mass, c.nd_ksize, c.lvl_start, c.lvl_tmp, c.chunk_sum, c.bbox,
                     c.node_total, c.g_begin, c.g_count, c.n_groups, c.nd_cf[0], c.nd_cf[1],
-                    c.nd_cf[2], c.nd_ef, c.nd_kf, c.ck_begin, c.ck_count, c.radix_dtot, c.nd_grav, c.part_begin,
+                    c.nd_cf[2], c.nd_ef, c.nd_kf, c.ck_begin, c.ck_count, c.radix_dtot, c.nd_grav, c.nd_bnd, c.part_begin,
                     c.part_count, c.part_n};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -865,6 +965,7 @@ static void make_tree_d(Ctx& c, bool reorder_all, bool full_depth)
     na.parent = c.nd_parent; na.level = c.nd_level; na.arrive = c.nd_arrive;
     for (int k = 0; k < 3; ++k) na.center[k] = c.nd_center[k];
     na.edge = c.nd_edge;
+    na.bnd = c.nd_bnd;
     const int grid = std::max(1, std::min(c.num_sms * 4, ceil_div(c.node_cap, LEVEL_CHUNK)));
     {
         // child counts of the roots, then one launch per level (children of level l and their counts)
@@ -882,7 +983,7 @@ static void make_tree_d(Ctx& c, bool reorder_all, bool full_depth)
     }
     cudaMemcpyAsync(c.node_total, c.lvl_start + lv + 2, sizeof(int), cudaMemcpyDeviceToDevice, s);
     if (c.p.use_gravity) launch_node_moments(c);   // node masses and centres of mass serve gravity only
-    split_groups_kernel<D><<<ceil_div(c.num_chunks, 128), 128, 0, s>>>(c.st, c.keys, c.ck_begin, c.ck_count,
+    split_groups_kernel<D><<<ceil_div(c.num_chunks, 8), 256, 0, s>>>(c.st, c.keys, c.ck_begin, c.ck_count,
                                                                    c.num_chunks, c.part_begin, c.part_count,
                                                                    c.part_n);
     scan_parts_kernel<<<1, 1024, 0, s>>>(c.part_n, c.num_chunks, c.n_groups);

@@ -169,3 +169,18 @@ def test_capped_tree_deepens_on_clustering(gpu_lib):
         sim.set("sml", sml)
         check_sets(sim)
         assert sim.get_tuning("tree_levels") == cap0 + 4
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_tree_shape(gpu_lib, case):
+    """Node and leaf counts per level of the initial octree equal the reference's recursive build
+    (BHNode::create_tree, src/bhtree.cpp:136-204)."""
+    from oracle import pyoracle
+    from sphcode_gb300 import sphgpu
+    p, f = _cases()[case]()
+    ref = pyoracle.OracleSim(p, f, kind="port")
+    ref.initialize()
+    with sphgpu.GpuSimulation(p, f, precision="fp32") as sim:
+        sim.initialize()
+        got, want = sim.tree_stats(), ref.tree_stats()
+        assert np.array_equal(got, want), (case, got[:2], want[:2], np.nonzero(got != want)[0][:8])
