@@ -367,23 +367,32 @@ __device__ __forceinline__ void store_bounds(int* buf, int node, const int* bnd)
     for (int c = 1; c < NC; ++c) buf[(size_t)node * (NC - 1) + (c - 1)] = bnd[c];
 }
 
+// Split decision (src/bhtree.cpp:154-158), child boundaries and child count of every level-l node,
+// with the per-chunk (LEVEL_CHUNK nodes) totals accumulated into chunk_sum (zeroed beforehand).
+// Blocks of COUNT_THREADS threads take sub-chunks of as many nodes, spread over the block's warps
+// (the first nodes to lane 0 of each warp), so that the few large ranges of the upper levels are
+// searched by separate warps.
+constexpr int COUNT_THREADS = 256;
 template <int D>
-__global__ void __launch_bounds__(LEVEL_CHUNK) level_count_kernel(NodeArrays na, const unsigned long long* keys,
-                                   const int* lvl_start, int l, int levels, int lv, int leaf_num,
+__global__ void __launch_bounds__(COUNT_THREADS) level_count_kernel(NodeArrays na, const unsigned long long* keys,
+                                   int n, const int* lvl_start, int l, int levels, int lv, int leaf_num,
                                    int* lvl_tmp, int* chunk_sum, int* trunc)
 {
     constexpr int NC = 1 << D;
-    __shared__ int red[32];
+    __shared__ int red[COUNT_THREADS / 32];
     const int s = lvl_start[l], e = lvl_start[l + 1];
-    const int nchunks = (e - s + LEVEL_CHUNK - 1) / LEVEL_CHUNK;
-    for (int chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
-        const int node = s + chunk * LEVEL_CHUNK + threadIdx.x;
+    const int nsub = (e - s + COUNT_THREADS - 1) / COUNT_THREADS;
+    const int spread = (threadIdx.x & 31) * (COUNT_THREADS / 32) + (threadIdx.x >> 5);
+    for (int sub = blockIdx.x; sub < nsub; sub += gridDim.x) {
+        const int node = s + sub * COUNT_THREADS + spread;
         int nc = 0;
         bool split = false;
         int b = 0, cnt = 0;
         if (node < e) {
             b = na.begin[node];
             cnt = na.count[node];
+            // slots of a parent the node pool could not hold were not written (the error bit is set)
+            if (b < 0 || cnt < 0 || b + cnt > n) { b = 0; cnt = 0; }
             split = (l == 1) || (cnt > leaf_num && l <= lv);
             // a node the full build would split, left a leaf by the cap
             if (!split && cnt > leaf_num && l <= levels) atomicOr(trunc, 1);
@@ -399,37 +408,35 @@ __global__ void __launch_bounds__(LEVEL_CHUNK) level_count_kernel(NodeArrays na,
             if (!split) { na.first[node] = -1; na.nchild[node] = 0; }
             lvl_tmp[node - s] = nc;
         }
-        // block sum
+        // block sum into the chunk's total (a sub-chunk lies within one chunk)
         int v = nc;
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
         if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
         __syncthreads();
         if (threadIdx.x < 32) {
-            int u = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0;
+            int u = threadIdx.x < COUNT_THREADS / 32 ? red[threadIdx.x] : 0;
             for (int o = 16; o > 0; o >>= 1) u += __shfl_xor_sync(FULL, u, o);
-            if (threadIdx.x == 0) chunk_sum[chunk] = u;
+            if (threadIdx.x == 0 && u) atomicAdd(&chunk_sum[(sub * COUNT_THREADS) / LEVEL_CHUNK], u);
         }
         __syncthreads();
     }
 }
 
 
-// One launch per level: emits the children of the level-l nodes (level l + 1: begin, count,
-// centre, edge, parent) and, for each child, its own split decision and child count, so that the
-// next launch can place the grandchildren.  tmp_cur / cs_cur hold the child counts of the level-l
-// nodes and their per-chunk totals (accumulated by the previous launch); this launch accumulates
-// tmp_next / cs_next for level l + 1 and clears cs_clear, the totals the launch after it fills.
-// Node indices are breadth-first and, within a level, in key order.
+// One launch per level: places the children of the level-l nodes (level l + 1: begin, count,
+// centre, edge, parent) from the child counts and boundaries that level_count_kernel found.
+// tmp_cur / cs_cur hold the child counts of the level-l nodes and their per-chunk totals; the
+// launch also clears cs_clear, the totals that the count of level l + 2 fills.  Node indices are
+// breadth-first and, within a level, in key order.
 template <int D>
-__global__ void __launch_bounds__(LEVEL_CHUNK) level_build_kernel(NodeArrays na, const unsigned long long* keys, int n, int* lvl_start, int l,
-                                   int levels, int lv, int leaf_num, const int* tmp_cur, int* tmp_next,
-                                   const int* cs_cur, int* cs_next, int* cs_clear, int cs_cap, int node_cap,
-                                   unsigned* err, int* trunc)
+__global__ void __launch_bounds__(LEVEL_CHUNK) level_build_kernel(NodeArrays na, int* lvl_start, int l,
+                                                                  const int* tmp_cur, const int* cs_cur,
+                                                                  int* cs_clear, int cs_cap, int node_cap,
+                                                                  unsigned* err)
 {
     constexpr int NC = 1 << D;
     __shared__ int sc[LEVEL_CHUNK];
     __shared__ int red[32];
-    __shared__ int agg[NC + 2];   // child totals per next-level chunk touched by this chunk's children
     const int s = lvl_start[l], e = lvl_start[l + 1];
     const int nchunks = (e - s + LEVEL_CHUNK - 1) / LEVEL_CHUNK;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < cs_cap; q += gridDim.x * blockDim.x) cs_clear[q] = 0;
@@ -467,7 +474,6 @@ __global__ void __launch_bounds__(LEVEL_CHUNK) level_build_kernel(NodeArrays na,
             __syncthreads();
         }
         const int off = sc[threadIdx.x] - nc + chunk_off;
-        const int chunk_children = sc[LEVEL_CHUNK - 1];
         __syncthreads();
         if (node < e && nc > 0) {
             const int b = na.begin[node], cnt = na.count[node];
@@ -506,46 +512,6 @@ __global__ void __launch_bounds__(LEVEL_CHUNK) level_build_kernel(NodeArrays na,
                 }
             }
         }
-        __syncthreads();
-        // the children of this chunk's nodes are consecutive: one thread per child for its split
-        // decision (src/bhtree.cpp:154-158) and child count
-        const int lc = l + 1;
-        const int c0 = cbase + chunk_off, c1 = min(c0 + chunk_children, node_cap);
-        const int q0 = (c0 - cbase) / LEVEL_CHUNK;   // first next-level chunk touched
-        if (threadIdx.x < NC + 2) agg[threadIdx.x] = 0;
-        __syncthreads();
-        // children spread over the warps (the first 32 to lane 0 of each warp), so that the few
-        // large ranges of the upper levels are searched by separate warps
-        const int spread = (threadIdx.x & 31) * (blockDim.x >> 5) + (threadIdx.x >> 5);
-        for (int base = c0; base < c1; base += blockDim.x) {
-            const int ci = base + spread;
-            bool valid = ci < c1;
-            int cb = 0, ccnt = 0;
-            if (valid) {
-                cb = na.begin[ci];
-                ccnt = na.count[ci];
-                // slots of a parent the node pool could not hold were not written (the error bit is set)
-                if (cb < 0 || ccnt < 0 || cb + ccnt > n) { tmp_next[ci - cbase] = 0; valid = false; }
-            }
-            const bool split = valid && ccnt > leaf_num && lc <= lv;
-            if (valid && !split && ccnt > leaf_num && lc <= levels) atomicOr(trunc, 1);
-            int cbnd[NC + 1];
-            find_bounds<D>(keys, split, cb, ccnt, D * (levels - lc), cbnd);
-            if (valid) {
-                int ncc = 0;
-                if (split) {
-#pragma unroll
-                    for (int g = 0; g < NC; ++g) ncc += cbnd[g + 1] > cbnd[g];
-                    store_bounds<D>(na.bnd, ci, cbnd);
-                }
-                tmp_next[ci - cbase] = ncc;
-                if (ncc) atomicAdd(&agg[(ci - cbase) / LEVEL_CHUNK - q0], ncc);
-            }
-        }
-        __syncthreads();
-        // at most NC * LEVEL_CHUNK children from one chunk: they touch at most NC + 1 chunks
-        if (threadIdx.x < NC + 2 && agg[threadIdx.x]) atomicAdd(&cs_next[q0 + threadIdx.x], agg[threadIdx.x]);
-        __syncthreads();
     }
 }
 
@@ -967,19 +933,22 @@ static void make_tree_d(Ctx& c, bool reorder_all, bool full_depth)
     na.edge = c.nd_edge;
     na.bnd = c.nd_bnd;
     const int grid = std::max(1, std::min(c.num_sms * 4, ceil_div(c.node_cap, LEVEL_CHUNK)));
+    const int cgrid = std::max(1, std::min(c.num_sms * 16, ceil_div(c.node_cap, COUNT_THREADS)));
     {
         // child counts of the roots, then one launch per level (children of level l and their counts)
         const int cs_cap = ceil_div(c.node_cap, LEVEL_CHUNK) + 1;
         int* tmp[2] = {c.lvl_tmp, c.lvl_tmp + c.node_cap};
         int* cs[3] = {c.chunk_sum, c.chunk_sum + cs_cap, c.chunk_sum + 2 * cs_cap};
         cudaMemsetAsync(c.chunk_sum, 0, sizeof(int) * 3 * (size_t)cs_cap, s);
-        level_count_kernel<D><<<grid, LEVEL_CHUNK, 0, s>>>(na, c.keys, c.lvl_start, 1, levels, lv,
-                                                         c.p.leaf_num, tmp[1], cs[1], c.d_work + TREE_TRUNC_SLOT);
-        for (int l = 1; l <= lv; ++l)
-            level_build_kernel<D><<<grid, LEVEL_CHUNK, 0, s>>>(
-                na, c.keys, n, c.lvl_start, l, levels, lv, c.p.leaf_num, tmp[l & 1], tmp[(l + 1) & 1],
-                cs[l % 3], cs[(l + 1) % 3], cs[(l + 2) % 3], cs_cap, c.node_cap, c.d_err,
-                c.d_work + TREE_TRUNC_SLOT);
+        level_count_kernel<D><<<cgrid, COUNT_THREADS, 0, s>>>(na, c.keys, n, c.lvl_start, 1, levels, lv,
+                                                             c.p.leaf_num, tmp[1], cs[1], c.d_work + TREE_TRUNC_SLOT);
+        for (int l = 1; l <= lv; ++l) {
+            level_build_kernel<D><<<grid, LEVEL_CHUNK, 0, s>>>(na, c.lvl_start, l, tmp[l & 1], cs[l % 3],
+                                                             cs[(l + 2) % 3], cs_cap, c.node_cap, c.d_err);
+            level_count_kernel<D><<<cgrid, COUNT_THREADS, 0, s>>>(na, c.keys, n, c.lvl_start, l + 1, levels, lv,
+                                                                 c.p.leaf_num, tmp[(l + 1) & 1], cs[(l + 1) % 3],
+                                                                 c.d_work + TREE_TRUNC_SLOT);
+        }
     }
     cudaMemcpyAsync(c.node_total, c.lvl_start + lv + 2, sizeof(int), cudaMemcpyDeviceToDevice, s);
     if (c.p.use_gravity) launch_node_moments(c);   // node masses and centres of mass serve gravity only
