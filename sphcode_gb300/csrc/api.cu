@@ -516,12 +516,12 @@ int autotune_impl(Ctx& c)
 {
     const int base_pre = c.dim == 1 ? 128 : c.dim == 2 ? 512 : 1024;
     const int base_fluid = c.dim == 1 ? 128 : c.dim == 2 ? 384 : 1024;
-    const double fr[4] = {0.5, 0.75, 1.0, 1.5};
+    const double fr[5] = {0.5, 0.75, 1.0, 1.5, 2.0};
     pre_inputs(c, 0);
     float best_total = 1e30f;
     int best_gw = c.gw_pre, best_tp = base_pre, best_tf = base_fluid;
-    for (int gw = 1; gw <= 2; ++gw) {
-        if (32 * gw > 32 * 8) break;
+    // groups of 32, 64 and 128 targets (one to four warps)
+    for (int gw = 1; gw <= 4; gw *= 2) {
         c.gw_pre = gw;
         if (build_groups(c) != SPHGPU_OK) break;
         launch_make_tree(c, true, true);   // same positions: an identity reorder, new group split
