@@ -132,6 +132,7 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
         const T hinv_i = r0i.w;
 
         // ---- pair candidates: r^2 < max(h_i, h_j)^2 (1 + delta), j != i ----
+        unsigned long long wmask = 0ull;   // words holding candidates (tiles of at most 64 words)
         for (int w = 0; w < nw; ++w) {
             unsigned bits = 0;
             // the word's smallest 1/h_j bounds every source's 1/max(h_i, h_j) from below
@@ -148,7 +149,9 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
                     if (r2 * (Hinv * Hinv) < dhi) bits |= 1u << b;
                 }
             }
-            tile.mask[w * GT + t] = active ? bits : 0u;
+            if (!active) bits = 0u;
+            tile.mask[w * GT + t] = bits;
+            if (bits && w < 64) wmask |= 1ull << w;
         }
 
         const T rho_i = r1i.x, p_i = r1i.y, c_i = r1i.z, X_i = r1i.w;
@@ -174,7 +177,8 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
         for (int k = 0; k < D; ++k) acc[k].zero();
         dene.zero();
 
-        MaskIter it(tile.mask, GT, t, nw);
+        // 3D tiles hold many words without candidates for a target; in 2D the plain scan is cheaper
+        typename std::conditional<D == 3, MaskWordIter, MaskIter>::type it(tile.mask, GT, t, nw, wmask);
         int s;
         while (it.next(s)) {
             {

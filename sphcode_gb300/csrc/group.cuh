@@ -161,7 +161,7 @@ struct MaskIter {
     unsigned* mask;
     int gt, t, nw, w, b;
     unsigned bits;
-    __device__ __forceinline__ MaskIter(unsigned* m, int gt_, int t_, int nw_)
+    __device__ __forceinline__ MaskIter(unsigned* m, int gt_, int t_, int nw_, unsigned long long = ~0ull)
         : mask(m), gt(gt_), t(t_), nw(nw_), w(0), b(0), bits(nw_ > 0 ? m[t_] : 0u) {}
     __device__ __forceinline__ bool next(int& s)
     {
@@ -177,6 +177,53 @@ struct MaskIter {
     // drop the source last returned by next() from the stored mask
     __device__ __forceinline__ void clear_current() { mask[w * gt + t] &= ~(1u << b); }
     // drop source s (returned by an earlier next()) from the stored mask
+    __device__ __forceinline__ void clear(int s) { mask[(s >> 5) * gt + t] &= ~(1u << (s & 31)); }
+};
+
+// MaskIter over the words that hold candidates only (bit w of `words`, recorded while the mask
+// was built; tiles of at most 64 words), loading the next such word's bits while the current one
+// is consumed.  Larger tiles scan every word in turn.  It costs a few registers more than MaskIter.
+struct MaskWordIter {
+    unsigned* mask;
+    int gt, t, nw, w, b;
+    unsigned bits;
+    unsigned long long wm;   // words still to visit after pw
+    int pw;                  // next word to visit (-1: none)
+    unsigned pbits;          // its bits, loaded ahead
+    __device__ __forceinline__ MaskWordIter(unsigned* m, int gt_, int t_, int nw_, unsigned long long words)
+        : mask(m), gt(gt_), t(t_), nw(nw_), w(-1), b(0), bits(0u), pw(-1), pbits(0u)
+    {
+        wm = nw_ > 64 ? 0ull : (words & (nw_ == 64 ? ~0ull : ((1ull << nw_) - 1ull)));
+        advance();
+    }
+    __device__ __forceinline__ void advance()
+    {
+        if (wm) {
+            pw = __ffsll((long long)wm) - 1;
+            wm &= wm - 1;
+            pbits = mask[pw * gt + t];
+        } else {
+            pw = -1;
+        }
+    }
+    __device__ __forceinline__ bool next(int& s)
+    {
+        while (bits == 0) {
+            if (nw > 64) {
+                if (++w >= nw) return false;
+                bits = mask[w * gt + t];
+                continue;
+            }
+            if (pw < 0) return false;
+            w = pw;
+            bits = pbits;
+            advance();
+        }
+        b = __ffs(bits) - 1;
+        bits &= bits - 1;
+        s = w * 32 + b;
+        return true;
+    }
     __device__ __forceinline__ void clear(int s) { mask[(s >> 5) * gt + t] &= ~(1u << (s & 31)); }
 };
 

@@ -111,6 +111,7 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
         for (int k = 0; k < D; ++k) xo[k] = (T)min_image(xi[k] - gm->gc[k], a.pb, k);
 
         // ---- candidates: r^2 < h_s^2, exactly (src/bhtree.cpp:256) ----
+        unsigned long long wmask = 0ull;   // words holding candidates (tiles of at most 64 words)
         {
             const double hs2 = __dmul_rn(hs, hs);
             const double band = r2_band<T, D>(gm, hs);
@@ -133,7 +134,9 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
                         if (exact_r2<D>(st, xi, tile.idx[w * 32 + b], a.pb) < hs2) bits |= 1u << b;
                     }
                 }
-                tile.mask[w * GT + t] = active ? bits : 0u;
+                if (!active) bits = 0u;
+                tile.mask[w * GT + t] = bits;
+                if (bits && w < 64) wmask |= 1ull << w;
             }
         }
 
@@ -153,7 +156,7 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
                     s1.zero();
                     // two candidates per trip: independent dependency chains, one compensated
                     // add per pair
-                    MaskIter it(tile.mask, GT, t, nw);
+                    MaskWordIter it(tile.mask, GT, t, nw, wmask);
                     int sa, sb;
                     while (it.next(sa)) {
                         const bool two = it.next(sb);
@@ -219,7 +222,7 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
             const double band = r2_band<T, D>(gm, hf);
             const T lo_t = to_T_down<T>(hf2 - band), hi_t = to_T_up<T>(hf2 + band);
             // the next candidate's velocity record is loaded before the current one is evaluated
-            MaskIter it(tile.mask, GT, t, nw);
+            MaskWordIter it(tile.mask, GT, t, nw, wmask);
             int snext;
             bool have = it.next(snext);
             V4 vq{};
@@ -334,7 +337,7 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
 #pragma unroll
                 for (int q = 0; q < D; ++q) dv[k][q].zero();
             }
-            MaskIter it(tile.mask, GT, t, nw);
+            MaskWordIter it(tile.mask, GT, t, nw, wmask);
             int s;
             while (it.next(s)) {
                 {
