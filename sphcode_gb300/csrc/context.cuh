@@ -239,7 +239,13 @@ void launch_pair_passes(Ctx& c, const void* kern, Args& a, int tcap, int elt4, i
         int cap, stack_cap, leaf_cap, grid;
         const bool last_tier = pass >= passes - 2;
         if (pass == 0) { cap = std::min(tcap, big); stack_cap = 128; leaf_cap = 96; }
-        else if (!last_tier) { cap = std::min(c.pass2_scale * tcap, big); stack_cap = 512; leaf_cap = 512; }
+        else if (!last_tier) {
+            // walk capacities sized so that a 2D or 3D CTA of the doubled tile keeps a third block
+            // per SM (1D trees with one particle per leaf need more leaf slots)
+            cap = std::min(c.pass2_scale * tcap, big);
+            stack_cap = 256;
+            leaf_cap = c.dim == 1 ? 512 : 256;
+        }
         else { cap = big; stack_cap = 1024; leaf_cap = 1024; }
         a.L = make_layout(gt, cap, elt4, eltT, stack_cap, leaf_cap);
         grid = last_tier ? c.num_sms : std::max(1, kernel_occupancy(kern, gt, a.L.total)) * c.num_sms;
