@@ -92,6 +92,7 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.lines = []
+        self.first = 0
 
     def start(self):
         try:
@@ -100,8 +101,17 @@ class ClockSampler:
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            # nvidia-smi takes a moment to start: wait for its first sample, so that the samples
+            # of the timed region are not lost to its start-up
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 5.0 and self.proc.poll() is None:
+                time.sleep(0.01)
         except Exception:
             self.proc = None
+
+    def mark(self):
+        """The timed region starts: later samples are the ones reported."""
+        self.first = len(self.lines)
 
     def _read(self):
         for line in self.proc.stdout:
@@ -117,7 +127,9 @@ class ClockSampler:
             self.proc.kill()
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
+        # the samples taken from the start of the timed region on (at least the last one)
+        lines = self.lines[min(self.first, max(len(self.lines) - 1, 0)):]
+        for line in lines:
             parts = [x.strip() for x in line.split(",")]
             if len(parts) < 9:
                 continue
@@ -272,7 +284,8 @@ def adjoint_report():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    # about a second of timed KHI steps: the clock sampler (every 200 ms) sees several samples
+    ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="khi")
@@ -390,6 +403,7 @@ def main():
     clocks = ClockSampler(local)
     clocks.start()
     barrier()
+    clocks.mark()
     ms = sim.bench_steps(args.steps, flush_l2=True)
     barrier()
     clk = clocks.stop()
