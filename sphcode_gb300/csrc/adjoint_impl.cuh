@@ -508,7 +508,7 @@ __global__ void adj_final_kernel(State st, int n, AdjLayout lay, double* adj, co
     if (threadIdx.x == 0) partials[blockIdx.x] = red[0];
 }
 
-__global__ inline void adj_alpha_sum_kernel(const double* partials, int nparts, double* alpha_bar)
+static __global__ void adj_alpha_sum_kernel(const double* partials, int nparts, double* alpha_bar)
 {
     __shared__ double red[1024];
     red[threadIdx.x] = threadIdx.x < nparts ? partials[threadIdx.x] : 0.0;
