@@ -5,8 +5,8 @@
  * (include/module.hpp:10-14: initialize(shared_ptr<SPHParameters>),
  * calculation(shared_ptr<Simulation>)) called by sph::Solver (src/solver.cpp:387-429).
  * Each entry point below is the device-side body of one of those calls, so a GPU Module
- * subclass is a drop-in that forwards its calculation() here (see INTEGRATION.md for the
- * Module subclasses and the ctypes binding).  Plain pointers and sizes only; no C++ or CUDA
+ * subclass is a drop-in that forwards its calculation() here (sphcode_gb300/cxx/gpu_modules.hpp
+ * holds such subclasses).  Plain pointers and sizes only; no C++ or CUDA
  * types cross this boundary.  Every function returns an sphgpu_status code; no exception
  * crosses the ABI.
  *
@@ -269,9 +269,9 @@ int sphgpu_adjoint_initialize(sphgpu_ctx* ctx, double* adj, const double* dens_b
 
 /* Energy and momentum sums of sphgpu_energy over caller-owned device arrays, with no device
  * allocation at all.  No counterpart in the reference.  It is meant for callers that cannot
- * call cudaMalloc where they need the sums: code inside another library's CUDA stream capture
- * (allocation is not allowed while a stream is captured) and host programs that own every byte
- * of device memory through a pool they reserved at start-up.
+ * call cudaMalloc where they need the sums: host programs that own every byte of device memory
+ * through a pool they reserved at start-up, and loops that must not stall the device (cudaMalloc
+ * and cudaFree can synchronise it).
  *
  * Inputs are device pointers in the caller's particle order: mass[n], vel[n * dim] (interleaved
  * x0 y0 z0 x1 ...), ene[n] and phi[n] (phi may be NULL: potential 0).  out is a device pointer
@@ -282,7 +282,10 @@ int sphgpu_adjoint_initialize(sphgpu_ctx* ctx, double* adj, const double* dens_b
  * loading the library keeps until the process exits; hence n <= 33,554,432 (4096 chunks of 8192
  * particles), larger n returns SPHGPU_ERR_CAPACITY with the text in sphgpu_last_error(NULL).
  * The first call on a device looks up the array's device address (cudaGetSymbolAddress) with
- * that device current; make that first call before any stream capture.  All calls share the one
+ * that device current, and looks it up again if the device's context has changed since (e.g.
+ * after cudaDeviceReset); make that first call before any stream capture.  A CUDA error left
+ * pending by the caller's earlier work is reported (SPHGPU_ERR_CUDA) and left pending; errors of
+ * this call's own launches are cleared after they are reported.  All calls share the one
  * array: calls that may overlap on the GPU (different streams, or different host threads on the
  * same device) race on it and must be serialised by the caller. */
 int sphgpu_energy_noalloc(int dim, int n, const double* mass, const double* vel, const double* ene,

@@ -3,8 +3,8 @@
 # libraries used as the parity pin of the C port (oracle/sph_oracle.c) and, where available, as
 # the CPU baseline.  Test infrastructure only; nothing here is part of the product.
 #
-#   oracle/build_ref.sh            build from the reference checkout (default /root/reference,
-#                                  override with SPHCODE_REFERENCE=...)
+#   SPHCODE_REFERENCE=<checkout> oracle/build_ref.sh
+#                                  build from the reference checkout at <checkout> (required)
 #
 # The reference fixes DIM with `#define DIM 1` (include/defines.hpp:5) and resolves quoted
 # includes next to each header, so per-DIM copies of include/ with that one line changed are
@@ -22,7 +22,11 @@
 # reference checkout (SPHCODE_REFERENCE pointing at the snapshot).
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${SPHCODE_REFERENCE:-/root/reference}"
+if [ -z "${SPHCODE_REFERENCE:-}" ]; then
+    echo "build_ref.sh: set SPHCODE_REFERENCE to the reference checkout (or its snapshot)" >&2
+    exit 2
+fi
+REF="$SPHCODE_REFERENCE"
 OUT="$HERE/_ref"
 CXX="${CXX:-g++}"
 JOBS="${JOBS:-$(nproc)}"

@@ -89,11 +89,12 @@ def build_port(force: bool = False) -> None:
         os.replace(out + ".tmp", out)
 
 
-def build_reference() -> bool:
-    """Run the oracle/_ref recipe if the reference sources are present. Returns availability."""
+def build_reference(src: Optional[str] = None) -> bool:
+    """Run the oracle/_ref recipe on the reference checkout `src` (else $SPHCODE_REFERENCE, else
+    the snapshot an earlier build kept in oracle/_ref/snapshot).  Returns availability."""
     script = os.path.join(HERE, "build_ref.sh")
-    src = os.environ.get("SPHCODE_REFERENCE", "/root/reference")
-    if not os.path.exists(os.path.join(src, "include", "defines.hpp")):
+    src = src or os.environ.get("SPHCODE_REFERENCE", "")
+    if not (src and os.path.exists(os.path.join(src, "include", "defines.hpp"))):
         snap = os.path.join(REF, "snapshot")
         if os.path.exists(os.path.join(snap, "include", "defines.hpp")):
             src = snap

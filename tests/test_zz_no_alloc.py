@@ -1,7 +1,7 @@
 """The allocation-free energy/momentum entry point (sphgpu_energy_noalloc).
 
-It serves callers that cannot allocate device memory where they need the sums, such as code
-inside another library's stream capture or a host that reserves all device memory up front.  The
+It serves callers that cannot allocate device memory where they need the sums, such as a host
+that reserves all device memory up front or a loop that must not stall the device.  The
 test calls it through the C-ABI on device arrays the test owns, twice in a row, and compares both
 results with the context-based sphgpu_energy on the same state (1e-12 relative, the FP64
 tolerance of these sums: only the summation order differs).  It also checks that a particle
