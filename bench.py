@@ -31,15 +31,34 @@ sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s on 1 GB300, FP32-pair vs FP64 form at stated rel err"
 
-# Static flop counts of the reference's pair bodies (FMA = 2, add/mul/div/sqrt = 1 each), per
-# interacting pair, used for the compute roofline of the force kernel.
+# Static flop counts of the reference's pair bodies (each add, multiply, divide and square root
+# = 1, an FMA = 2), per pair: FluidForce per interacting pair {r < max(h_i, h_j)}
+# (src/fluid_force.cpp:56-116, src/disph/d_fluid_force.cpp:26-86, src/gsph/g_fluid_force.cpp:79-163);
+# PreInteraction per Newton iteration and pair {r < h} (src/pre_interaction.cpp:227-283,
+# src/disph/d_pre_interaction.cpp:187-217: r_ij, |r_ij|, W, dW/dh, two sums) and per pair of the
+# density pass (src/pre_interaction.cpp:78-161, src/disph/d_pre_interaction.cpp:60-154: W, dW/dh,
+# the density-type sums, the signal velocity, grad W and the div/rot v sums of Balsara / TD-AV).
 FLUID_FLOPS_PER_PAIR = {("disph", 2): 120, ("disph", 3): 135, ("ssph", 2): 110, ("ssph", 3): 125,
                         ("ssph", 1): 90, ("gsph", 1): 180, ("disph", 1): 100}
+PRE_NEWTON_FLOPS_PER_PAIR = {1: 44, 2: 47, 3: 50}
+PRE_DENS_FLOPS_PER_PAIR = {("disph", 2): 91, ("disph", 3): 110, ("ssph", 2): 86, ("ssph", 3): 104,
+                           ("ssph", 1): 60, ("disph", 1): 62, ("gsph", 1): 70}
+# Barnes-Hut walk: per leaf pair (HK89-softened potential and force, src/bhtree.cpp:273-299) and per
+# accepted monopole (src/bhtree.cpp:327-329).
+GRAV_FLOPS_LEAF, GRAV_FLOPS_NODE = 60, 20
+
+
 # Compulsory HBM bytes of the force stage per particle: FP64 reads of pos(D), vel(D), mass,
 # dens, pres, ene, sml, sound, alpha, balsara, gradh + FP32 mirror write/read (48 B) + writes of
 # acc(D), dene.
 def fluid_bytes_per_particle(D):
     return 8 * (2 * D + 9) + 48 * 2 + 8 * (D + 1)
+
+
+# PreInteraction: reads pos(D), vel(D), mass, dens, ene, sound, alpha, balsara and the FP32 mirrors
+# (32 B written and read), writes sml, dens, pres, gradh, balsara, alpha (FP64) and the count.
+def pre_bytes_per_particle(D):
+    return 8 * (2 * D + 6) + 32 * 2 + 8 * 6 + 4
 
 
 def aggregate(ms_local, n_local, steps, dist=None, device="cpu"):
@@ -299,6 +318,10 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true",
                     help="skip the Gresho-Chan adjoint cost / finite-difference report")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-oracle", action="store_true",
+                    help="skip the comparison with the reference's modules after initialize + 1 step")
+    ap.add_argument("--no-workloads", action="store_true",
+                    help="skip the FP32/FP64 summaries of the other workloads")
     ap.add_argument("--pass2-scale", type=int, default=0)
     ap.add_argument("--tile-pre", type=int, default=0)
     ap.add_argument("--tile-fluid", type=int, default=0)
@@ -409,7 +432,7 @@ def main():
     clk = clocks.stop()
     ms, value = aggregate(ms, n, args.steps, dist, "cuda")
 
-    # per-stage device times (eager launches, CUDA events between stages)
+    # per-stage device times (eager launches, CUDA events between stages on the library's stream)
     sim.set_tuning("timing", 1)
     sim.step(1)
     stages = {k: 0.0 for k in ("tree", "pre", "fluid", "gravity", "integrate")}
@@ -419,6 +442,12 @@ def main():
         for k, v in sim.stage_times().items():
             stages[k] += v / reps
     overflow = {"pre": sim.get_tuning("overflow_pre"), "fluid": sim.get_tuning("overflow_fluid")}
+    # work counters of one more step (counted in a step of its own, outside every timed step)
+    sim.set_tuning("count_work", 1)
+    sim.pair_counters(reset=True)
+    sim.step(1)
+    counters = sim.pair_counters(reset=True)
+    sim.set_tuning("count_work", 0)
     schedule = {"group_warps": sim.get_tuning("group_warps"), "tile_pre": sim.get_tuning("tile_cap_pre"),
                 "tile_fluid": sim.get_tuning("tile_cap"), "pass2_scale": sim.get_tuning("pass2_scale"),
                 "autotuned": bool(sim.get_tuning("autotune")),
@@ -429,9 +458,14 @@ def main():
     newton_fail = sim.newton_failures()
     sim.close()
 
-    # ---- FP64 plain form and the FP32-vs-FP64 error after initialize + 1 step -----------------
+    # ---- FP64 plain form; both forms against the GPU FP64 form and the reference -------------
     fp64 = None
-    errs = {}
+    errs, errs_oracle, errs64_oracle = {}, None, None
+    fields_cmp = ("dens", "sml", "pres", "acc", "dene", "pos", "vel", "ene")
+
+    def rel(a, b):
+        return float(np.max(np.abs(a - b)) / max(float(np.max(np.abs(b))), 1e-300))
+
     if not args.no_fp64:
         s64 = make("fp64")
         s32 = make("fp32")
@@ -439,10 +473,14 @@ def main():
         s32.initialize()
         s64.step(1)
         s32.step(1)
-        for name in ("dens", "sml", "pres", "acc", "dene", "pos", "vel", "ene"):
-            a, b = s32.get(name), s64.get(name)
-            errs[name] = float(np.max(np.abs(a - b)) / max(float(np.max(np.abs(b))), 1e-300))
+        got32 = {k: s32.get(k) for k in fields_cmp}
+        got64 = {k: s64.get(k) for k in fields_cmp}
+        errs = {k: rel(got32[k], got64[k]) for k in fields_cmp}
         s32.close()
+        if rank == 0 and world == 1 and not args.no_oracle:
+            ref = oracle_step(p, f)
+            errs_oracle = {k: rel(got32[k], ref[k]) for k in fields_cmp}
+            errs64_oracle = {k: rel(got64[k], ref[k]) for k in fields_cmp}
         s64.step(args.warmup - 1)
         k64 = max(3, args.steps // 4)
         barrier()
@@ -486,44 +524,62 @@ def main():
         e2e_sim.close()
         e2e = {"value": world * n * args.steps / e2e_s, "unit": "particle-steps/s",
                "h2d_bytes_per_step": n * dt.itemsize, "d2h_bytes_per_step": n * dt.itemsize,
-               "path": "sphgpu_upload_aos + sphgpu_step(1) + sphgpu_download_aos on a pinned "
-                       "std::vector<SPHParticle>-layout buffer (record reuse on: the download "
-                       "takes the members outside the layout from the upload's records)"}
+               "path": "sphgpu_upload_aos + sphgpu_step(1) + sphgpu_download_aos, pinned "
+                       "SPHParticle-layout buffer, record reuse on"}
 
-    # ---- roofline of the dominant kernel ----------------------------------------------------
+    # ---- rooflines: every pair stage, the dominant one as `roofline` -----------------------------
     fp32_peak, fp64_peak = sphgpu.measure_peaks()
-    dom = max(("pre", "fluid", "gravity", "tree"), key=lambda k: stages[k])
-    flops_pair = FLUID_FLOPS_PER_PAIR.get((p.sph_type, D), 120)
-    fluid_flops = mean_pairs * n * flops_pair
-    fluid_ms = stages["fluid"]
-    import json as _json
     peaks = {}
     try:
-        peaks = _json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    fluid_bytes = fluid_bytes_per_particle(D) * n
-    roofline = {"kernel": "fluid_kernel (FluidForce, FP32 pairs)", "bound": "fp32",
-                "achieved": fluid_flops / (fluid_ms * 1e-3) / 1e12, "peak": fp32_peak,
-                "unit": "TFLOP/s", "frac": None, "traffic": None,
-                "algorithmic_flops_per_launch": fluid_flops, "pairs_per_particle": mean_pairs,
-                "flops_per_pair": flops_pair, "launch_ms": fluid_ms,
-                "peak_source": "sphgpu_measure_peaks FP32 FMA loop on this GPU",
-                "hbm": {"achieved": fluid_bytes / (fluid_ms * 1e-3) / 1e9, "peak": hbm_peak,
-                        "unit": "GB/s", "frac": fluid_bytes / (fluid_ms * 1e-3) / 1e9 / hbm_peak,
-                        "algorithmic_bytes_per_launch": fluid_bytes,
-                        "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}}
-    roofline["frac"] = roofline["achieved"] / fp32_peak if fp32_peak > 0 else None
+    hbm_src = "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback 6800 GB/s"
+
+    def line_for(kernel, flops, ms, nbytes, extra):
+        ach = flops / (ms * 1e-3) / 1e12 if ms > 0 else 0.0
+        gbs = nbytes / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
+        out = {"kernel": kernel, "bound": "fp32", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
+               "frac": ach / fp32_peak if fp32_peak > 0 else None, "traffic": None,
+               "algorithmic_flops_per_launch": flops, "launch_ms": ms,
+               "peak_source": "sphgpu_measure_peaks FP32 FMA loop on this GPU (of measured)",
+               "hbm": {"achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+                       "algorithmic_bytes_per_launch": nbytes, "peak_source": hbm_src}}
+        out.update(extra)
+        return out
+
+    flops_pair = FLUID_FLOPS_PER_PAIR.get((p.sph_type, D), 120)
+    fnew = PRE_NEWTON_FLOPS_PER_PAIR[D]
+    fden = PRE_DENS_FLOPS_PER_PAIR.get((p.sph_type, D), 90)
+    pre_flops = counters["pre_iter_pairs"] * fnew + counters["pre_pairs"] * fden
+    tgt = max(counters["pre_targets"], 1)
+    rooflines = {
+        "pre": line_for("pre_kernel (PreInteraction, FP32 pairs; 11 passes + mirror)", pre_flops, stages["pre"],
+                        pre_bytes_per_particle(D) * n,
+                        {"newton_iterations_per_particle": counters["pre_iters"] / tgt,
+                         "neighbours_per_particle": counters["pre_pairs"] / tgt,
+                         "candidates_per_particle": counters["pre_candidates"] / tgt,
+                         "staged_sources_tested_per_particle": counters["pre_tests"] / tgt,
+                         "flops_per_pair": {"newton": fnew, "density": fden},
+                         "work_source": "device counters of one step (sphgpu_pair_counters)"}),
+        "fluid": line_for("fluid_kernel (FluidForce, FP32 pairs; 11 passes + mirror)", mean_pairs * n * flops_pair,
+                          stages["fluid"], fluid_bytes_per_particle(D) * n,
+                          {"pairs_per_particle": mean_pairs, "flops_per_pair": flops_pair,
+                           "staged_sources_tested_per_particle": counters["fluid_tests"] / max(n, 1)}),
+    }
+    dom = max(("pre", "fluid", "gravity", "tree"), key=lambda k: stages[k])
+    roofline = dict(rooflines.get(dom, rooflines["pre"]))
+    roofline["dominant_stage"] = dom
     if args.workload == "khi":
-        # DRAM bytes of one fluid_kernel launch from the committed ncu capture of this workload
+        # DRAM bytes of one launch of the dominant pair kernel from the committed ncu capture
         import re
         try:
             prof = open(os.path.join(ROOT, "profiles", "pair_kernels_khi_786k_fp32.md")).read()
-            m = re.search(r"traffic_bytes_per_launch fluid_kernel: (\d+)", prof)
+            m = re.search(r"traffic_bytes_per_launch %s_kernel: (\d+)" % dom, prof)
             if m:
                 roofline["traffic"] = int(m.group(1))
-                roofline["traffic_source"] = "ncu dram__bytes_read.sum + dram__bytes_write.sum, " \
+                roofline["traffic_source"] = "ncu dram__bytes_read.sum + dram__bytes_write.sum of pass 1, " \
                                              "profiles/pair_kernels_khi_786k_fp32.md"
         except OSError:
             pass
@@ -539,7 +595,33 @@ def main():
     if rank == 0 and world == 1 and not args.no_adjoint:
         adjoint = adjoint_report()
 
+    others = {}
+    if rank == 0 and world == 1 and not args.no_workloads:
+        for name in ("evrard", "ensemble", "gresho"):
+            if name != args.workload:
+                others[name] = workload_summary(name, make_sim=None)
+
     if rank == 0:
+        def r3(x):
+            return None if x is None else float(f"{x:.3g}")
+        summary = {
+            "fp32_value": r3(value), "fp64_value": r3(fp64["value"]) if fp64 else None,
+            "fp32_over_fp64": r3(value / fp64["value"]) if fp64 else None,
+            "fp32_rel_err_vs_fp64": {k: r3(v) for k, v in errs.items()},
+            "fp32_rel_err_vs_oracle": {k: r3(v) for k, v in errs_oracle.items()} if errs_oracle else None,
+            "fp64_rel_err_vs_oracle": {k: r3(v) for k, v in errs64_oracle.items()} if errs64_oracle else None,
+            "oracle": "reference modules, strict FP64, initialize + 1 step" if errs_oracle else None,
+            "roofline": {"kernel": dom, "tflops": r3(roofline["achieved"]), "frac": r3(roofline["frac"])},
+            "workloads": {k: {"fp32": r3(v["fp32"]), "fp64": r3(v["fp64"]), "ratio": r3(v["ratio"])}
+                          for k, v in others.items()},
+            "adjoint": ({"bwd_over_fwd_fp32": r3(adjoint["cost"]["fp32"]["backward_over_forward"]),
+                         "bwd_over_fwd_fp64": r3(adjoint["cost"]["fp64"]["backward_over_forward"]),
+                         "fd_rel_err_20_steps": {k: r3(v) for k, v in adjoint["fd_check"]["rel_err"].items()},
+                         "fp32_vs_fp64_200_steps": {k: r3(v) for k, v in adjoint["fp32_vs_fp64_200_steps"].items()},
+                         "note": "the FP32-pair gradient over 200 steps is not usable (see fp32_vs_fp64_200_steps); "
+                                 "the cost claim holds for the FP64 gradient and for FP32 over <= 20 steps"}
+                        if adjoint else None),
+        }
         line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -549,18 +631,56 @@ def main():
                            "form": "fp32_pair (FP32 pair sums, Kahan totals, FP64 state)",
                            "l2": "2 x L2 buffer overwritten between timed steps",
                            "parallelism": f"replicas{world}"},
-                "fp64_form": fp64,
-                "fp32_over_fp64": (value / fp64["value"]) if fp64 else None,
-                "fp32_rel_err_vs_fp64_after_1_step": errs,
+                "adjoint": adjoint, "workloads": others,
                 "stage_ms": stages, "overflow_groups": overflow, "newton_failures": newton_fail,
-                "schedule": schedule,
+                "schedule": schedule, "work_counters": counters, "rooflines": rooflines,
+                "peaks": {"fp32_tflops": fp32_peak, "fp64_tflops": fp64_peak},
+                "fp64_form": fp64, "fp32_over_fp64": (value / fp64["value"]) if fp64 else None,
+                "fp32_rel_err_vs_fp64_after_1_step": errs,
+                "fp32_rel_err_vs_oracle_after_1_step": errs_oracle,
+                "fp64_rel_err_vs_oracle_after_1_step": errs64_oracle,
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
                 "gpu_launches": launches_per_step * args.steps,
-                "peaks": {"fp32_tflops": fp32_peak, "fp64_tflops": fp64_peak},
-                "adjoint": adjoint}
+                "summary": summary}
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def oracle_step(p, f):
+    """The reference's own modules (strict FP64 flavour; the C restatement where they are not
+    built) after initialize + 1 step, on every host core: the fields the bench compares."""
+    from oracle import pyoracle
+    kind = "ref" if pyoracle.reference_available("strict") else "port"
+    ref = pyoracle.OracleSim(p, f, kind=kind, flavor="strict", threads=os.cpu_count())
+    ref.initialize()
+    ref.step()
+    out = {k: ref.get(k) for k in ("dens", "sml", "pres", "acc", "dene", "pos", "vel", "ene")}
+    ref.close()
+    return out
+
+
+def workload_summary(name, make_sim=None, steps=20, steps64=4):
+    """FP32-pair and FP64 particle-steps/s of another workload (initialize with the tuner, 3
+    warm-up steps, then timed steps with the L2 flushed between them)."""
+    from sphcode_gb300 import sphgpu
+    p, f, desc, runs = workload(name)
+    n = int(f["mass"].shape[0])
+    out = {"workload": desc, "n_particles": n}
+    for prec, k in (("fp32", steps), ("fp64", steps64)):
+        with sphgpu.GpuSimulation(p, f, precision=prec, runs=runs) as sim:
+            sim.initialize()
+            sim.step(3)
+            ms = sim.bench_steps(k, flush_l2=True)
+            out[prec] = n * k / (ms * 1e-3)
+            out[prec + "_ms_per_step"] = ms / k
+            if prec == "fp32":
+                sim.set_tuning("timing", 1)
+                sim.step(1)
+                out["fp32_stage_ms"] = {kk: round(v, 4) for kk, v in sim.stage_times().items()}
+                sim.set_tuning("timing", 0)
+    out["ratio"] = out["fp32"] / out["fp64"]
+    return out
 
 
 if __name__ == "__main__":

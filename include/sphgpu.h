@@ -210,9 +210,27 @@ const char* sphgpu_last_error(const sphgpu_ctx* ctx);
  * the host since that upload (the upload, calculate, download pattern of a Module);
  * 20, 21 (read only) the level limit of the last octree build, and the level limit of the
  * step builds without gravity (0: all key levels; raised by four whenever a build leaves a node
- * with more than leafParticleNumber particles unsplit at the limit). */
+ * with more than leafParticleNumber particles unsplit at the limit);
+ * 22 source-tile limit of every pair-kernel pass, the large-capacity passes included (0 = none;
+ * a multiple of 32): targets whose sources do not fit make the stage return SPHGPU_ERR_CAPACITY
+ * and record themselves in 13..17;
+ * 23 octree node limit below the 5 N + runs pool (0 = none): a level whose children do not all
+ * fit is left unsplit and the build returns SPHGPU_ERR_NODE_POOL ("There is no free node",
+ * src/bhtree.cpp:179-181);
+ * 24 tuner fault injection: bit k set makes the tuner's trial k (in trial order) count as having
+ * raised the tile status bit, so that it is rejected (tests of the rejection path);
+ * 25 work counters of the pair kernels on/off (sphgpu_pair_counters; off by default). */
 int sphgpu_set_tuning(sphgpu_ctx* ctx, int which, int value);
 int sphgpu_get_tuning(sphgpu_ctx* ctx, int which, int* value);
+
+/* Work counters of the pair kernels accumulated while knob 25 is on (no reference
+ * counterpart; they feed the algorithmic work counts of the benchmark's roofline).  out[16]:
+ * {0 PreInteraction targets, 1 sum of search-radius candidates |{j : r_ij < 1.2 h_guess}|,
+ * 2 sum of Newton iterations, 3 sum of iterations x |{j : r_ij < h_i}|, 4 sum of neighbour counts
+ * |{j : r_ij < h_i}|, 5 staged sources tested per PreInteraction target (summed), 6 the same for
+ * FluidForce, 7 PreInteraction target ranges processed (all passes), 8 FluidForce ranges,
+ * 9..15 zero}.  reset != 0 zeroes them after the read. */
+int sphgpu_pair_counters(sphgpu_ctx* ctx, unsigned long long* out, int reset);
 
 /* Per-stage device time of the last sphgpu_step / stage call in milliseconds, measured with
  * CUDA events on the context's stream: out = {tree, pre, fluid, gravity, integrate}. */

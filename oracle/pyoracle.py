@@ -229,13 +229,15 @@ class OracleSim:
         if rc:
             raise RuntimeError(f"step -> {rc}")
 
-    def neighbors(self, is_ij: bool, exhaustive: bool = False, cap: Optional[int] = None):
-        """Neighbour lists for the current smoothing lengths, as a list of sorted int arrays."""
+    def neighbors(self, is_ij: bool, exhaustive: bool = False, cap: Optional[int] = None,
+                  counts_only: bool = False):
+        """Neighbour counts and lists (rows of `cap` ids, the first count entries valid) for the
+        current smoothing lengths; with counts_only the lists are not stored (list is None)."""
         cap = cap or 2048
         counts = np.zeros(self.n, dtype=np.int32)
-        lst = np.zeros((self.n, cap), dtype=np.int32)
+        lst = None if counts_only else np.zeros((self.n, cap), dtype=np.int32)
         rc = self._f("neighbors")(self._h, int(is_ij), int(exhaustive), counts.ctypes.data,
-                                  lst.ctypes.data, cap)
+                                  None if lst is None else lst.ctypes.data, cap)
         if rc:
             raise RuntimeError(f"neighbors -> {rc}")
         return counts, lst

@@ -385,7 +385,8 @@ int API(neighbors)(void* h, int is_ij, int exh, int* counts, int* list, int cap)
             const int nn = exh ? sph::exhaustive_search(p[i], p[i].sml, p, n, nl, cap, periodic, is_ij != 0)
                                : tree->neighbor_search(p[i], nl, p, is_ij != 0);
             counts[i] = nn;
-            for (int k = 0; k < nn && k < cap; ++k) list[(size_t)i * cap + k] = nl[k];
+            if (list)   // NULL: counts only
+                for (int k = 0; k < nn && k < cap; ++k) list[(size_t)i * cap + k] = nl[k];
         }
     }
     return 0;

@@ -1183,7 +1183,8 @@ int API(neighbors)(void* h, int is_ij, int exh, int* counts, int* list, int cap)
             const int nn = exh ? exhaustive(s, i, is_ij, c, cap, &ovf) : search(s, i, is_ij, c, cap, &ovf);
             if (ovf) err = ORC_ERR_NEIGHBOR_LIST;
             counts[i] = nn;
-            for (int k = 0; k < nn; ++k) list[(size_t)i * cap + k] = c[k].j;
+            if (list)   /* NULL: counts only */
+                for (int k = 0; k < nn; ++k) list[(size_t)i * cap + k] = c[k].j;
         }
         free(c);
     }

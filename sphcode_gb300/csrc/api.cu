@@ -199,7 +199,7 @@ unsigned err_bits_to_status(unsigned bits)
 std::string err_bits_text(unsigned bits)
 {
     std::string s;
-    if (bits & ERR_NODE_POOL) s += "octree needs more than 5 N nodes (There is no free node); ";
+    if (bits & ERR_NODE_POOL) s += "octree needs more nodes than the pool holds (There is no free node); ";
     if (bits & ERR_STACK) s += "walk stack overflow; ";
     if (bits & ERR_LEAVES) s += "leaf list overflow; ";
     if (bits & ERR_TILE) s += "source tile overflow in the large-capacity pass; ";
@@ -281,7 +281,7 @@ void free_ctx(Ctx& c)
     c.alt.run = nullptr;
     free_state(c.alt, false);
     void* ptrs[] = {c.d_run_begin, c.d_time, c.d_dt, c.d_hvs, c.d_dtmin, c.d_sums, c.d_err,
-                    c.d_newton_fail, c.d_work, c.d_ovf_list, c.d_ovf_list2, c.d_stage, c.d_aos, c.d_flush,
+                    c.d_newton_fail, c.d_work, c.d_counters, c.d_ovf_list, c.d_ovf_list2, c.d_stage, c.d_aos, c.d_flush,
                     c.adj_buf, c.adj_mir, c.adj_partials};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -389,6 +389,7 @@ int create_impl(const sphgpu_params* params, int dim, int n_runs, const int* run
         A((void**)&c.d_err, sizeof(unsigned));
         A((void**)&c.d_newton_fail, sizeof(int));
         A((void**)&c.d_work, sizeof(int) * 64);
+        A((void**)&c.d_counters, sizeof(unsigned long long) * PAIR_COUNTERS);
         // halving can leave every target as a range of its own: n entries at most
         c.ovf_cap = std::max(c.n, 2 * c.max_groups) + 64;
         A((void**)&c.d_ovf_list, sizeof(int2) * c.ovf_cap);
@@ -416,6 +417,7 @@ int create_impl(const sphgpu_params* params, int dim, int n_runs, const int* run
         cudaMemset(c.d_err, 0, sizeof(unsigned));
         cudaMemset(c.d_newton_fail, 0, sizeof(int));
         cudaMemset(c.d_work, 0, sizeof(int) * 64);
+        cudaMemset(c.d_counters, 0, sizeof(unsigned long long) * PAIR_COUNTERS);
         fill_ord_kernel<<<ceil_div(c.R, 128), 128>>>(c.d_hvs, c.R, 1.7976931348623157e308);
         fill_ord_kernel<<<ceil_div(c.R, 128), 128>>>(c.d_dtmin, c.R, 1.7976931348623157e308);
         init_ids_kernel<<<ceil_div(c.n, THREADS), THREADS>>>(c.st.id, c.st.run, c.d_run_begin, c.R, c.n);
@@ -518,6 +520,12 @@ int autotune_impl(Ctx& c)
     const int base_fluid = c.dim == 1 ? 128 : c.dim == 2 ? 384 : 1024;
     const double fr[5] = {0.5, 0.75, 1.0, 1.5, 2.0};
     pre_inputs(c, 0);
+    int trial = 0;   // trial index (bit of the fault-injection mask, knob 24)
+    auto injected = [&]() -> unsigned {
+        const unsigned bit = trial < 32 && ((c.tune_fail_mask >> trial) & 1u) ? (unsigned)ERR_TILE : 0u;
+        ++trial;
+        return bit;
+    };
     float best_total = 1e30f;
     int best_gw = c.gw_pre, best_tp = base_pre, best_tf = base_fluid;
     // groups of 32, 64 and 128 targets (one to four warps)
@@ -531,7 +539,7 @@ int autotune_impl(Ctx& c)
             const int cap = std::max(32, (int)(base_pre * f) / 32 * 32);
             c.tile_cap_pre = cap;
             const float ms = time_ms(c, [&] { pre_inputs(c, 1); launch_pre(c, false); }, 2);
-            const unsigned bad = take_err_bits(c);
+            const unsigned bad = take_err_bits(c) | injected();
             if (bad) c.tune_rejects |= bad;
             else if (ms < bp) { bp = ms; tp = cap; }
         }
@@ -543,7 +551,7 @@ int autotune_impl(Ctx& c)
             const int cap = std::max(32, (int)(base_fluid * f) / 32 * 32);
             c.tile_cap = cap;
             const float ms = time_ms(c, [&] { launch_fluid(c); }, 2);
-            const unsigned bad = take_err_bits(c);
+            const unsigned bad = take_err_bits(c) | injected();
             if (bad) c.tune_rejects |= bad;
             else if (ms < bf) { bf = ms; tf = cap; }
         }
@@ -1211,6 +1219,16 @@ int sphgpu_set_tuning(sphgpu_ctx* h, int which, int value)
         c.pass2_scale = value;
         break;
     case 4: c.autotune = value != 0; break;
+    case 22:
+        if (value < 0 || (value % 32) != 0 || value > 16384) return SPHGPU_ERR_ARG;
+        c.tile_limit = value;
+        break;
+    case 23:
+        if (value < 0) return SPHGPU_ERR_ARG;
+        c.node_limit = value;
+        break;
+    case 24: c.tune_fail_mask = (unsigned)value; break;
+    case 25: c.count_work = value != 0; break;
     case 18: c.fixed_dt = value != 0; break;
     case 19: c.aos_reuse = value != 0; break;
     case 5: c.timing = value != 0; break;
@@ -1245,6 +1263,10 @@ int sphgpu_get_tuning(sphgpu_ctx* h, int which, int* value)
     case 19: *value = c.aos_reuse ? 1 : 0; break;
     case 20: *value = c.tree_levels; break;
     case 21: *value = c.depth_cap; break;
+    case 22: *value = c.tile_limit; break;
+    case 23: *value = c.node_limit; break;
+    case 24: *value = (int)c.tune_fail_mask; break;
+    case 25: *value = c.count_work ? 1 : 0; break;
     case 13: case 14: case 15: case 16: case 17: {
         cudaStreamSynchronize(c.stream);
         cudaMemcpy(value, c.d_work + sphgpu::FAIL_INFO_SLOT + (which - 13), sizeof(int), cudaMemcpyDeviceToHost);
@@ -1294,6 +1316,17 @@ int sphgpu_bench_steps(sphgpu_ctx* h, int n_steps, int flush_l2, double* ms)
     const int rc = sphgpu::finish(c, "bench");
     if (rc == SPHGPU_OK) sphgpu::check_tree_cap(c);
     return rc;
+}
+
+int sphgpu_pair_counters(sphgpu_ctx* h, unsigned long long* out, int reset)
+{
+    CTX_OR_FAIL(h);
+    if (!out) return SPHGPU_ERR_ARG;
+    cudaError_t e = cudaStreamSynchronize(c.stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(out, c.d_counters, sizeof(unsigned long long) * sphgpu::PAIR_COUNTERS, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && reset) e = cudaMemset(c.d_counters, 0, sizeof(unsigned long long) * sphgpu::PAIR_COUNTERS);
+    return sphgpu::cuda_status(c, e, "pair_counters");
 }
 
 int sphgpu_stage_times(sphgpu_ctx* h, double* out)

@@ -271,6 +271,28 @@ __host__ __device__ inline long long host_dbl_to_ord(double x)
     return i >= 0 ? i : (i ^ 0x7fffffffffffffffLL);
 }
 
+// ------------------------------------------------------------------------------------------
+// Work counters of the pair kernels (sphgpu_pair_counters), collected only when asked for.
+enum PairCounter : int {
+    PC_PRE_TARGETS = 0,      // PreInteraction targets (non-initial passes)
+    PC_PRE_CANDIDATES = 1,   // sum of |{j : r_ij < 1.2 h_guess}| (the search-radius candidates)
+    PC_PRE_ITERS = 2,        // sum of Newton iterations run
+    PC_PRE_ITER_PAIRS = 3,   // sum over targets of iterations x |{j : r_ij < h_i}|
+    PC_PRE_PAIRS = 4,        // sum of |{j : r_ij < h_i}| (the neighbour counts)
+    PC_PRE_TESTS = 5,        // staged sources tested per target, summed (candidate-mask tests)
+    PC_FLUID_TESTS = 6,      // the same for FluidForce
+    PC_PRE_GROUPS = 7,       // target ranges processed by PreInteraction (all passes)
+    PC_FLUID_GROUPS = 8,     // target ranges processed by FluidForce (all passes)
+    PAIR_COUNTERS = 16
+};
+
+// Adds v over the 32 lanes of a converged warp into *p (lane 0 issues one atomic).
+__device__ __forceinline__ void warp_count(unsigned long long* p, unsigned long long v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(p, v);
+}
+
 __device__ __forceinline__ unsigned lanemask_lt()
 {
     unsigned m;

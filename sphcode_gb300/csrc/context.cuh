@@ -135,6 +135,17 @@ struct Ctx {
     // to stop splitting early raises it (TREE_TRUNC_SLOT).
     int depth_cap = 0;
     int tree_levels = 0;            // split levels of the last build
+    // capacity limits below the allocated ones (0: none), for callers that bound the work of a
+    // stage and for tests of the capacity statuses: the source tile of every pair pass (knob 22)
+    // and the octree node pool (knob 23)
+    int tile_limit = 0;
+    int node_limit = 0;
+    // tuner trials (in trial order, bit k = trial k) treated as if they had raised the tile
+    // status bit: host-side fault injection for tests of the tuner's rejection path (knob 24)
+    unsigned tune_fail_mask = 0;
+    // work counters of the pair kernels (knob 25; sphgpu_pair_counters): off in timed runs
+    bool count_work = false;
+    unsigned long long* d_counters = nullptr;   // PAIR_COUNTERS entries
 
     // adjoint scratch (allocated on the first adjoint call)
     double* adj_buf = nullptr;      // ADJ_SLOTS x n doubles
@@ -247,6 +258,7 @@ void launch_pair_passes(Ctx& c, const void* kern, Args& a, int tcap, int elt4, i
             leaf_cap = c.dim == 1 ? 512 : 256;
         }
         else { cap = big; stack_cap = 1024; leaf_cap = 1024; }
+        if (c.tile_limit > 0) cap = std::min(cap, c.tile_limit);
         a.L = make_layout(gt, cap, elt4, eltT, stack_cap, leaf_cap);
         grid = last_tier ? c.num_sms : std::max(1, kernel_occupancy(kern, gt, a.L.total)) * c.num_sms;
         // work counter 2 pass, produced-range count 2 pass + 1 (zeroed with the others)

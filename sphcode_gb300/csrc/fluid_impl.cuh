@@ -36,6 +36,7 @@ struct FluidArgs {
     double alpha_ac;
     int gsph_2nd;
     const double* dt_run;
+    unsigned long long* counters;   // PairCounter slots, or nullptr (not counted)
 };
 
 // van Leer limiter (src/gsph/g_fluid_force.cpp:28-36).
@@ -308,6 +309,10 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
                 }
             }
         }
+        if (a.counters) {
+            warp_count(a.counters + PC_FLUID_GROUPS, t == 0 ? 1ull : 0ull);
+            warp_count(a.counters + PC_FLUID_TESTS, active ? (unsigned long long)ntile : 0ull);
+        }
         if (active) {
 #pragma unroll
             for (int k = 0; k < D; ++k) st.f[F_ACC + k][i] = (double)acc[k].get();
@@ -394,6 +399,7 @@ void run_fluid(Ctx& c)
     a.alpha_ac = c.p.alpha_ac;
     a.gsph_2nd = c.p.gsph_2nd_order;
     a.dt_run = c.d_dt;
+    a.counters = c.count_work ? c.d_counters : nullptr;
     const int tcap = c.tile_cap ? c.tile_cap : fluid_default_tile_cap<D>();
     launch_pair_passes<FluidArgs<T>>(c, (const void*)kern, a, tcap, sizeof(V4), sizeof(T),
         [](const void* k, int grid, int block, size_t smem, cudaStream_t st, FluidArgs<T>& args) {

@@ -42,6 +42,7 @@ struct PreArgs {
     int* newton_fail;
     double* hguess;   // per-particle guess: the first pass stores it, later passes reuse it
     double nn_over_a; // neighborNumber / A_D
+    unsigned long long* counters;   // PairCounter slots, or nullptr (not counted)
 };
 
 template <int D>
@@ -112,6 +113,7 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
 
         // ---- candidates: r^2 < h_s^2, exactly (src/bhtree.cpp:256) ----
         unsigned long long wmask = 0ull;   // words holding candidates (tiles of at most 64 words)
+        int ncand = 0;
         {
             const double hs2 = __dmul_rn(hs, hs);
             const double band = r2_band<T, D>(gm, hs);
@@ -136,12 +138,14 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
                 }
                 if (!active) bits = 0u;
                 tile.mask[w * GT + t] = bits;
+                ncand += __popc(bits);
                 if (bits && w < 64) wmask |= 1ull << w;
             }
         }
 
         // ---- smoothing length: Newton-Raphson on rho h^D = b (or n h^D = b for disph) ----
         double h = hg;
+        int iters = 0;
         if (!a.initial && a.iterative) {
             // N / A_D is a constant: one FP64 division per launch, not per target
             const T bconst = (T)((TYPE == 1) ? a.nn_over_a : mi * a.nn_over_a);
@@ -149,6 +153,7 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
             for (int it = 0; it < 10; ++it) {
                 if (!__any_sync(FULL, !done)) break;
                 if (!done) {
+                    ++iters;
                     const T hT = (T)h;
                     const T hinvT = T(1) / hT;
                     Sum<T> s0, s1;
@@ -290,6 +295,16 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
                     }
                 }
             }
+        }
+        if (a.counters) {
+            const bool cnt = active && !a.initial;
+            warp_count(a.counters + PC_PRE_GROUPS, t == 0 ? 1ull : 0ull);
+            warp_count(a.counters + PC_PRE_TARGETS, cnt ? 1ull : 0ull);
+            warp_count(a.counters + PC_PRE_CANDIDATES, cnt ? (unsigned long long)ncand : 0ull);
+            warp_count(a.counters + PC_PRE_ITERS, cnt ? (unsigned long long)iters : 0ull);
+            warp_count(a.counters + PC_PRE_ITER_PAIRS, cnt ? (unsigned long long)iters * nnb : 0ull);
+            warp_count(a.counters + PC_PRE_PAIRS, cnt ? (unsigned long long)nnb : 0ull);
+            warp_count(a.counters + PC_PRE_TESTS, cnt ? (unsigned long long)ntile : 0ull);
         }
         if (a.initial) {
             if (active) {
@@ -488,6 +503,7 @@ void run_pre(Ctx& c, bool initial)
     a.newton_fail = c.d_newton_fail;
     a.hguess = (double*)c.mir[8];
     a.nn_over_a = (double)c.p.neighbor_number / volume_const<D>();
+    a.counters = c.count_work ? c.d_counters : nullptr;
     const int tcap = c.tile_cap_pre ? c.tile_cap_pre : default_tile_cap<D>();
     launch_pair_passes<PreArgs<T>>(c, (const void*)kern, a, tcap, sizeof(V4), sizeof(T),
         [](const void* k, int grid, int block, size_t smem, cudaStream_t st, PreArgs<T>& args) {

@@ -453,13 +453,14 @@ __global__ void __launch_bounds__(LEVEL_CHUNK) level_build_kernel(NodeArrays na,
         return u;
     };
     const int cbase = e;   // level l + 1 starts where level l ends
-    if (blockIdx.x == 0) {
-        const int total = prefix(nchunks);
-        if (threadIdx.x == 0) {
-            int next = cbase + total;
-            if (next > node_cap) { atomicOr(err, (unsigned)ERR_NODE_POOL); next = node_cap; }
-            lvl_start[l + 2] = next;
-        }
+    // children that do not all fit the node pool: no node of level l is split (the level's nodes
+    // stay leaves, the next level is empty), the status bit reports it, and no slot of the pool
+    // is left half-written
+    const int total = prefix(nchunks);
+    const bool full = cbase + total > node_cap;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (full) atomicOr(err, (unsigned)ERR_NODE_POOL);
+        lvl_start[l + 2] = full ? cbase : cbase + total;
     }
     for (int chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
         const int chunk_off = prefix(chunk);
@@ -483,8 +484,7 @@ __global__ void __launch_bounds__(LEVEL_CHUNK) level_build_kernel(NodeArrays na,
 #pragma unroll
             for (int c = 1; c < NC; ++c) bnd[c] = na.bnd[(size_t)node * (NC - 1) + (c - 1)];
             const int fc = cbase + off;
-            if (fc + nc > node_cap) {
-                atomicOr(err, (unsigned)ERR_NODE_POOL);
+            if (full) {
                 na.first[node] = -1;
                 na.nchild[node] = 0;
             } else {
@@ -932,6 +932,8 @@ static void make_tree_d(Ctx& c, bool reorder_all, bool full_depth)
     for (int k = 0; k < 3; ++k) na.center[k] = c.nd_center[k];
     na.edge = c.nd_edge;
     na.bnd = c.nd_bnd;
+    // nodes the build may use: the pool (5 N + runs), or less under the node-limit knob
+    const int pool = c.node_limit > 0 ? std::min(c.node_limit, c.node_cap) : c.node_cap;
     const int grid = std::max(1, std::min(c.num_sms * 4, ceil_div(c.node_cap, LEVEL_CHUNK)));
     const int cgrid = std::max(1, std::min(c.num_sms * 16, ceil_div(c.node_cap, COUNT_THREADS)));
     {
@@ -944,7 +946,7 @@ static void make_tree_d(Ctx& c, bool reorder_all, bool full_depth)
                                                              c.p.leaf_num, tmp[1], cs[1], c.d_work + TREE_TRUNC_SLOT);
         for (int l = 1; l <= lv; ++l) {
             level_build_kernel<D><<<grid, LEVEL_CHUNK, 0, s>>>(na, c.lvl_start, l, tmp[l & 1], cs[l % 3],
-                                                             cs[(l + 2) % 3], cs_cap, c.node_cap, c.d_err);
+                                                             cs[(l + 2) % 3], cs_cap, pool, c.d_err);
             level_count_kernel<D><<<cgrid, COUNT_THREADS, 0, s>>>(na, c.keys, n, c.lvl_start, l + 1, levels, lv,
                                                                  c.p.leaf_num, tmp[(l + 1) & 1], cs[(l + 1) % 3],
                                                                  c.d_work + TREE_TRUNC_SLOT);

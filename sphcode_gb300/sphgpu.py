@@ -32,7 +32,8 @@ STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_NODE_POOL", 4: "ERR_CAPA
 TUNING = {"group_warps": 0, "fluid_warps": 1, "gravity_warps": 2, "tile_cap": 3, "autotune": 4,
           "timing": 5, "graph": 6, "graph_kernels": 7, "overflow_pre": 8, "overflow_fluid": 9,
           "tile_cap_pre": 10, "tune_rejects": 11, "pass2_scale": 12, "fixed_dt": 18, "aos_reuse": 19,
-          "tree_levels": 20, "depth_cap": 21}
+          "tree_levels": 20, "depth_cap": 21, "tile_limit": 22, "node_limit": 23,
+          "tune_fail_mask": 24, "count_work": 25}
 
 
 class SphGpuError(RuntimeError):
@@ -83,6 +84,7 @@ _SIGS = {
     "sphgpu_set_tuning": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
     "sphgpu_get_tuning": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "sphgpu_stage_times": (ctypes.c_int, [_P, _P]),
+    "sphgpu_pair_counters": (ctypes.c_int, [_P, _P, ctypes.c_int]),
     "sphgpu_bench_steps": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "sphgpu_measure_peaks": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "sphgpu_energy_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _P, _P, _P, _P, _P, _P]),
@@ -266,9 +268,12 @@ class GpuSimulation:
         return ms.value
 
     def neighbors(self, is_ij: bool, cap: int = 1024):
+        """Neighbour counts and lists (cap ids per particle) for the current smoothing lengths,
+        in the caller's order; cap = 0 returns the counts only (lists None)."""
         counts = np.zeros(self.n, dtype=np.int32)
-        lst = np.zeros((self.n, cap), dtype=np.int32)
-        _check(self.lib.sphgpu_neighbors(self._h, int(is_ij), counts.ctypes.data, lst.ctypes.data, cap),
+        lst = np.zeros((self.n, cap), dtype=np.int32) if cap > 0 else None
+        _check(self.lib.sphgpu_neighbors(self._h, int(is_ij), counts.ctypes.data,
+                                         None if lst is None else lst.ctypes.data, int(cap)),
                "neighbors", self._h)
         return counts, lst
 
@@ -295,10 +300,29 @@ class GpuSimulation:
         _check(self.lib.sphgpu_get_tuning(self._h, TUNING[which], ctypes.byref(v)), "get_tuning", self._h)
         return v.value
 
+    def fail_range(self) -> List[int]:
+        """The last target range no pair-kernel pass could fit: [first particle (key order),
+        count, search radius x 1e9, leaves, overflow code] (tuning knobs 13..17)."""
+        out = []
+        for which in range(13, 18):
+            v = ctypes.c_int()
+            _check(self.lib.sphgpu_get_tuning(self._h, which, ctypes.byref(v)), "get_tuning", self._h)
+            out.append(v.value)
+        return out
+
     def stage_times(self) -> Dict[str, float]:
         out = np.zeros(5)
         _check(self.lib.sphgpu_stage_times(self._h, out.ctypes.data), "stage_times", self._h)
         return dict(zip(["tree", "pre", "fluid", "gravity", "integrate"], out.tolist()))
+
+    COUNTERS = ["pre_targets", "pre_candidates", "pre_iters", "pre_iter_pairs", "pre_pairs",
+                "pre_tests", "fluid_tests", "pre_groups", "fluid_groups"]
+
+    def pair_counters(self, reset: bool = True) -> Dict[str, int]:
+        """Work counters of the pair kernels collected while the count_work knob is on."""
+        out = np.zeros(16, dtype=np.uint64)
+        _check(self.lib.sphgpu_pair_counters(self._h, out.ctypes.data, int(reset)), "pair_counters", self._h)
+        return {k: int(v) for k, v in zip(self.COUNTERS, out.tolist())}
 
     def close(self) -> None:
         if getattr(self, "_h", None):

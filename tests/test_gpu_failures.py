@@ -1,0 +1,141 @@
+"""Failure paths of the C-ABI, each made on the host and each returning a clean status.
+
+No case faults or hangs the GPU: the failures come from inputs the kernels handle (a NaN in the
+internal energy, an isolated particle), from capacity limits set through tuning knobs below the
+allocated capacities (the kernels check every capacity and record what did not fit), or from
+host-side fault injection into the tuner.  After each failure the context is destroyed
+normally, and a fresh context on the same device runs a step to show the device is usable.
+
+Reference behaviours matched: Newton non-convergence is logged and the particle falls back to
+the unscaled guess (src/pre_interaction.cpp:277-282); an octree that needs more nodes than the
+pool holds is an error ("There is no free node", src/bhtree.cpp:179-181).
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+ERR_NODE_POOL, ERR_CAPACITY, ERR_NOT_FINITE = 3, 4, 5
+
+
+def _device_still_usable():
+    from sphcode_gb300 import ics, sphgpu
+    p, f = ics.sod()
+    with sphgpu.GpuSimulation(p, f, precision="fp64") as sim:
+        sim.initialize()
+        sim.step(1)
+        assert np.all(np.isfinite(sim.get("dens")))
+
+
+def test_nan_energy_is_reported(gpu_lib):
+    """A NaN internal energy set after initialize makes the next step return
+    SPHGPU_ERR_NOT_FINITE (its pressure and force terms become NaN; positions stay finite within
+    that step, so the tree build and the walks see finite coordinates)."""
+    from sphcode_gb300 import ics, sphgpu
+    p, f = ics.khi(64, 45)
+    for prec in ("fp64", "fp32"):
+        with sphgpu.GpuSimulation(p, f, precision=prec) as sim:
+            sim.initialize()
+            ene = sim.get("ene")
+            ene[123] = np.nan
+            sim.set("ene", ene)
+            with pytest.raises(sphgpu.SphGpuError) as e:
+                sim.step(1)
+            assert e.value.code == ERR_NOT_FINITE, str(e.value)
+            assert "non-finite" in str(e.value)
+            assert np.all(np.isfinite(sim.get("pos")))
+    _device_still_usable()
+
+
+def test_tile_limit_reports_capacity_and_range(gpu_lib):
+    """A source-tile limit below what single targets need (3D, neighborNumber 50) makes
+    PreInteraction return SPHGPU_ERR_CAPACITY and record the failing range in knobs 13..17."""
+    from sphcode_gb300 import ics, sphgpu
+    p, f = ics.evrard(4000, seed=7)
+    with sphgpu.GpuSimulation(p, f, precision="fp32") as sim:
+        sim.set_tuning("autotune", 0)
+        sim.set_tuning("tile_limit", 32)
+        assert sim.get_tuning("tile_limit") == 32
+        with pytest.raises(sphgpu.SphGpuError) as e:
+            sim.initialize()
+        assert e.value.code == ERR_CAPACITY, str(e.value)
+        assert "source tile overflow" in str(e.value)
+        begin, count = sim.fail_range()[:2]
+        assert 0 <= begin < sim.n and 1 <= count <= sim.n - begin
+    _device_still_usable()
+
+
+def test_node_limit_reports_node_pool(gpu_lib):
+    """A node limit far below the 5 N pool makes the octree build stop splitting and the call
+    return SPHGPU_ERR_NODE_POOL (src/bhtree.cpp:179-181)."""
+    from sphcode_gb300 import ics, sphgpu
+    p, f = ics.evrard(4000, seed=7)
+    with sphgpu.GpuSimulation(p, f, precision="fp32") as sim:
+        sim.set_tuning("autotune", 0)
+        sim.set_tuning("node_limit", 200)
+        with pytest.raises(sphgpu.SphGpuError) as e:
+            sim.initialize()
+        assert e.value.code == ERR_NODE_POOL, str(e.value)
+        assert "There is no free node" in str(e.value)
+        stats = sim.tree_stats()
+        assert 0 < int(stats[0]) <= 200   # nodes built stay within the limit
+    _device_still_usable()
+
+
+def test_newton_failure_falls_back_to_guess(gpu_lib):
+    """A particle far from all others has only itself as a candidate: rho h^D is then constant
+    in h, Newton's step is undefined and the reference falls back to the unscaled guess.  The FP64
+    form reports the oracle's failure count and smoothing lengths; the FP32-pair form reports
+    the isolated particle's failure and its guess as well."""
+    from oracle import pyoracle
+    from sphcode_gb300 import ics, sphgpu
+    p, f = ics.evrard(4000, seed=7)
+    far = np.array([6.0, -5.0, 4.0])
+    f = {k: np.concatenate([v, v[:1]]) for k, v in f.items()}
+    f["pos"][-1] = far
+    r = float(np.linalg.norm(far))
+    f["dens"][-1] = 1.0 / (2.0 * np.pi * r)
+    f["pres"][-1] = (p.gamma - 1.0) * f["dens"][-1] * f["ene"][-1]
+    f["mass"] = np.full(f["mass"].size, 1.0 / f["mass"].size)
+    ref = pyoracle.OracleSim(p, f, kind="port")
+    ref.initialize()
+    want = ref.newton_failures()
+    assert want >= 1
+    h_ref = ref.get("sml")
+    # the isolated particle's density is its own kernel value at its smoothing length
+    m = f["mass"][-1]
+    w0 = 495.0 / (32.0 * np.pi) / h_ref[-1] ** 3   # Wendland C4 at r = 0 (3D)
+    assert abs(ref.get("dens")[-1] - m * w0) <= 1e-12 * m * w0
+    for prec in ("fp64", "fp32"):
+        with sphgpu.GpuSimulation(p, f, precision=prec) as sim:
+            sim.initialize()
+            got = sim.newton_failures()
+            h = sim.get("sml")
+            if prec == "fp64":
+                assert got == want
+                assert rel_err(h, h_ref) <= 1e-9
+            else:
+                assert got >= 1
+            assert abs(h[-1] - h_ref[-1]) <= 1e-12 * h_ref[-1]
+    _device_still_usable()
+
+
+def test_tuner_rejects_failing_trials(gpu_lib):
+    """Trials the tuner sees raise a status bit are never chosen.  Trials run in the order
+    group size (1, 2, 4 warps) x {5 PreInteraction tiles, then 5 FluidForce tiles}; injecting a
+    failure into every trial of the one- and two-warp groups and into the first four
+    PreInteraction trials of the four-warp group leaves one admissible schedule for
+    PreInteraction: four warps with twice the base tile (2 x 512 in 2D)."""
+    from sphcode_gb300 import ics, sphgpu
+    p, f = ics.khi(64, 45)
+    mask = (1 << 20) - 1 | (0b1111 << 20)
+    with sphgpu.GpuSimulation(p, f, precision="fp32") as sim:
+        sim.set_tuning("tune_fail_mask", mask)
+        sim.initialize()
+        assert sim.get_tuning("group_warps") == 4
+        assert sim.get_tuning("tile_cap_pre") == 1024
+        assert sim.get_tuning("tune_rejects") & 8   # the tile bit of the injected failures
+        sim.step(1)
+        assert np.all(np.isfinite(sim.get("acc")))
