@@ -17,11 +17,18 @@
 #   libref_strict_dD.so : -O2 -fno-fast-math -ffp-contract=off  (parity pin)
 #   libref_fast_dD.so   : -O3 -funroll-loops -ffast-math        (the reference Makefile's flags,
 #                                                                 Makefile:4-10; timing)
+# Where the sphgpu library is built (sphcode_gb300/_lib/libsphgpu.so, or $SPHGPU_LIB_DIR), a
+# third flavour links the GPU Module drop-ins (sphcode_gb300/cxx/gpu_modules.cpp) in place of the
+# reference's PreInteraction, FluidForce and GravityForce, with the reference's Simulation,
+# TimeStep and tree sources and the same harness glue:
+#   libref_gpu_dD.so    : ref_harness.cpp -DUSE_SPHGPU + gpu_modules.cpp + the strict objects
 # Outputs go only to oracle/_ref/ (git-ignored).  A snapshot of the consumed reference sources is
 # kept in oracle/_ref/snapshot/ so that the same recipe can rebuild them on a machine without the
 # reference checkout (SPHCODE_REFERENCE pointing at the snapshot).
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
+ROOT="$(cd "$HERE/.." && pwd)"
+GPU_LIB_DIR="${SPHGPU_LIB_DIR:-$ROOT/sphcode_gb300/_lib}"
 if [ -z "${SPHCODE_REFERENCE:-}" ]; then
     echo "build_ref.sh: set SPHCODE_REFERENCE to the reference checkout (or its snapshot)" >&2
     exit 2
@@ -79,6 +86,12 @@ for D in 1 2 3; do
         run $CXX $COMMON $FLAGS -DDIM_FROM_HEADER -I"$INC" -I"$HERE" -c "$HERE/ref_harness.cpp" \
             -o "$OUT/d$D/obj_$FL/ref_harness.o"
     done
+    if [ -f "$GPU_LIB_DIR/libsphgpu.so" ]; then
+        mkdir -p "$OUT/d$D/obj_gpu"
+        GINC="-I$INC -I$HERE -I$ROOT/include -I$ROOT/sphcode_gb300/cxx"
+        run $CXX $COMMON $STRICT -DUSE_SPHGPU $GINC -c "$HERE/ref_harness.cpp" -o "$OUT/d$D/obj_gpu/ref_harness.o"
+        run $CXX $COMMON $STRICT $GINC -c "$ROOT/sphcode_gb300/cxx/gpu_modules.cpp" -o "$OUT/d$D/obj_gpu/gpu_modules.o"
+    fi
 done
 for p in "${pids[@]}"; do wait "$p"; done
 
@@ -86,5 +99,10 @@ for D in 1 2 3; do
     for FL in strict fast; do
         $CXX -shared -fopenmp -o "$OUT/libref_${FL}_d$D.so" "$OUT"/d$D/obj_$FL/*.o
     done
+    if [ -f "$GPU_LIB_DIR/libsphgpu.so" ]; then
+        REFOBJ=$(ls "$OUT"/d$D/obj_strict/*.o | grep -v '/ref_harness.o$')
+        $CXX -shared -fopenmp -o "$OUT/libref_gpu_d$D.so" $REFOBJ "$OUT"/d$D/obj_gpu/*.o \
+            -L"$GPU_LIB_DIR" -lsphgpu -Wl,-rpath,"$GPU_LIB_DIR"
+    fi
 done
 echo "build_ref.sh: built $(ls "$OUT"/libref_*.so | wc -l) libraries in $OUT"

@@ -100,9 +100,37 @@ def build_reference(src: Optional[str] = None) -> bool:
             src = snap
         else:
             return reference_available()
+    if _reference_up_to_date(src):
+        return reference_available()
     env = dict(os.environ, SPHCODE_REFERENCE=src)
     subprocess.check_call(["bash", script], env=env, stdout=subprocess.DEVNULL)
     return reference_available()
+
+
+def _reference_up_to_date(src: str) -> bool:
+    """True when every library of the recipe is newer than its inputs (the recipe, the harness,
+    the reference sources and headers, and for the GPU-module flavour the sphgpu library)."""
+    root = os.path.dirname(HERE)
+    gpu_lib = os.path.join(root, "sphcode_gb300", "_lib", "libsphgpu.so")
+    outs = [os.path.join(REF, f"libref_{fl}_d{d}.so") for fl in ("strict", "fast") for d in (1, 2, 3)]
+    ins = [os.path.join(HERE, "build_ref.sh"), os.path.join(HERE, "ref_harness.cpp"),
+           os.path.join(HERE, "sph_oracle.h")]
+    for sub in ("src", "include"):
+        for dp, _, fns in os.walk(os.path.join(src, sub)):
+            ins += [os.path.join(dp, fn) for fn in fns]
+    if os.path.exists(gpu_lib):
+        outs += [os.path.join(REF, f"libref_gpu_d{d}.so") for d in (1, 2, 3)]
+        cxx = os.path.join(root, "sphcode_gb300", "cxx")
+        ins += [gpu_lib, os.path.join(root, "include", "sphgpu.h")]
+        ins += [os.path.join(cxx, fn) for fn in os.listdir(cxx)]
+    if not all(os.path.exists(o) for o in outs):
+        return False
+    return min(os.path.getmtime(o) for o in outs) > max(os.path.getmtime(i) for i in ins)
+
+
+def gpu_modules_available() -> bool:
+    """The reference Solver glue with the GPU Module drop-ins (libref_gpu_dD.so) is built."""
+    return all(os.path.exists(os.path.join(REF, f"libref_gpu_d{d}.so")) for d in (1, 2, 3))
 
 
 def reference_available(flavor: str = "strict") -> bool:
@@ -122,7 +150,7 @@ def _load(kind: str, flavor: str) -> ctypes.CDLL:
         else:
             libs = []
             for d in (1, 2, 3):
-                path = os.path.join(REF, f"libref_{flavor}_d{d}.so")
+                path = os.path.join(REF, f"libref_{'gpu' if kind == 'gpumod' else flavor}_d{d}.so")
                 if not os.path.exists(path):
                     raise FileNotFoundError(path)
                 libs.append(ctypes.CDLL(path, mode=ctypes.RTLD_LOCAL))
@@ -132,10 +160,12 @@ def _load(kind: str, flavor: str) -> ctypes.CDLL:
 
 
 class OracleSim:
-    """One simulation held by the port ("port") or by the reference modules ("ref")."""
+    """One simulation held by the port ("port"), by the reference modules ("ref"), or by the
+    reference's Solver glue with the GPU Module drop-ins in place of its PreInteraction,
+    FluidForce and GravityForce ("gpumod"; `gpu_precision` 0 FP32-pair, 1 FP64)."""
 
     def __init__(self, params, fields: Dict[str, np.ndarray], kind: str = "port",
-                 flavor: str = "strict", threads: Optional[int] = None):
+                 flavor: str = "strict", threads: Optional[int] = None, gpu_precision: int = 1):
         self.dim = int(params.dim)
         self.kind = kind
         lib = _load(kind, flavor)
@@ -146,6 +176,11 @@ class OracleSim:
             self._lib = lib[self.dim - 1]
             self._pfx = f"ref{self.dim}_"
         self._bind()
+        if kind == "gpumod":
+            fn = getattr(self._lib, self._pfx + "set_gpu_precision")
+            fn.restype = None
+            fn.argtypes = [ctypes.c_int]
+            fn(int(gpu_precision))
         n = int(np.asarray(fields["mass"]).shape[0])
         self.n = n
         cp = params.to_c(OrcParams)
@@ -214,20 +249,29 @@ class OracleSim:
     def set_scalar(self, which: str, v: float) -> None:
         self._f("set_scalar")(self._h, {"time": 0, "dt": 1, "h_per_v_sig": 2}[which], float(v))
 
+    def _error(self, what: str, rc: int) -> RuntimeError:
+        text = ""
+        if self.kind != "port":
+            fn = getattr(self._lib, self._pfx + "last_exception")
+            fn.restype = ctypes.c_char_p
+            fn.argtypes = []
+            text = ": " + fn().decode(errors="replace")
+        return RuntimeError(f"{what} -> {rc}{text}")
+
     def initialize(self) -> None:
         rc = self._f("initialize")(self._h)
         if rc:
-            raise RuntimeError(f"initialize -> {rc}")
+            raise self._error("initialize", rc)
 
     def stage(self, name: str) -> None:
         rc = self._f("stage")(self._h, STAGES[name])
         if rc:
-            raise RuntimeError(f"stage {name} -> {rc}")
+            raise self._error(f"stage {name}", rc)
 
     def step(self) -> None:
         rc = self._f("step")(self._h)
         if rc:
-            raise RuntimeError(f"step -> {rc}")
+            raise self._error("step", rc)
 
     def neighbors(self, is_ij: bool, exhaustive: bool = False, cap: Optional[int] = None,
                   counts_only: bool = False):

@@ -43,6 +43,14 @@
 
 #include "sph_oracle.h"
 
+#ifdef USE_SPHGPU
+// The GPU Module drop-ins (sphcode_gb300/cxx/gpu_modules.hpp) in place of the reference's
+// PreInteraction, FluidForce and GravityForce: the plug point of Solver::initialize
+// (src/solver.cpp:359-370), the rest of the Solver glue unchanged.
+#include "gpu_modules.hpp"
+static int g_gpu_precision = SPHGPU_FP64;
+#endif
+
 namespace sph {
 std::string Logger::dir_name;
 std::ofstream Logger::log_io;
@@ -156,12 +164,15 @@ void make_tree(Ref* r)
     r->sim->make_tree();
 }
 
+std::string g_last_exception;
+
 template <typename F>
 int guarded(F&& f)
 {
     try {
         f();
     } catch (std::exception& e) {
+        g_last_exception = e.what();
         return ORC_ERR_EXCEPTION;
     }
     return 0;
@@ -207,6 +218,14 @@ void* API(create)(const orc_params* p, int n)
         r->sim->add_vector_array(names);
     }
     r->gforce = std::make_shared<sph::GravityForce>();
+#ifdef USE_SPHGPU
+    {
+        auto dev = std::make_shared<sph::gpu::Device>(g_gpu_precision);
+        r->pre = std::make_shared<sph::gpu::PreInteraction>(dev);
+        r->fforce = std::make_shared<sph::gpu::FluidForce>(dev);
+        r->gforce = std::make_shared<sph::gpu::GravityForce>(dev);
+    }
+#endif
     r->timestep->initialize(r->param);
     r->pre->initialize(r->param);
     r->fforce->initialize(r->param);
@@ -416,6 +435,14 @@ void API(energy)(void* h, double* out)
 }
 
 int API(newton_failures)(void* h) { (void)h; return -1; }
+
+// Text of the last exception a module threw (THROW_ERROR), for the caller's error message.
+const char* API(last_exception)() { return g_last_exception.c_str(); }
+
+#ifdef USE_SPHGPU
+// Arithmetic form of the GPU modules of the contexts created from now on (sphgpu_precision).
+void API(set_gpu_precision)(int precision) { g_gpu_precision = precision; }
+#endif
 
 void API(set_threads)(int n)
 {

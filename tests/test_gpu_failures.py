@@ -118,7 +118,8 @@ def test_newton_failure_falls_back_to_guess(gpu_lib):
                 assert rel_err(h, h_ref) <= 1e-9
             else:
                 assert got >= 1
-            assert abs(h[-1] - h_ref[-1]) <= 1e-12 * h_ref[-1]
+            # the guess comes from the initial-smoothing density, a pair sum of the form's type
+            assert abs(h[-1] - h_ref[-1]) <= (1e-12 if prec == "fp64" else 1e-6) * h_ref[-1]
     _device_still_usable()
 
 
