@@ -54,6 +54,12 @@ if [ "$(cd "$REF" && pwd)" != "$OUT/snapshot" ]; then
     mkdir -p "$OUT/snapshot/src/disph" "$OUT/snapshot/src/gsph"
     cp -r "$REF/include" "$OUT/snapshot/include"
     for s in $SRCS; do cp "$REF/$s" "$OUT/snapshot/$s"; done
+    # the sample parameter files (read by the parameter-reader tests)
+    for j in "$REF"/sample/*/*.json; do
+        d="$OUT/snapshot/sample/$(basename "$(dirname "$j")")"
+        mkdir -p "$d"
+        cp "$j" "$d/"
+    done
     chmod -R u+w "$OUT/snapshot"
 fi
 

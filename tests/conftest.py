@@ -37,6 +37,15 @@ def gpu_lib():
     return sphgpu.library()
 
 
+def reference_root():
+    """A directory holding the reference's sample/ parameter files: $SPHCODE_REFERENCE, or the
+    source snapshot the oracle recipe keeps in oracle/_ref/snapshot; None when neither exists."""
+    for cand in (os.environ.get("SPHCODE_REFERENCE"), os.path.join(ROOT, "oracle", "_ref", "snapshot")):
+        if cand and os.path.isdir(os.path.join(cand, "sample")):
+            return cand
+    return None
+
+
 def knife_edge(pos, h, i, periodic=None, rel=1e-12):
     """True if some particle lies within rel * h[i] of the distance h[i] from particle i (then
     the last bits of h decide whether it counts as a neighbour).  periodic = (lo, hi) arrays."""
