@@ -1,4 +1,4 @@
-"""Writes tests/golden/mt19937_uniform.npz: the draws the reference's pairing-instability sample
+"""Writes tests/golden/samples/mt19937_uniform.npz: the draws the reference's pairing-instability
 takes (src/sample/pairing_instability.cpp:29-35: std::mt19937 engine(1) and
 std::uniform_real_distribution<real>(-0.05 dx, 0.05 dx) with dx = 1/64), produced by the GNU C++
 standard library itself, for the Python restatement in sphcode_gb300/ics.py to be pinned to.
@@ -40,7 +40,7 @@ def main():
     raw = np.array([int(x) for x in out[:16]], dtype=np.uint64)
     draws = np.array([float.fromhex(x) for x in out[16:]], dtype=np.float64)
     assert draws.size == COUNT
-    np.savez_compressed(os.path.join(HERE, "mt19937_uniform.npz"), raw=raw, draws=draws)
+    np.savez_compressed(os.path.join(HERE, "samples", "mt19937_uniform.npz"), raw=raw, draws=draws)
 
 
 if __name__ == "__main__":

@@ -11,7 +11,7 @@ epsilonAV 0.2 when the time-dependent AV is on) and the sample's particle count 
 
 Initial conditions: particle counts, masses and states of each generator as the reference's
 loops produce them, and the pairing-instability offsets against the draws of the GNU C++
-library's std::mt19937 / std::uniform_real_distribution (tests/golden/mt19937_uniform.npz).
+library's std::mt19937 / std::uniform_real_distribution (tests/golden/samples/mt19937_uniform.npz).
 """
 import math
 import os
@@ -128,7 +128,7 @@ def test_sample_counts_and_states(root):
 
 
 def test_mt19937_and_uniform_draws_match_the_cxx_library():
-    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "mt19937_uniform.npz"))
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "samples", "mt19937_uniform.npz"))
     eng = ics._MT19937(1)
     assert [eng() for _ in range(16)] == [int(x) for x in g["raw"]]
     eng = ics._MT19937(1)
@@ -143,7 +143,7 @@ def test_mt19937_and_uniform_draws_match_the_cxx_library():
 
 
 def test_pairing_offsets_are_the_library_draws(root):
-    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "mt19937_uniform.npz"))["draws"]
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "samples", "mt19937_uniform.npz"))["draws"]
     p, f = ics.reference_sample("pairing_instability", root)
     N, dx = 64, 1.0 / 64
     x, y, i = -0.5 + dx * 0.5, -0.5 + dx * 0.5, 0
