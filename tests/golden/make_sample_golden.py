@@ -1,5 +1,5 @@
 """Writes tests/golden/samples/mt19937_uniform.npz: the draws the reference's pairing-instability
-takes (src/sample/pairing_instability.cpp:29-35: std::mt19937 engine(1) and
+sample takes (src/sample/pairing_instability.cpp:29-35: std::mt19937 engine(1) and
 std::uniform_real_distribution<real>(-0.05 dx, 0.05 dx) with dx = 1/64), produced by the GNU C++
 standard library itself, for the Python restatement in sphcode_gb300/ics.py to be pinned to.
 
