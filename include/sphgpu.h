@@ -219,7 +219,9 @@ const char* sphgpu_last_error(const sphgpu_ctx* ctx);
  * src/bhtree.cpp:179-181);
  * 24 tuner fault injection: bit k set makes the tuner's trial k (in trial order) count as having
  * raised the tile status bit, so that it is rejected (tests of the rejection path);
- * 25 work counters of the pair kernels on/off (sphgpu_pair_counters; off by default). */
+ * 25 work counters of the pair kernels on/off (sphgpu_pair_counters; off by default);
+ * 27 leaf-list capacity of the first pair-kernel pass (0 = by dimension: 96 in 1D and 2D, 256 in
+ * 3D; the walk stack holds at least as many entries). */
 int sphgpu_set_tuning(sphgpu_ctx* ctx, int which, int value);
 int sphgpu_get_tuning(sphgpu_ctx* ctx, int which, int* value);
 

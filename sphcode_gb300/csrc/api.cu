@@ -1229,6 +1229,10 @@ int sphgpu_set_tuning(sphgpu_ctx* h, int which, int value)
         break;
     case 24: c.tune_fail_mask = (unsigned)value; break;
     case 25: c.count_work = value != 0; break;
+    case 27:
+        if (value < 0 || value > 1024) return SPHGPU_ERR_ARG;
+        c.leaf_cap1 = value;
+        break;
     case 18: c.fixed_dt = value != 0; break;
     case 19: c.aos_reuse = value != 0; break;
     case 5: c.timing = value != 0; break;
@@ -1267,6 +1271,7 @@ int sphgpu_get_tuning(sphgpu_ctx* h, int which, int* value)
     case 23: *value = c.node_limit; break;
     case 24: *value = (int)c.tune_fail_mask; break;
     case 25: *value = c.count_work ? 1 : 0; break;
+    case 27: *value = c.leaf_cap1; break;
     case 13: case 14: case 15: case 16: case 17: {
         cudaStreamSynchronize(c.stream);
         cudaMemcpy(value, c.d_work + sphgpu::FAIL_INFO_SLOT + (which - 13), sizeof(int), cudaMemcpyDeviceToHost);

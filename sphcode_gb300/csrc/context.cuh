@@ -145,6 +145,7 @@ struct Ctx {
     unsigned tune_fail_mask = 0;
     // work counters of the pair kernels (knob 25; sphgpu_pair_counters): off in timed runs
     bool count_work = false;
+    int leaf_cap1 = 0;              // leaf-list capacity of the first pair pass (knob 27; 0: by dimension)
     unsigned long long* d_counters = nullptr;   // PAIR_COUNTERS entries
 
     // adjoint scratch (allocated on the first adjoint call)
@@ -249,7 +250,13 @@ void launch_pair_passes(Ctx& c, const void* kern, Args& a, int tcap, int elt4, i
     for (int pass = 0; pass < passes; ++pass) {
         int cap, stack_cap, leaf_cap, grid;
         const bool last_tier = pass >= passes - 2;
-        if (pass == 0) { cap = std::min(tcap, big); stack_cap = 128; leaf_cap = 96; }
+        if (pass == 0) {
+            // walk capacities of the first pass: a 3D group's search box meets many more leaves
+            // than a 2D one's (knob 27 overrides)
+            cap = std::min(tcap, big);
+            leaf_cap = c.leaf_cap1 > 0 ? c.leaf_cap1 : (c.dim == 3 ? 256 : 96);
+            stack_cap = std::max(128, leaf_cap);
+        }
         else if (!last_tier) {
             // walk capacities sized so that a 2D or 3D CTA of the doubled tile keeps a third block
             // per SM (1D trees with one particle per leaf need more leaf slots)

@@ -223,10 +223,33 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
         T vsig = T(2) * ciT;
         int nnb = 0;
         {
+            // the neighbour set {r < h} at the final h: candidates beyond it leave the mask first
+            // (T test outside the guard band, the reference's FP64 r < h inside it, in a loop of
+            // its own), so that the sums below run over neighbours only, without divergence
             const double hf2 = __dmul_rn(hf, hf);
             const double band = r2_band<T, D>(gm, hf);
             const T lo_t = to_T_down<T>(hf2 - band), hi_t = to_T_up<T>(hf2 + band);
-            // the next candidate's velocity record is loaded before the current one is evaluated
+            bool in_band = false;
+            {
+                MaskWordIter it(tile.mask, GT, t, nw, wmask);
+                int s;
+                while (it.next(s)) {
+                    T r[D];
+                    const T r2 = tile_r2<D, T>(xo, tile.pm[s], r);
+                    if (r2 > hi_t) it.clear(s);
+                    else in_band |= !(r2 < lo_t);
+                }
+            }
+            if (in_band) {
+                MaskWordIter it(tile.mask, GT, t, nw, wmask);
+                int s;
+                while (it.next(s)) {
+                    T r[D];
+                    const T r2 = tile_r2<D, T>(xo, tile.pm[s], r);
+                    if (!(r2 < lo_t) && !(__dsqrt_rn(exact_r2<D>(st, xi, tile.idx[s], a.pb)) < hf)) it.clear(s);
+                }
+            }
+            // the next neighbour's velocity record is loaded before the current one is evaluated
             MaskWordIter it(tile.mask, GT, t, nw, wmask);
             int snext;
             bool have = it.next(snext);
@@ -240,10 +263,6 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
                 const V4 p = tile.pm[s];
                 T r[D];
                 const T r2 = tile_r2<D, T>(xo, p, r);
-                if (!(r2 < lo_t)) {
-                    if (r2 > hi_t) { it.clear(s); continue; }
-                    if (!(__dsqrt_rn(exact_r2<D>(st, xi, tile.idx[s], a.pb)) < hf)) { it.clear(s); continue; }
-                }
                 ++nnb;
                 const int j = tile.idx[s];
                 const T rr = sqrt(r2);
