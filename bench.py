@@ -450,6 +450,8 @@ def main():
     sim.set_tuning("count_work", 0)
     schedule = {"group_warps": sim.get_tuning("group_warps"), "tile_pre": sim.get_tuning("tile_cap_pre"),
                 "tile_fluid": sim.get_tuning("tile_cap"), "pass2_scale": sim.get_tuning("pass2_scale"),
+                "pair_sched": ["groups", "groups+tpp after pass 1", "groups+tpp after pass 2",
+                               "thread-per-particle"][sim.get_tuning("pair_sched")],
                 "autotuned": bool(sim.get_tuning("autotune")),
                 "rejected_candidate_status_bits": sim.get_tuning("tune_rejects")}
     sim.set_tuning("timing", 0)

@@ -190,8 +190,9 @@ int sphgpu_newton_failures(sphgpu_ctx* ctx, int* count);
 const char* sphgpu_last_error(const sphgpu_ctx* ctx);
 
 /* Kernel schedule knobs.  With autotune on (the default), sphgpu_initialize times
- * PreInteraction and FluidForce for candidate target-group sizes and tile capacities on the
- * initial state and keeps the fastest; setting 0, 3 or 10 explicitly turns the tuner off. */
+ * PreInteraction and FluidForce for candidate target-group sizes and tile capacities, then the
+ * schedule family (knob 28) on the fastest of those, on the initial state and keeps the fastest;
+ * setting 0, 3 or 10 explicitly turns the tuner off. */
 /* Knobs:
  * which = 0 target-group size in warps, 1 FluidForce warps, 2 GravityForce warps,
  * 3 source-tile capacity (0 = automatic), 4 autotune on/off, 5 per-stage event timing on/off
@@ -221,7 +222,12 @@ const char* sphgpu_last_error(const sphgpu_ctx* ctx);
  * raised the tile status bit, so that it is rejected (tests of the rejection path);
  * 25 work counters of the pair kernels on/off (sphgpu_pair_counters; off by default);
  * 27 leaf-list capacity of the first pair-kernel pass (0 = by dimension: 96 in 1D and 2D, 256 in
- * 3D; the walk stack holds at least as many entries). */
+ * 3D; the walk stack holds at least as many entries);
+ * 28 pair-kernel schedule: 0 target groups staged in shared memory, with later passes for the
+ * ranges a pass cannot fit, halved down to single targets; 1 and 2 the first one or two group
+ * passes, then the thread-per-particle kernel (each target walks the octree itself) for the
+ * ranges left; 3 thread-per-particle only (PreInteraction and FluidForce alike; the tuner tries
+ * all four on its chosen groups and tiles). */
 int sphgpu_set_tuning(sphgpu_ctx* ctx, int which, int value);
 int sphgpu_get_tuning(sphgpu_ctx* ctx, int which, int* value);
 

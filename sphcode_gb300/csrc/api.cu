@@ -563,6 +563,24 @@ int autotune_impl(Ctx& c)
     int rc = build_groups(c);
     if (rc != SPHGPU_OK) return rc;
     launch_make_tree(c, true, true);
+    // the schedule family on the chosen groups and tiles: the group passes alone (0, timed
+    // above), the thread-per-particle kernel for the ranges the first one or two group passes
+    // leave (1, 2), or thread-per-particle throughout (3)
+    int best_sched = 0;
+    for (int sc = 1; sc <= 3; ++sc) {
+        c.pair_sched = sc;
+        const float mp = time_ms(c, [&] { pre_inputs(c, 1); launch_pre(c, false); }, 2);
+        unsigned bad = take_err_bits(c) | injected();
+        pre_inputs(c, 1);
+        launch_pre(c, false);
+        launch_set_kernel_size(c);
+        const float mf = time_ms(c, [&] { launch_fluid(c); }, 2);
+        bad |= take_err_bits(c) | injected();
+        if (bad) c.tune_rejects |= bad;
+        // another family has to win clearly: near-equal timings would pick on noise
+        else if (mp + mf < 0.97f * best_total) { best_total = mp + mf; best_sched = sc; }
+    }
+    c.pair_sched = best_sched;
     pre_inputs(c, 1);
     c.tuned = true;
     return SPHGPU_OK;
@@ -1233,6 +1251,10 @@ int sphgpu_set_tuning(sphgpu_ctx* h, int which, int value)
         if (value < 0 || value > 1024) return SPHGPU_ERR_ARG;
         c.leaf_cap1 = value;
         break;
+    case 28:
+        if (value < 0 || value > 3) return SPHGPU_ERR_ARG;
+        c.pair_sched = value;
+        break;
     case 18: c.fixed_dt = value != 0; break;
     case 19: c.aos_reuse = value != 0; break;
     case 5: c.timing = value != 0; break;
@@ -1272,6 +1294,7 @@ int sphgpu_get_tuning(sphgpu_ctx* h, int which, int* value)
     case 24: *value = (int)c.tune_fail_mask; break;
     case 25: *value = c.count_work ? 1 : 0; break;
     case 27: *value = c.leaf_cap1; break;
+    case 28: *value = c.pair_sched; break;
     case 13: case 14: case 15: case 16: case 17: {
         cudaStreamSynchronize(c.stream);
         cudaMemcpy(value, c.d_work + sphgpu::FAIL_INFO_SLOT + (which - 13), sizeof(int), cudaMemcpyDeviceToHost);

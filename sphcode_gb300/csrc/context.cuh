@@ -146,6 +146,7 @@ struct Ctx {
     // work counters of the pair kernels (knob 25; sphgpu_pair_counters): off in timed runs
     bool count_work = false;
     int leaf_cap1 = 0;              // leaf-list capacity of the first pair pass (knob 27; 0: by dimension)
+    int pair_sched = 0;             // pair-kernel schedule (knob 28, see launch_pair_passes)
     unsigned long long* d_counters = nullptr;   // PAIR_COUNTERS entries
 
     // adjoint scratch (allocated on the first adjoint call)
@@ -222,7 +223,9 @@ constexpr int FAIL_INFO_SLOT = 48;   // d_work[48..52]: the last failing range
 constexpr int TREE_TRUNC_SLOT = 60;  // d_work[60]: a capped tree build left a splittable node
 template <class Args>
 void launch_pair_passes(Ctx& c, const void* kern, Args& a, int tcap, int elt4, int eltT,
-                        void (*launch)(const void*, int, int, size_t, cudaStream_t, Args&));
+                        void (*launch)(const void*, int, int, size_t, cudaStream_t, Args&),
+                        const void* tpp_kern = nullptr,
+                        void (*launch_tpp)(const void*, int, int, cudaStream_t, Args&) = nullptr);
 
 // The largest source tile that fits the opt-in shared memory next to the walk capacities of the
 // overflow pass.
@@ -238,7 +241,9 @@ inline int big_tile_cap(const Ctx& c, int gt, int elt4, int eltT, int stack_cap,
 
 template <class Args>
 void launch_pair_passes(Ctx& c, const void* kern, Args& a, int tcap, int elt4, int eltT,
-                        void (*launch)(const void*, int, int, size_t, cudaStream_t, Args&))
+                        void (*launch)(const void*, int, int, size_t, cudaStream_t, Args&),
+                        const void* tpp_kern,
+                        void (*launch_tpp)(const void*, int, int, cudaStream_t, Args&))
 {
     const int gt = c.group_threads;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, max_optin_smem(c));
@@ -247,7 +252,18 @@ void launch_pair_passes(Ctx& c, const void* kern, Args& a, int tcap, int elt4, i
     int halvings = 0;
     while ((1 << halvings) < gt) ++halvings;
     const int passes = std::min(MAX_PAIR_PASSES, 1 + (halvings + 1) + 2);
-    for (int pass = 0; pass < passes; ++pass) {
+    // schedule (knob 28): 0 group passes down to single targets, 1 / 2 the first one / two group
+    // passes and then the thread-per-particle kernel for the ranges left, 3 thread-per-particle only
+    const int sched = tpp_kern ? c.pair_sched : 0;
+    const int tpp_grid = tpp_kern ? std::max(1, kernel_occupancy(tpp_kern, 128, 0)) * c.num_sms : 0;
+    if (sched == 3) {
+        a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 0, nullptr, nullptr, c.ovf_cap,
+                           nullptr, nullptr, 0, 0, c.d_err, c.d_work + FAIL_INFO_SLOT};
+        launch_tpp(tpp_kern, tpp_grid, 128, c.stream, a);
+        return;
+    }
+    const int group_passes = sched == 1 ? 1 : sched == 2 ? 2 : passes;
+    for (int pass = 0; pass < group_passes; ++pass) {
         int cap, stack_cap, leaf_cap, grid;
         const bool last_tier = pass >= passes - 2;
         if (pass == 0) {
@@ -276,6 +292,13 @@ void launch_pair_passes(Ctx& c, const void* kern, Args& a, int tcap, int elt4, i
                            c.d_work + 2 * pass + 1, c.ovf_cap, pass >= 1 ? 1 : 0, c.d_err,
                            c.d_work + FAIL_INFO_SLOT};
         launch(kern, grid, gt, a.L.total, c.stream, a);
+    }
+    if (sched == 1 || sched == 2) {
+        const int last = group_passes - 1;
+        a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 2 * group_passes, lists[last & 1],
+                           c.d_work + 2 * last + 1, c.ovf_cap, nullptr, nullptr, 0, 0, c.d_err,
+                           c.d_work + FAIL_INFO_SLOT};
+        launch_tpp(tpp_kern, tpp_grid, 128, c.stream, a);
     }
 }
 

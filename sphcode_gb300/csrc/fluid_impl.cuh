@@ -67,94 +67,18 @@ __device__ __forceinline__ void hll(const T* l, const T* r, T& pstar, T& vstar)
     pstar = (c1 * c5 - c2 * c4) * c3;
 }
 
-template <int D, typename T, int TYPE, int K>
-__global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
+// FluidForce of target i (key slot) over the pair source `src`, whose next() yields each member
+// j of the target's pair set {j : r_ij < max(h_i, h_j), r_ij != 0} once, in a fixed order, with
+// the separation x_i - x_j in T, r^2, m_j and 1/h_j.  Writes acc and du/dt of i when active.
+template <int D, typename T, int TYPE, int K, class Src>
+__device__ __forceinline__ void fluid_target(const FluidArgs<T>& a, int i, int run, bool active, Src& src)
 {
     using V4 = typename Vec4<T>::type;
     using KF = Kern<D, K, T>;
-    extern __shared__ __align__(16) unsigned char smem[];
-    const SmemLayout L = a.L;
-    GroupMisc* gm = reinterpret_cast<GroupMisc*>(smem + L.off_misc);
-    const Tile<T> tile = tile_of<T>(smem, L);
     const State& st = a.st;
-    const int t = threadIdx.x;
-    const int GT = blockDim.x;
-
-    for (;;) {
-        int gb, gn;
-        if (!next_group(gm, a.work, gb, gn)) break;
-        if (gn == 0) continue;   // the unused half of an unsplit chunk
-        // targets interleaved over the CTA's warps (warp w takes every (GT/32)-th target), so
-        // that the warps meet at the next group's barrier with similar amounts of work
-        const int tl = (t & 31) * (GT >> 5) + (t >> 5);
-        const bool active = tl < gn;
-        const int i = gb + (active ? tl : 0);
-        double xi[D];
-#pragma unroll
-        for (int k = 0; k < D; ++k) xi[k] = st.f[F_POS + k][i];
-        const double hi = st.f[F_SML][i];
-        group_box<D>(gm, xi, active, hi, a.pb);
-        const int run = st.run[gb];
-        if (!group_walk<D, T>(smem, L, gm, a.tv, run, true, a.pb)) { report_overflow(a.work, gb, gn, gm); continue; }
-        {
-            // keep sources within max(R, h_j) of the group box
-            BoxAccept<D, T> box;
-            box.init(gm);
-            const T Rt = to_T_up<T>(gm->R);
-            const T* hmir = a.hmir;
-            const int ntile = stage_sources<D, T>(smem, L, gm, a.xrel, tile, [&](int j, const T* off) {
-                const T hj = hmir[j];
-                return box(off, Rt > hj ? Rt : hj);
-            }, [&](int j) { return a.rec0[j].w; });
-            if (ntile < 0) { report_overflow(a.work, gb, gn, gm); continue; }
-            gm->ntile = ntile;
-        }
-        const int ntile = gm->ntile;
-        const int nw = (ntile + 31) >> 5;
-
-        // Relative guard band of the T-precision test r^2 < H^2 for H = max(h_i, h_j) >= h_min
-        // of the group: the component error E (comp_err) at separations ~H is below e_rel H, so
-        // |r2_T - r2| < delta H^2 there.
-        // (in the FP32 form formed in FP32 and widened by 0.1 %: a wider band only sends more
-        // pairs to the exact test, and an FP64 divide per target costs 1/64-rate cycles)
-        T delta;
-        {
-            const T hm = (T)gm->rmin;
-            const T e_rel = (T)comp_err<T>(gm, gm->rmin) / hm * T(1.001) + (T)(Unit<T>::u * 3.0);
-            delta = T(2.002) * (T(2.0 * 1.7320508075688772) * e_rel + T(D) * e_rel * e_rel + (T)(8.0 * Unit<T>::u));
-        }
-        const T dlo = T(1) - delta, dhi = T(1) + delta;
-
-        T xo[D];
-#pragma unroll
-        for (int k = 0; k < D; ++k) xo[k] = (T)min_image(xi[k] - gm->gc[k], a.pb, k);
-        const V4 r0i = a.rec0[i], r1i = a.rec1[i], r2i = a.rec2[i];
-        const T vi[3] = {r0i.x, r0i.y, r0i.z};
-        const T hinv_i = r0i.w;
-
-        // ---- pair candidates: r^2 < max(h_i, h_j)^2 (1 + delta), j != i ----
-        unsigned long long wmask = 0ull;   // words holding candidates (tiles of at most 64 words)
-        for (int w = 0; w < nw; ++w) {
-            unsigned bits = 0;
-            // the word's smallest 1/h_j bounds every source's 1/max(h_i, h_j) from below
-            const T wmin = D == 3 ? tile.wbox[2 * w].w : hinv_i;
-            const T Hw = hinv_i < wmin ? hinv_i : wmin;
-            if (word_box_r2<D, T>(xo, tile, w) * (Hw * Hw) < dhi) {
-                const int smax = min(32, ntile - w * 32);
-                for (int b = 0; b < smax; ++b) {
-                    const int s = w * 32 + b;
-                    T r[D];
-                    const T r2 = tile_r2<D, T>(xo, tile.pm[s], r);
-                    const T hinv_j = tile.aux[s];
-                    const T Hinv = hinv_i < hinv_j ? hinv_i : hinv_j;   // 1 / max(h_i, h_j)
-                    if (r2 * (Hinv * Hinv) < dhi) bits |= 1u << b;
-                }
-            }
-            if (!active) bits = 0u;
-            tile.mask[w * GT + t] = bits;
-            if (bits && w < 64) wmask |= 1ull << w;
-        }
-
+    const V4 r0i = a.rec0[i], r1i = a.rec1[i], r2i = a.rec2[i];
+    const T vi[3] = {r0i.x, r0i.y, r0i.z};
+    const T hinv_i = r0i.w;
         const T rho_i = r1i.x, p_i = r1i.y, c_i = r1i.z, X_i = r1i.w;
         const T al_i = r2i.x, b_i = r2i.y, u_i = r2i.z;
         const T m_i = (T)st.f[F_MASS][i];
@@ -178,31 +102,16 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
         for (int k = 0; k < D; ++k) acc[k].zero();
         dene.zero();
 
-        // 3D tiles hold many words without candidates for a target; in 2D the plain scan is cheaper
-        typename std::conditional<D == 3, MaskWordIter, MaskIter>::type it(tile.mask, GT, t, nw, wmask);
-        int s;
-        while (it.next(s)) {
+        T rv[D], r2, mj, hinv_j;
+        int j;
+        while (src.next(rv, r2, mj, hinv_j, j)) {
             {
-                const V4 p = tile.pm[s];
-                T rv[D];
-                const T r2 = tile_r2<D, T>(xo, p, rv);
-                const int j = tile.idx[s];
-                if (j == i) continue;
-                const T hinv_j = tile.aux[s];
-                const T Hinv = hinv_i < hinv_j ? hinv_i : hinv_j;
-                if (!(r2 * (Hinv * Hinv) < dlo) || r2 == T(0)) {
-                    const double r2x = exact_r2<D>(st, xi, j, a.pb);
-                    const double rx = __dsqrt_rn(r2x);
-                    if (rx >= fmax(hi, st.f[F_SML][j]) || rx == 0.0) continue;
-                    if (r2 == T(0)) continue;   // unresolvable in T (coincident offsets)
-                }
                 const V4 r0j = a.rec0[j];
                 const T rinv = rsqrt_t(r2);
                 const T r = r2 * rinv;
                 const T cfi = KF::dw_coef(r, rinv, hinv_i);
                 const T cfj = KF::dw_coef(r, rinv, hinv_j);
                 const V4 r1j = a.rec1[j];
-                const T mj = p.w;
                 if (TYPE == 2) {
                     // ---- Godunov SPH pair (src/gsph/g_fluid_force.cpp:79-163) ----
                     const T rho_j = r1j.x, p_j = r1j.y, c_j = r1j.z;
@@ -309,14 +218,231 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
                 }
             }
         }
-        if (a.counters) {
-            warp_count(a.counters + PC_FLUID_GROUPS, t == 0 ? 1ull : 0ull);
-            warp_count(a.counters + PC_FLUID_TESTS, active ? (unsigned long long)ntile : 0ull);
-        }
         if (active) {
 #pragma unroll
             for (int k = 0; k < D; ++k) st.f[F_ACC + k][i] = (double)acc[k].get();
             st.f[F_DENE][i] = (double)dene.get();
+        }
+}
+
+// Pair source of the group schedule: the candidate bits of target i over the CTA's staged tile,
+// each decided exactly (T test outside the guard band, the reference's FP64 test inside it).
+template <int D, typename T, class It>
+struct TileSource {
+    using V4 = typename Vec4<T>::type;
+    It it;
+    const Tile<T>* tile;
+    const State* st;
+    const Periodic* pb;
+    const double* xi;
+    const T* xo;
+    double hi;
+    T hinv_i, dlo;
+    int i;
+    __device__ __forceinline__ bool next(T* rv, T& r2, T& mj, T& hinv_j, int& j)
+    {
+        int s;
+        while (it.next(s)) {
+            const V4 p = tile->pm[s];
+            r2 = tile_r2<D, T>(xo, p, rv);
+            j = tile->idx[s];
+            if (j == i) continue;
+            hinv_j = tile->aux[s];
+            const T Hinv = hinv_i < hinv_j ? hinv_i : hinv_j;
+            if (!(r2 * (Hinv * Hinv) < dlo) || r2 == T(0)) {
+                const double r2x = exact_r2<D>(*st, xi, j, *pb);
+                const double rx = __dsqrt_rn(r2x);
+                if (rx >= fmax(hi, st->f[F_SML][j]) || rx == 0.0) continue;
+                if (r2 == T(0)) continue;   // unresolvable in T (coincident offsets)
+            }
+            mj = p.w;
+            return true;
+        }
+        return false;
+    }
+};
+
+// Pair source of the thread-per-particle schedule: the target's own walk (is_ij reach, the
+// reference's BHTree::neighbor_search with is_ij) over the particles of the leaves it reaches,
+// each decided exactly like the tile source's.
+template <int D, typename T>
+struct WalkSource {
+    using V4 = typename Vec4<T>::type;
+    TargetWalk<D, T> w;
+    const V4* xrel;
+    const V4* rec0;
+    const T* hmir;
+    const State* st;
+    const Periodic* pb;
+    double hi;
+    T hiT;
+    int i;
+    __device__ __forceinline__ bool next(T* rv, T& r2, T& mj, T& hinv_j, int& j)
+    {
+        int jj;
+        while (w.next(jj)) {
+            if (jj == i) continue;
+            const V4 q = xrel[jj];
+            r2 = w.sep(q, rv);
+            const T hj = hmir[jj];
+            const T H = hiT > hj ? hiT : hj;
+            const T band = w.band(H);
+            if (!(r2 < H * H - band) || r2 == T(0)) {
+                if (r2 > H * H + band) continue;
+                const double r2x = exact_r2<D>(*st, w.xi, jj, *pb);
+                const double rx = __dsqrt_rn(r2x);
+                if (rx >= fmax(hi, st->f[F_SML][jj]) || rx == 0.0) continue;
+                if (r2 == T(0)) continue;
+            }
+            j = jj;
+            mj = q.w;
+            hinv_j = rec0[jj].w;
+            return true;
+        }
+        return false;
+    }
+};
+
+template <int D, typename T, int TYPE, int K>
+__global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
+{
+    using V4 = typename Vec4<T>::type;
+    using KF = Kern<D, K, T>;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const SmemLayout L = a.L;
+    GroupMisc* gm = reinterpret_cast<GroupMisc*>(smem + L.off_misc);
+    const Tile<T> tile = tile_of<T>(smem, L);
+    const State& st = a.st;
+    const int t = threadIdx.x;
+    const int GT = blockDim.x;
+
+    for (;;) {
+        int gb, gn;
+        if (!next_group(gm, a.work, gb, gn)) break;
+        if (gn == 0) continue;   // the unused half of an unsplit chunk
+        // targets interleaved over the CTA's warps (warp w takes every (GT/32)-th target), so
+        // that the warps meet at the next group's barrier with similar amounts of work
+        const int tl = (t & 31) * (GT >> 5) + (t >> 5);
+        const bool active = tl < gn;
+        const int i = gb + (active ? tl : 0);
+        double xi[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) xi[k] = st.f[F_POS + k][i];
+        const double hi = st.f[F_SML][i];
+        group_box<D>(gm, xi, active, hi, a.pb);
+        const int run = st.run[gb];
+        if (!group_walk<D, T>(smem, L, gm, a.tv, run, true, a.pb)) { report_overflow(a.work, gb, gn, gm); continue; }
+        {
+            // keep sources within max(R, h_j) of the group box
+            BoxAccept<D, T> box;
+            box.init(gm);
+            const T Rt = to_T_up<T>(gm->R);
+            const T* hmir = a.hmir;
+            const int ntile = stage_sources<D, T>(smem, L, gm, a.xrel, tile, [&](int j, const T* off) {
+                const T hj = hmir[j];
+                return box(off, Rt > hj ? Rt : hj);
+            }, [&](int j) { return a.rec0[j].w; });
+            if (ntile < 0) { report_overflow(a.work, gb, gn, gm); continue; }
+            gm->ntile = ntile;
+        }
+        const int ntile = gm->ntile;
+        const int nw = (ntile + 31) >> 5;
+
+        // Relative guard band of the T-precision test r^2 < H^2 for H = max(h_i, h_j) >= h_min
+        // of the group: the component error E (comp_err) at separations ~H is below e_rel H, so
+        // |r2_T - r2| < delta H^2 there.
+        // (in the FP32 form formed in FP32 and widened by 0.1 %: a wider band only sends more
+        // pairs to the exact test, and an FP64 divide per target costs 1/64-rate cycles)
+        T delta;
+        {
+            const T hm = (T)gm->rmin;
+            const T e_rel = (T)comp_err<T>(gm, gm->rmin) / hm * T(1.001) + (T)(Unit<T>::u * 3.0);
+            delta = T(2.002) * (T(2.0 * 1.7320508075688772) * e_rel + T(D) * e_rel * e_rel + (T)(8.0 * Unit<T>::u));
+        }
+        const T dlo = T(1) - delta, dhi = T(1) + delta;
+
+        T xo[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) xo[k] = (T)min_image(xi[k] - gm->gc[k], a.pb, k);
+        const T hinv_i = a.rec0[i].w;
+
+        // ---- pair candidates: r^2 < max(h_i, h_j)^2 (1 + delta), j != i ----
+        unsigned long long wmask = 0ull;   // words holding candidates (tiles of at most 64 words)
+        for (int w = 0; w < nw; ++w) {
+            unsigned bits = 0;
+            // the word's smallest 1/h_j bounds every source's 1/max(h_i, h_j) from below
+            const T wmin = D == 3 ? tile.wbox[2 * w].w : hinv_i;
+            const T Hw = hinv_i < wmin ? hinv_i : wmin;
+            if (word_box_r2<D, T>(xo, tile, w) * (Hw * Hw) < dhi) {
+                const int smax = min(32, ntile - w * 32);
+                for (int b = 0; b < smax; ++b) {
+                    const int s = w * 32 + b;
+                    T r[D];
+                    const T r2 = tile_r2<D, T>(xo, tile.pm[s], r);
+                    const T hinv_j = tile.aux[s];
+                    const T Hinv = hinv_i < hinv_j ? hinv_i : hinv_j;   // 1 / max(h_i, h_j)
+                    if (r2 * (Hinv * Hinv) < dhi) bits |= 1u << b;
+                }
+            }
+            if (!active) bits = 0u;
+            tile.mask[w * GT + t] = bits;
+            if (bits && w < 64) wmask |= 1ull << w;
+        }
+
+        // 3D tiles hold many words without candidates for a target; in 2D the plain scan is cheaper
+        using It = typename std::conditional<D == 3, MaskWordIter, MaskIter>::type;
+        TileSource<D, T, It> src{It(tile.mask, GT, t, nw, wmask), &tile, &st, &a.pb, xi, xo, hi, hinv_i, dlo, i};
+        fluid_target<D, T, TYPE, K>(a, i, run, active, src);
+        if (a.counters) {
+            warp_count(a.counters + PC_FLUID_GROUPS, t == 0 ? 1ull : 0ull);
+            warp_count(a.counters + PC_FLUID_TESTS, active ? (unsigned long long)ntile : 0ull);
+        }
+    }
+}
+
+// The thread-per-particle schedule: a warp takes a target range (the group list, or the ranges
+// an earlier group pass could not fit) and each lane one target, which walks the octree itself
+// and sums its pairs straight from the per-particle mirrors (no shared staging, no capacity but
+// the walk stack's).
+template <int D, typename T, int TYPE, int K>
+__global__ void __launch_bounds__(128) fluid_tpp_kernel(FluidArgs<T> a)
+{
+    const State& st = a.st;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int k = 0;
+        if (lane == 0) k = atomicAdd(a.work.counter, 1);
+        k = __shfl_sync(FULL, k, 0);
+        int gb = -1, gn = 0;
+        if (a.work.list) {
+            if (k < min(*a.work.list_count, a.work.list_cap)) { const int2 r = a.work.list[k]; gb = r.x; gn = r.y; }
+        } else if (k < *a.work.n_groups) {
+            gb = a.work.g_begin[k];
+            gn = a.work.g_count[k];
+        }
+        if (gb < 0) break;
+        for (int o = 0; o < gn; o += 32) {
+            const bool active = o + lane < gn;
+            const int i = gb + (active ? o + lane : 0);
+            double xi[D];
+#pragma unroll
+            for (int q = 0; q < D; ++q) xi[q] = st.f[F_POS + q][i];
+            const double hi = st.f[F_SML][i];
+            const int run = st.run[i];
+            int stk[WALK_STACK];
+            WalkSource<D, T> src;
+            src.w.start(stk, a.tv, a.pb, xi, run, hi, true);
+            if (!active) src.w.sp = 0;
+            src.xrel = a.xrel;
+            src.rec0 = a.rec0;
+            src.hmir = a.hmir;
+            src.st = &st;
+            src.pb = &a.pb;
+            src.hi = hi;
+            src.hiT = (T)hi;
+            src.i = i;
+            fluid_target<D, T, TYPE, K>(a, i, run, active, src);
+            if (src.w.overflow) atomicOr(a.work.err, (unsigned)ERR_STACK);
         }
     }
 }
@@ -404,6 +530,10 @@ void run_fluid(Ctx& c)
     launch_pair_passes<FluidArgs<T>>(c, (const void*)kern, a, tcap, sizeof(V4), sizeof(T),
         [](const void* k, int grid, int block, size_t smem, cudaStream_t st, FluidArgs<T>& args) {
             reinterpret_cast<void (*)(FluidArgs<T>)>(const_cast<void*>(k))<<<grid, block, smem, st>>>(args);
+        },
+        (const void*)fluid_tpp_kernel<D, T, TYPE, K>,
+        [](const void* k, int grid, int block, cudaStream_t st, FluidArgs<T>& args) {
+            reinterpret_cast<void (*)(FluidArgs<T>)>(const_cast<void*>(k))<<<grid, block, 0, st>>>(args);
         });
 }
 

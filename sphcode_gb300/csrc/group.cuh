@@ -638,6 +638,114 @@ __device__ int stage_sources(unsigned char* smem, const SmemLayout& L, GroupMisc
     return base;
 }
 
+// ---- thread-per-particle walk -----------------------------------------------------------------
+// The octree walk of one target on its own (the thread-per-particle schedule): a depth-first walk
+// with a per-thread stack that visits the particles of every leaf whose box can lie within the
+// reach of x_i per axis (BHTree::neighbor_search, src/bhtree.cpp:239-249; reach = r, or
+// max(r, node kernel size) with use_ksize), tested in FP32 on the node mirrors with a relative
+// margin and an absolute slack that keep every node the exact FP64 test keeps.  For each leaf the
+// offset of its centre from x_i is formed once in FP64 and rounded to T, so a source's separation
+// is x_j - x_i = coff + (x_j - leaf centre) with the second term from the per-particle mirror.
+constexpr int WALK_STACK = 160;   // 7 waiting siblings per level of a 21-level 3D octree, and more
+
+template <int D, typename T>
+struct TargetWalk {
+    const TreeView* tv;
+    const Periodic* pb;
+    double xi[D];
+    float xf[D];
+    float slack, rf, xmag;
+    bool use_ksize;
+    bool overflow;
+    int sp, jb, je;
+    T coff[D];   // leaf centre - x_i
+    T bq;        // bound on |x_j - leaf centre| per axis for the current leaf
+    T amax;      // max_k |coff_k| + bq of the current leaf
+    int* stack;  // WALK_STACK entries owned by the caller (a local array, so that the walker's
+                 // scalars can stay in registers)
+
+    __device__ __forceinline__ void start(int* stk, const TreeView& t, const Periodic& p, const double* x, int root,
+                                          double r, bool ksize)
+    {
+        stack = stk;
+        tv = &t;
+        pb = &p;
+        float mag = 0.f;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            xi[k] = x[k];
+            xf[k] = (float)x[k];
+            mag = fmaxf(mag, fabsf(xf[k]) + (p.on ? p.lenf[k] : 0.f));
+        }
+        xmag = mag;
+        slack = 4.0f * 5.9604645e-08f * mag + 1e-30f;
+        rf = __double2float_ru(r);
+        use_ksize = ksize;
+        overflow = false;
+        stack[0] = root;
+        sp = 1;
+        jb = je = 0;
+    }
+
+    // The next particle (key slot j) of a walked leaf; false when the walk is done.
+    __device__ __forceinline__ bool next(int& j)
+    {
+        while (jb >= je) {
+            if (sp == 0) return false;
+            const int node = stack[--sp];
+            if (tv->count[node] <= 0) continue;
+            const float e2 = 0.5f * tv->ef[node];
+            const float reach = use_ksize ? fmaxf(rf, tv->kf[node]) : rf;
+            bool hit = true;
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+                const float d = fabsf(min_image_f(tv->cf[k][node] - xf[k], *pb, k));
+                if (d > (e2 + reach) * 1.00001f + slack) hit = false;
+            }
+            if (!hit) continue;
+            const int fc = tv->first_child[node];
+            if (fc < 0) {
+                jb = tv->begin[node];
+                je = jb + tv->count[node];
+                T am = T(0);
+#pragma unroll
+                for (int k = 0; k < D; ++k) {
+                    coff[k] = (T)min_image(tv->center[k][node] - xi[k], *pb, k);
+                    am = fmax(am, fabs(coff[k]));
+                }
+                bq = (T)(0.5 * tv->edge[node] * (1.0 + 1e-6));
+                amax = am + bq;
+            } else {
+                const int nc = tv->nchild[node];
+                if (sp + nc > WALK_STACK) { overflow = true; sp = 0; jb = je = 0; return false; }
+                for (int c = nc - 1; c >= 0; --c) stack[sp++] = fc + c;
+            }
+        }
+        j = jb++;
+        return true;
+    }
+
+    // Separation x_i - x_j in T of slot j of the current leaf (q = its {x_j - leaf centre, m}) and
+    // the bound on the rounding error of r^2 = |x_i - x_j|^2 for separations up to rmax.
+    template <class V4>
+    __device__ __forceinline__ T sep(const V4& q, T* rv) const
+    {
+        rv[0] = -(coff[0] + q.x);
+        T r2 = rv[0] * rv[0];
+        if (D > 1) { rv[D > 1 ? 1 : 0] = -(coff[D > 1 ? 1 : 0] + q.y); r2 = fma(rv[D > 1 ? 1 : 0], rv[D > 1 ? 1 : 0], r2); }
+        if (D > 2) { rv[D > 2 ? 2 : 0] = -(coff[D > 2 ? 2 : 0] + q.z); r2 = fma(rv[D > 2 ? 2 : 0], rv[D > 2 ? 2 : 0], r2); }
+        return r2;
+    }
+    __device__ __forceinline__ T band(T rmax) const
+    {
+        // per component: rounding of coff and of the sum, below 2 u (|coff| + bq), plus the FP64
+        // rounding of the centre offset against the coordinate scale
+        const T u = T(Unit<T>::u);
+        const T E = T(2.5) * u * amax + T(8.0 * Unit<double>::u) * (amax + T(xmag));
+        return T(2.0 * 1.7320508075688772) * E * rmax + T(D) * E * E + T(D + 3) * u * rmax * rmax;
+    }
+};
+
 // ---- exact FP64 decisions for the guard band ---------------------------------------------------
 template <int D>
 __device__ __forceinline__ double exact_r2(const State& st, const double* xi, int j, const Periodic& pb)

@@ -54,6 +54,439 @@ __device__ __forceinline__ double h_guess(double nn, double m, double rho)
     return pow(x, 1.0 / 3.0);
 }
 
+// Pair source of the group schedule: the candidate bits of the target over the CTA's staged
+// tile (exact candidates, see pre_kernel); restrict() clears the bits beyond h (T test outside
+// the guard band, the reference's FP64 r < h inside it, in a loop of its own) so that the member
+// loops run without divergence on non-members.
+template <int D, typename T>
+struct TilePreSource {
+    using V4 = typename Vec4<T>::type;
+    const Tile<T>* tile;
+    const State* st;
+    const Periodic* pb;
+    const V4* mvel;
+    const double* xi;
+    const T* xo;
+    int gt, t, nw;
+    unsigned long long wmask;
+    const GroupMisc* gm;
+
+    template <class F>
+    __device__ __forceinline__ void newton_pass(F f)
+    {
+        MaskWordIter it(tile->mask, gt, t, nw, wmask);
+        int sa, sb;
+        while (it.next(sa)) {
+            const bool two = it.next(sb);
+            T r[D];
+            const V4 pa = tile->pm[sa];
+            const T rra = sqrt(tile_r2<D, T>(xo, pa, r));
+            T rrb = T(0), mb = T(0);
+            if (two) {
+                const V4 pb_ = tile->pm[sb];
+                rrb = sqrt(tile_r2<D, T>(xo, pb_, r));
+                mb = pb_.w;
+            }
+            f(rra, pa.w, rrb, mb, two);
+        }
+    }
+
+    __device__ __forceinline__ void restrict(double hf)
+    {
+        const double hf2 = __dmul_rn(hf, hf);
+        const double band = r2_band<T, D>(gm, hf);
+        const T lo_t = to_T_down<T>(hf2 - band), hi_t = to_T_up<T>(hf2 + band);
+        bool in_band = false;
+        {
+            MaskWordIter it(tile->mask, gt, t, nw, wmask);
+            int s;
+            while (it.next(s)) {
+                T r[D];
+                const T r2 = tile_r2<D, T>(xo, tile->pm[s], r);
+                if (r2 > hi_t) it.clear(s);
+                else in_band |= !(r2 < lo_t);
+            }
+        }
+        if (in_band) {
+            MaskWordIter it(tile->mask, gt, t, nw, wmask);
+            int s;
+            while (it.next(s)) {
+                T r[D];
+                const T r2 = tile_r2<D, T>(xo, tile->pm[s], r);
+                if (!(r2 < lo_t) && !(__dsqrt_rn(exact_r2<D>(*st, xi, tile->idx[s], *pb)) < hf)) it.clear(s);
+            }
+        }
+    }
+
+    template <class F>
+    __device__ __forceinline__ void for_members(bool load_v, F f)
+    {
+        // the next member's velocity record is loaded before the current one is evaluated
+        MaskWordIter it(tile->mask, gt, t, nw, wmask);
+        int snext;
+        bool have = it.next(snext);
+        V4 vq{};
+        if (have && load_v) vq = mvel[tile->idx[snext]];
+        while (have) {
+            const int s = snext;
+            const V4 vjr = vq;
+            have = it.next(snext);
+            if (have && load_v) vq = mvel[tile->idx[snext]];
+            const V4 p = tile->pm[s];
+            T r[D];
+            const T r2 = tile_r2<D, T>(xo, p, r);
+            f(r, r2, p.w, tile->aux[s], tile->idx[s], vjr);
+        }
+    }
+};
+
+// Pair source of the thread-per-particle schedule: the target's own walk (search radius h_s, the
+// reference's BHTree::neighbor_search without is_ij), once per pass; candidates r_ij^2 < h_s^2
+// and members r_ij < h decided exactly (T test outside the walker's guard band, the reference's
+// FP64 arithmetic inside it).
+template <int D, typename T>
+struct WalkPreSource {
+    using V4 = typename Vec4<T>::type;
+    const TreeView* tv;
+    const Periodic* pb;
+    const State* st;
+    const V4* xrel;
+    const V4* mvel;
+    const T* mu;
+    const double* xi;
+    double hs, hf;
+    int root;
+    bool active, restricted;
+
+    // next candidate (or member, once restricted) of the walk w: separation, r^2 and slot
+    __device__ __forceinline__ bool next(TargetWalk<D, T>& w, T* r, T& r2, V4& q, int& j)
+    {
+        const double hs2 = __dmul_rn(hs, hs);
+        const T hsT = (T)hs, hfT = (T)hf;
+        while (w.next(j)) {
+            q = xrel[j];
+            r2 = w.sep(q, r);
+            const T bs = w.band(hsT);
+            if (r2 > hsT * hsT + bs) continue;
+            double rx2 = -1.0;
+            if (!(r2 < hsT * hsT - bs)) {
+                rx2 = exact_r2<D>(*st, xi, j, *pb);
+                if (!(rx2 < hs2)) continue;
+            }
+            if (restricted) {
+                const T bf = w.band(hfT);
+                if (r2 > hfT * hfT + bf) continue;
+                if (!(r2 < hfT * hfT - bf)) {
+                    if (rx2 < 0.0) rx2 = exact_r2<D>(*st, xi, j, *pb);
+                    if (!(__dsqrt_rn(rx2) < hf)) continue;
+                }
+            }
+            return true;
+        }
+        return false;
+    }
+
+    template <class F>
+    __device__ __forceinline__ void newton_pass(F f)
+    {
+        int stk[WALK_STACK];
+        TargetWalk<D, T> w;
+        w.start(stk, *tv, *pb, xi, root, hs, false);
+        if (!active) w.sp = 0;
+        T r[D], r2;
+        V4 q;
+        int j;
+        while (next(w, r, r2, q, j)) f(sqrt(r2), q.w, T(0), T(0), false);
+    }
+
+    __device__ __forceinline__ void restrict(double h)
+    {
+        hf = h;
+        restricted = true;
+    }
+
+    template <class F>
+    __device__ __forceinline__ void for_members(bool load_v, F f)
+    {
+        int stk[WALK_STACK];
+        TargetWalk<D, T> w;
+        w.start(stk, *tv, *pb, xi, root, fmin(hs, hf), false);
+        if (!active) w.sp = 0;
+        T r[D], r2;
+        V4 q;
+        int j;
+        while (next(w, r, r2, q, j)) {
+            const V4 vj = load_v ? mvel[j] : V4{};
+            f(r, r2, q.w, mu[j], j, vj);
+        }
+    }
+};
+
+// PreInteraction of target i (key slot) from its smoothing-length guess hg and search radius hs,
+// over the pair source `src`:
+//   newton_pass(f): f(r_a, m_a, r_b, m_b, two) for the candidates {j : r_ij < h_s} (one or two
+//                   per call, r = |x_i - x_j| in T);
+//   restrict(h):    the members from now on are the candidates with r_ij < h, decided exactly;
+//   for_members(load_v, f): f(x_i - x_j in T, r^2, m_j, u_j, j, {v_j, c_j}) for each member
+//                   ({v_j, c_j} loaded only when load_v).
+// Warp-collective (the h / v_sig minimum and the Newton loop's exit test): all 32 lanes call it.
+template <int D, typename T, int TYPE, int K, class Src>
+__device__ __forceinline__ void pre_target(const PreArgs<T>& a, int i, int run, bool active, double hg, double hs,
+                                           Src& src, int* iters_out, int* nnb_out)
+{
+    using V4 = typename Vec4<T>::type;
+    using KF = Kern<D, K, T>;
+    const State& st = a.st;
+    const double mi = st.f[F_MASS][i];
+        // ---- smoothing length: Newton-Raphson on rho h^D = b (or n h^D = b for disph) ----
+        double h = hg;
+        int iters = 0;
+        if (!a.initial && a.iterative) {
+            // N / A_D is a constant: one FP64 division per launch, not per target
+            const T bconst = (T)((TYPE == 1) ? a.nn_over_a : mi * a.nn_over_a);
+            bool done = !active, conv = false;
+            for (int it = 0; it < 10; ++it) {
+                if (!__any_sync(FULL, !done)) break;
+                if (!done) {
+                    ++iters;
+                    const T hT = (T)h;
+                    const T hinvT = T(1) / hT;
+                    Sum<T> s0, s1;
+                    s0.zero();
+                    s1.zero();
+                    // two candidates per call where the source pairs them: independent
+                    // dependency chains, one compensated add per call
+                    src.newton_pass([&](T rra, T ma, T rrb, T mb, bool two) {
+                        T w = T(0), dw = T(0);
+                        {
+                            const T m = TYPE == 1 ? T(1) : ma;
+                            const T W = KF::w(rra, hinvT), dW = KF::dhw(rra, hinvT);
+                            if (rra < hT) { w = m * W; dw = m * dW; }
+                        }
+                        if (two) {
+                            const T m = TYPE == 1 ? T(1) : mb;
+                            const T W = KF::w(rrb, hinvT), dW = KF::dhw(rrb, hinvT);
+                            if (rrb < hT) { w += m * W; dw += m * dW; }
+                        }
+                        s0.add(w);
+                        s1.add(dw);
+                    });
+                    const T dens = (T)s0.get(), ddens = (T)s1.get();
+                    const T hd = powD<D>(hT);
+                    const T hd1 = D == 1 ? T(1) : D == 2 ? hT : hT * hT;
+                    const T f = dens * hd - bconst;
+                    const T df = ddens * hd + T(D) * dens * hd1;
+                    const double hn = h - (double)(f / df);
+                    if (fabs(hn - h) < (hn + h) * 1e-4) { done = true; conv = true; }
+                    h = hn;
+                }
+            }
+            if (active && !conv) {
+                h = hg;   // PreInteraction::newton_raphson falls back to the unscaled guess
+                atomicAdd(a.newton_fail, 1);
+            }
+        }
+        const double hf = a.initial ? hg : (a.iterative ? h : hs);
+
+        // ---- density, pressure, grad-h, signal velocity over {r < h} ----
+        const T hT = (T)hf;
+        const T hinvT = T(1) / hT;   // in the pair type (the FP64 divide costs 1/64-rate cycles)
+        const T ciT = a.mvel[i].w;
+        const T uiT = a.mu[i];
+        T vi[3] = {T(0), T(0), T(0)};
+        {
+            const V4 v = a.mvel[i];
+            vi[0] = v.x; vi[1] = v.y; vi[2] = v.z;
+        }
+        Sum<T> sd, sdh, sn, sp, sdp, sdn;
+        sd.zero(); sdh.zero(); sn.zero(); sp.zero(); sdp.zero(); sdn.zero();
+        // the Balsara / time-dependent-alpha sums over the same set {r < h}, accumulated in the
+        // same pass (src/pre_interaction.cpp:115-161 normalise them only afterwards)
+        const bool bal = a.use_balsara && D != 1;
+        const bool avsum = TYPE != 2 && !a.initial && (bal || a.use_tdav);
+        Sum<T> sdiv, srot[3];
+        sdiv.zero(); srot[0].zero(); srot[1].zero(); srot[2].zero();
+        T vsig = T(2) * ciT;
+        int nnb = 0;
+        {
+            src.restrict(hf);
+            src.for_members(!a.initial, [&](const T* r, T r2, T mj, T auxj, int j, const V4& vjr) {
+                ++nnb;
+                const T rr = sqrt(r2);
+                const T W = KF::w(rr, hinvT);
+                sd.add(mj * W);
+                if (TYPE == 0) {
+                    if (!a.initial) sdh.add(mj * KF::dhw(rr, hinvT));
+                } else if (TYPE == 1) {
+                    if (!a.initial) {
+                        const T dW = KF::dhw(rr, hinvT);
+                        const T muj = mj * auxj;
+                        sn.add(W);
+                        sp.add(muj * W);
+                        sdp.add(muj * dW);
+                        sdn.add(dW);
+                    }
+                }
+                if (!a.initial && j != i) {
+                    const V4 vj = vjr;
+                    T vij[3] = {T(0), T(0), T(0)};
+                    vij[0] = vi[0] - vj.x;
+                    if (D > 1) vij[1] = vi[1] - vj.y;
+                    if (D > 2) vij[2] = vi[2] - vj.z;
+                    T rv = r[0] * vij[0];
+                    if (D > 1) rv += r[D > 1 ? 1 : 0] * vij[1];
+                    if (D > 2) rv += r[D > 2 ? 2 : 0] * vij[2];
+                    const T vs = ciT + vj.w - T(3) * rv * (T(1) / rr);
+                    vsig = vs > vsig ? vs : vsig;
+                    if (avsum) {
+                        // grad W = r_ij cf; the particle itself contributes dW = 0
+                        const T cf = KF::dw_coef(rr, rr > T(0) ? T(1) / rr : T(0), hinvT);
+                        const T wj = (TYPE == 1) ? mj * auxj : mj;
+                        T dw[3] = {T(0), T(0), T(0)};
+#pragma unroll
+                        for (int k = 0; k < D; ++k) dw[k] = r[k] * cf;
+                        T vd = vij[0] * dw[0];
+                        if (D > 1) vd += vij[1] * dw[1];
+                        if (D > 2) vd += vij[2] * dw[2];
+                        sdiv.add(-wj * vd);
+                        if (bal) {
+                            if (D == 2) {
+                                srot[0].add((vij[0] * dw[1] - vij[1] * dw[0]) * wj);
+                            } else if (D == 3) {
+                                srot[0].add((vij[1] * dw[2] - vij[2] * dw[1]) * wj);
+                                srot[1].add((vij[2] * dw[0] - vij[0] * dw[2]) * wj);
+                                srot[2].add((vij[0] * dw[1] - vij[1] * dw[0]) * wj);
+                            }
+                        }
+                    }
+                }
+            });
+        }
+        *iters_out = iters;
+        *nnb_out = nnb;
+        if (a.initial) {
+            if (active) {
+                st.f[F_SML][i] = hf;
+                st.f[F_DENS][i] = (double)sd.get();
+            }
+            return;
+        }
+        const double dens = (double)sd.get();
+        const T densT = (T)dens;
+        double pres;
+        T gradh = T(0);
+        if (TYPE == 0) {
+            pres = (a.gamma - 1.0) * dens * (double)st.f[F_ENE][i];
+            gradh = T(1) / (T(1) + hT / (T(D) * densT) * (T)sdh.get());
+        } else if (TYPE == 1) {
+            const T n_i = (T)sn.get();
+            pres = (a.gamma - 1.0) * (double)sp.get();
+            const T c = hT / (T(D) * n_i);
+            gradh = c * (T)sdp.get() / (T(1) + c * (T)sdn.get());
+        } else {
+            pres = (a.gamma - 1.0) * dens * (double)st.f[F_ENE][i];
+        }
+        // h / v_sig minimum of the group -> run minimum (TimeStep input)
+        {
+            // minimum over the warp in T, converted once (the minimum commutes with the conversion)
+            T hv = active ? hT / vsig : T(3.0e38f);
+            for (int o = 16; o > 0; o >>= 1) { const T u = __shfl_xor_sync(FULL, hv, o); hv = u < hv ? u : hv; }
+            if ((threadIdx.x & 31) == 0) atomicMin(&a.hvs[run], dbl_to_ord((double)hv));
+        }
+
+        if (TYPE == 2) {
+            // ---- MUSCL gradients (src/gsph/g_pre_interaction.cpp:112-136) ----
+            if (active) {
+                st.f[F_SML][i] = hf;
+                st.f[F_DENS][i] = dens;
+                st.f[F_PRES][i] = pres;
+                st.neighbor[i] = nnb;
+            }
+            if (!a.gsph_2nd) return;
+            Sum<T> dd[D], du[D], dv[D][D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+                dd[k].zero(); du[k].zero();
+#pragma unroll
+                for (int q = 0; q < D; ++q) dv[k][q].zero();
+            }
+            src.for_members(true, [&](const T* r, T r2, T mj, T auxj, int, const V4& vj) {
+                    const T rr = sqrt(r2);
+                    const T cf = KF::dw_coef(rr, rr > T(0) ? T(1) / rr : T(0), hinvT);
+                    const T vjv[3] = {vj.x, vj.y, vj.z};
+                    const T mdu = mj * (auxj - uiT);
+#pragma unroll
+                    for (int k = 0; k < D; ++k) {
+                        const T dw = r[k] * cf;
+                        dd[k].add(dw * mj);
+                        du[k].add(dw * mdu);
+                    }
+#pragma unroll
+                    for (int q = 0; q < D; ++q) {
+                        const T mv = mj * (vjv[q] - vi[q]);
+#pragma unroll
+                        for (int k = 0; k < D; ++k) dv[q][k].add(r[k] * cf * mv);
+                    }
+            });
+            if (active) {
+                const double ui = st.f[F_ENE][i];
+                const T rho_inv = T(1) / densT;
+#pragma unroll
+                for (int k = 0; k < D; ++k) {
+                    const double ddk = (double)dd[k].get();
+                    st.f[F_GRADD + k][i] = ddk;
+                    st.f[F_GRADP + k][i] = (ddk * ui + (double)du[k].get()) * (a.gamma - 1.0);
+                }
+#pragma unroll
+                for (int q = 0; q < D; ++q)
+#pragma unroll
+                    for (int k = 0; k < D; ++k) st.f[F_GRADV + q * 3 + k][i] = (double)((T)dv[q][k].get() * rho_inv);
+            }
+            return;
+        }
+
+        // ---- Balsara switch and time-dependent alpha (src/pre_interaction.cpp:115-161) ----
+        T alpha = (T)st.f[F_ALPHA][i];
+        T balsara = (T)st.f[F_BALSARA][i];
+        double alpha_out = st.f[F_ALPHA][i], balsara_out = st.f[F_BALSARA][i];
+        const T dt = (T)a.dt_run[run];
+        if (avsum) {
+            T div = (T)sdiv.get();
+            T rot[3] = {(T)srot[0].get(), (T)srot[1].get(), (T)srot[2].get()};
+            if (TYPE == 1) {
+                const T p_inv = (T)(a.gamma - 1.0) / (T)pres;
+                div *= p_inv;
+                for (int k = 0; k < 3; ++k) rot[k] *= p_inv;
+            } else {
+                const T rho_inv = T(1) / densT;
+                div *= rho_inv;
+                for (int k = 0; k < 3; ++k) rot[k] *= rho_inv;
+            }
+            const T tau_inv = (T)a.eps_av * ciT / hT;
+            if (bal) {
+                const T rot_abs = D == 2 ? fabs(rot[0]) : sqrt(rot[0] * rot[0] + rot[1] * rot[1] + rot[2] * rot[2]);
+                balsara = fabs(div) / (fabs(div) + rot_abs + T(1e-4) * ciT / hT);
+                balsara_out = (double)balsara;
+                if (a.use_tdav) {
+                    const T sdv = -div > T(0) ? -div : T(0);
+                    alpha_out = st.f[F_ALPHA][i] + (double)((-(alpha - (T)a.alpha_min) * tau_inv + sdv * ((T)a.alpha_max - alpha)) * dt);
+                }
+            } else {
+                const T s_i = -div > T(0) ? -div : T(0);
+                alpha_out = (double)((alpha + dt * tau_inv * (T)a.alpha_min + s_i * dt * (T)a.alpha_max) / (T(1) + dt * tau_inv + s_i * dt));
+            }
+        }
+        if (active) {
+            st.f[F_SML][i] = hf;
+            st.f[F_DENS][i] = dens;
+            st.f[F_PRES][i] = pres;
+            st.f[F_GRADH][i] = (double)gradh;
+            st.f[F_BALSARA][i] = balsara_out;
+            st.f[F_ALPHA][i] = alpha_out;
+            st.neighbor[i] = nnb;
+        }
+}
+
 template <int D, typename T, int TYPE, int K>
 __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
 {
@@ -143,178 +576,10 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
             }
         }
 
-        // ---- smoothing length: Newton-Raphson on rho h^D = b (or n h^D = b for disph) ----
-        double h = hg;
-        int iters = 0;
-        if (!a.initial && a.iterative) {
-            // N / A_D is a constant: one FP64 division per launch, not per target
-            const T bconst = (T)((TYPE == 1) ? a.nn_over_a : mi * a.nn_over_a);
-            bool done = !active, conv = false;
-            for (int it = 0; it < 10; ++it) {
-                if (!__any_sync(FULL, !done)) break;
-                if (!done) {
-                    ++iters;
-                    const T hT = (T)h;
-                    const T hinvT = T(1) / hT;
-                    Sum<T> s0, s1;
-                    s0.zero();
-                    s1.zero();
-                    // two candidates per trip: independent dependency chains, one compensated
-                    // add per pair
-                    MaskWordIter it(tile.mask, GT, t, nw, wmask);
-                    int sa, sb;
-                    while (it.next(sa)) {
-                        const bool two = it.next(sb);
-                        T w = T(0), dw = T(0);
-                        {
-                            const V4 p = tile.pm[sa];
-                            T r[D];
-                            const T rr = sqrt(tile_r2<D, T>(xo, p, r));
-                            const T m = TYPE == 1 ? T(1) : p.w;
-                            const T W = KF::w(rr, hinvT), dW = KF::dhw(rr, hinvT);
-                            if (rr < hT) { w = m * W; dw = m * dW; }
-                        }
-                        if (two) {
-                            const V4 p = tile.pm[sb];
-                            T r[D];
-                            const T rr = sqrt(tile_r2<D, T>(xo, p, r));
-                            const T m = TYPE == 1 ? T(1) : p.w;
-                            const T W = KF::w(rr, hinvT), dW = KF::dhw(rr, hinvT);
-                            if (rr < hT) { w += m * W; dw += m * dW; }
-                        }
-                        s0.add(w);
-                        s1.add(dw);
-                    }
-                    const T dens = (T)s0.get(), ddens = (T)s1.get();
-                    const T hd = powD<D>(hT);
-                    const T hd1 = D == 1 ? T(1) : D == 2 ? hT : hT * hT;
-                    const T f = dens * hd - bconst;
-                    const T df = ddens * hd + T(D) * dens * hd1;
-                    const double hn = h - (double)(f / df);
-                    if (fabs(hn - h) < (hn + h) * 1e-4) { done = true; conv = true; }
-                    h = hn;
-                }
-            }
-            if (active && !conv) {
-                h = hg;   // PreInteraction::newton_raphson falls back to the unscaled guess
-                atomicAdd(a.newton_fail, 1);
-            }
-        }
-        const double hf = a.initial ? hg : (a.iterative ? h : hs);
-
-        // ---- density, pressure, grad-h, signal velocity over {r < h} ----
-        const T hT = (T)hf;
-        const T hinvT = T(1) / hT;   // in the pair type (the FP64 divide costs 1/64-rate cycles)
-        const T ciT = a.mvel[i].w;
-        const T uiT = a.mu[i];
-        T vi[3] = {T(0), T(0), T(0)};
-        {
-            const V4 v = a.mvel[i];
-            vi[0] = v.x; vi[1] = v.y; vi[2] = v.z;
-        }
-        Sum<T> sd, sdh, sn, sp, sdp, sdn;
-        sd.zero(); sdh.zero(); sn.zero(); sp.zero(); sdp.zero(); sdn.zero();
-        // the Balsara / time-dependent-alpha sums over the same set {r < h}, accumulated in the
-        // same pass (src/pre_interaction.cpp:115-161 normalise them only afterwards)
-        const bool bal = a.use_balsara && D != 1;
-        const bool avsum = TYPE != 2 && !a.initial && (bal || a.use_tdav);
-        Sum<T> sdiv, srot[3];
-        sdiv.zero(); srot[0].zero(); srot[1].zero(); srot[2].zero();
-        T vsig = T(2) * ciT;
-        int nnb = 0;
-        {
-            // the neighbour set {r < h} at the final h: candidates beyond it leave the mask first
-            // (T test outside the guard band, the reference's FP64 r < h inside it, in a loop of
-            // its own), so that the sums below run over neighbours only, without divergence
-            const double hf2 = __dmul_rn(hf, hf);
-            const double band = r2_band<T, D>(gm, hf);
-            const T lo_t = to_T_down<T>(hf2 - band), hi_t = to_T_up<T>(hf2 + band);
-            bool in_band = false;
-            {
-                MaskWordIter it(tile.mask, GT, t, nw, wmask);
-                int s;
-                while (it.next(s)) {
-                    T r[D];
-                    const T r2 = tile_r2<D, T>(xo, tile.pm[s], r);
-                    if (r2 > hi_t) it.clear(s);
-                    else in_band |= !(r2 < lo_t);
-                }
-            }
-            if (in_band) {
-                MaskWordIter it(tile.mask, GT, t, nw, wmask);
-                int s;
-                while (it.next(s)) {
-                    T r[D];
-                    const T r2 = tile_r2<D, T>(xo, tile.pm[s], r);
-                    if (!(r2 < lo_t) && !(__dsqrt_rn(exact_r2<D>(st, xi, tile.idx[s], a.pb)) < hf)) it.clear(s);
-                }
-            }
-            // the next neighbour's velocity record is loaded before the current one is evaluated
-            MaskWordIter it(tile.mask, GT, t, nw, wmask);
-            int snext;
-            bool have = it.next(snext);
-            V4 vq{};
-            if (have && !a.initial) vq = a.mvel[tile.idx[snext]];
-            while (have) {
-                const int s = snext;
-                const V4 vjr = vq;
-                have = it.next(snext);
-                if (have && !a.initial) vq = a.mvel[tile.idx[snext]];
-                const V4 p = tile.pm[s];
-                T r[D];
-                const T r2 = tile_r2<D, T>(xo, p, r);
-                ++nnb;
-                const int j = tile.idx[s];
-                const T rr = sqrt(r2);
-                const T W = KF::w(rr, hinvT);
-                sd.add(p.w * W);
-                if (TYPE == 0) {
-                    if (!a.initial) sdh.add(p.w * KF::dhw(rr, hinvT));
-                } else if (TYPE == 1) {
-                    if (!a.initial) {
-                        const T dW = KF::dhw(rr, hinvT);
-                        const T muj = p.w * tile.aux[s];
-                        sn.add(W);
-                        sp.add(muj * W);
-                        sdp.add(muj * dW);
-                        sdn.add(dW);
-                    }
-                }
-                if (!a.initial && j != i) {
-                    const V4 vj = vjr;
-                    T vij[3] = {T(0), T(0), T(0)};
-                    vij[0] = vi[0] - vj.x;
-                    if (D > 1) vij[1] = vi[1] - vj.y;
-                    if (D > 2) vij[2] = vi[2] - vj.z;
-                    T rv = r[0] * vij[0];
-                    if (D > 1) rv += r[D > 1 ? 1 : 0] * vij[1];
-                    if (D > 2) rv += r[D > 2 ? 2 : 0] * vij[2];
-                    const T vs = ciT + vj.w - T(3) * rv * (T(1) / rr);
-                    vsig = vs > vsig ? vs : vsig;
-                    if (avsum) {
-                        // grad W = r_ij cf; the particle itself contributes dW = 0
-                        const T cf = KF::dw_coef(rr, rr > T(0) ? T(1) / rr : T(0), hinvT);
-                        const T wj = (TYPE == 1) ? p.w * tile.aux[s] : p.w;
-                        T dw[3] = {T(0), T(0), T(0)};
-#pragma unroll
-                        for (int k = 0; k < D; ++k) dw[k] = r[k] * cf;
-                        T vd = vij[0] * dw[0];
-                        if (D > 1) vd += vij[1] * dw[1];
-                        if (D > 2) vd += vij[2] * dw[2];
-                        sdiv.add(-wj * vd);
-                        if (bal) {
-                            if (D == 2) {
-                                srot[0].add((vij[0] * dw[1] - vij[1] * dw[0]) * wj);
-                            } else if (D == 3) {
-                                srot[0].add((vij[1] * dw[2] - vij[2] * dw[1]) * wj);
-                                srot[1].add((vij[2] * dw[0] - vij[0] * dw[2]) * wj);
-                                srot[2].add((vij[0] * dw[1] - vij[1] * dw[0]) * wj);
-                            }
-                        }
-                    }
-                }
-            }
-        }
+        // ---- the target's PreInteraction over its candidate bits ----
+        TilePreSource<D, T> src{&tile, &st, &a.pb, a.mvel, xi, xo, GT, t, nw, wmask, gm};
+        int iters = 0, nnb = 0;
+        pre_target<D, T, TYPE, K>(a, i, run, active, hg, hs, src, &iters, &nnb);
         if (a.counters) {
             const bool cnt = active && !a.initial;
             warp_count(a.counters + PC_PRE_GROUPS, t == 0 ? 1ull : 0ull);
@@ -325,134 +590,47 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
             warp_count(a.counters + PC_PRE_PAIRS, cnt ? (unsigned long long)nnb : 0ull);
             warp_count(a.counters + PC_PRE_TESTS, cnt ? (unsigned long long)ntile : 0ull);
         }
-        if (a.initial) {
-            if (active) {
-                st.f[F_SML][i] = hf;
-                st.f[F_DENS][i] = (double)sd.get();
-            }
-            continue;
-        }
-        const double dens = (double)sd.get();
-        const T densT = (T)dens;
-        double pres;
-        T gradh = T(0);
-        if (TYPE == 0) {
-            pres = (a.gamma - 1.0) * dens * (double)st.f[F_ENE][i];
-            gradh = T(1) / (T(1) + hT / (T(D) * densT) * (T)sdh.get());
-        } else if (TYPE == 1) {
-            const T n_i = (T)sn.get();
-            pres = (a.gamma - 1.0) * (double)sp.get();
-            const T c = hT / (T(D) * n_i);
-            gradh = c * (T)sdp.get() / (T(1) + c * (T)sdn.get());
-        } else {
-            pres = (a.gamma - 1.0) * dens * (double)st.f[F_ENE][i];
-        }
-        // h / v_sig minimum of the group -> run minimum (TimeStep input)
-        {
-            // minimum over the warp in T, converted once (the minimum commutes with the conversion)
-            T hv = active ? hT / vsig : T(3.0e38f);
-            for (int o = 16; o > 0; o >>= 1) { const T u = __shfl_xor_sync(FULL, hv, o); hv = u < hv ? u : hv; }
-            if ((t & 31) == 0) atomicMin(&a.hvs[run], dbl_to_ord((double)hv));
-        }
+    }
+}
 
-        if (TYPE == 2) {
-            // ---- MUSCL gradients (src/gsph/g_pre_interaction.cpp:112-136) ----
-            if (active) {
-                st.f[F_SML][i] = hf;
-                st.f[F_DENS][i] = dens;
-                st.f[F_PRES][i] = pres;
-                st.neighbor[i] = nnb;
-            }
-            if (!a.gsph_2nd) continue;
-            Sum<T> dd[D], du[D], dv[D][D];
-#pragma unroll
-            for (int k = 0; k < D; ++k) {
-                dd[k].zero(); du[k].zero();
-#pragma unroll
-                for (int q = 0; q < D; ++q) dv[k][q].zero();
-            }
-            MaskWordIter it(tile.mask, GT, t, nw, wmask);
-            int s;
-            while (it.next(s)) {
-                {
-                    const V4 p = tile.pm[s];
-                    const int j = tile.idx[s];
-                    T r[D];
-                    const T rr = sqrt(tile_r2<D, T>(xo, p, r));
-                    const T cf = KF::dw_coef(rr, rr > T(0) ? T(1) / rr : T(0), hinvT);
-                    const V4 vj = a.mvel[j];
-                    const T vjv[3] = {vj.x, vj.y, vj.z};
-                    const T mdu = p.w * (tile.aux[s] - uiT);
-#pragma unroll
-                    for (int k = 0; k < D; ++k) {
-                        const T dw = r[k] * cf;
-                        dd[k].add(dw * p.w);
-                        du[k].add(dw * mdu);
-                    }
-#pragma unroll
-                    for (int q = 0; q < D; ++q) {
-                        const T mv = p.w * (vjv[q] - vi[q]);
-#pragma unroll
-                        for (int k = 0; k < D; ++k) dv[q][k].add(r[k] * cf * mv);
-                    }
-                }
-            }
-            if (active) {
-                const double ui = st.f[F_ENE][i];
-                const T rho_inv = T(1) / densT;
-#pragma unroll
-                for (int k = 0; k < D; ++k) {
-                    const double ddk = (double)dd[k].get();
-                    st.f[F_GRADD + k][i] = ddk;
-                    st.f[F_GRADP + k][i] = (ddk * ui + (double)du[k].get()) * (a.gamma - 1.0);
-                }
-#pragma unroll
-                for (int q = 0; q < D; ++q)
-#pragma unroll
-                    for (int k = 0; k < D; ++k) st.f[F_GRADV + q * 3 + k][i] = (double)((T)dv[q][k].get() * rho_inv);
-            }
-            continue;
+// The thread-per-particle schedule of PreInteraction: a warp takes a target range (the group
+// list, or the ranges an earlier group pass could not fit) and each lane one target, which walks
+// the octree itself in each pass over its candidates.
+template <int D, typename T, int TYPE, int K>
+__global__ void __launch_bounds__(128) pre_tpp_kernel(PreArgs<T> a)
+{
+    const State& st = a.st;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int k = 0;
+        if (lane == 0) k = atomicAdd(a.work.counter, 1);
+        k = __shfl_sync(FULL, k, 0);
+        int gb = -1, gn = 0;
+        if (a.work.list) {
+            if (k < min(*a.work.list_count, a.work.list_cap)) { const int2 r = a.work.list[k]; gb = r.x; gn = r.y; }
+        } else if (k < *a.work.n_groups) {
+            gb = a.work.g_begin[k];
+            gn = a.work.g_count[k];
         }
-
-        // ---- Balsara switch and time-dependent alpha (src/pre_interaction.cpp:115-161) ----
-        T alpha = (T)st.f[F_ALPHA][i];
-        T balsara = (T)st.f[F_BALSARA][i];
-        double alpha_out = st.f[F_ALPHA][i], balsara_out = st.f[F_BALSARA][i];
-        const T dt = (T)a.dt_run[run];
-        if (avsum) {
-            T div = (T)sdiv.get();
-            T rot[3] = {(T)srot[0].get(), (T)srot[1].get(), (T)srot[2].get()};
-            if (TYPE == 1) {
-                const T p_inv = (T)(a.gamma - 1.0) / (T)pres;
-                div *= p_inv;
-                for (int k = 0; k < 3; ++k) rot[k] *= p_inv;
+        if (gb < 0) break;
+        for (int o = 0; o < gn; o += 32) {
+            const bool active = o + lane < gn;
+            const int i = gb + (active ? o + lane : 0);
+            double xi[D];
+#pragma unroll
+            for (int q = 0; q < D; ++q) xi[q] = st.f[F_POS + q][i];
+            double hg;
+            if (a.work.list == nullptr) {
+                hg = h_guess<D>((double)a.nn, st.f[F_MASS][i], st.f[F_DENS][i]);
+                if (active) a.hguess[i] = hg;
             } else {
-                const T rho_inv = T(1) / densT;
-                div *= rho_inv;
-                for (int k = 0; k < 3; ++k) rot[k] *= rho_inv;
+                hg = a.hguess[i];
             }
-            const T tau_inv = (T)a.eps_av * ciT / hT;
-            if (bal) {
-                const T rot_abs = D == 2 ? fabs(rot[0]) : sqrt(rot[0] * rot[0] + rot[1] * rot[1] + rot[2] * rot[2]);
-                balsara = fabs(div) / (fabs(div) + rot_abs + T(1e-4) * ciT / hT);
-                balsara_out = (double)balsara;
-                if (a.use_tdav) {
-                    const T sdv = -div > T(0) ? -div : T(0);
-                    alpha_out = st.f[F_ALPHA][i] + (double)((-(alpha - (T)a.alpha_min) * tau_inv + sdv * ((T)a.alpha_max - alpha)) * dt);
-                }
-            } else {
-                const T s_i = -div > T(0) ? -div : T(0);
-                alpha_out = (double)((alpha + dt * tau_inv * (T)a.alpha_min + s_i * dt * (T)a.alpha_max) / (T(1) + dt * tau_inv + s_i * dt));
-            }
-        }
-        if (active) {
-            st.f[F_SML][i] = hf;
-            st.f[F_DENS][i] = dens;
-            st.f[F_PRES][i] = pres;
-            st.f[F_GRADH][i] = (double)gradh;
-            st.f[F_BALSARA][i] = balsara_out;
-            st.f[F_ALPHA][i] = alpha_out;
-            st.neighbor[i] = nnb;
+            const double hs = a.initial ? hg : hg * a.ratio;
+            const int run = st.run[i];
+            WalkPreSource<D, T> src{&a.tv, &a.pb, &st, a.xrel, a.mvel, a.mu, xi, hs, hs, run, active, false};
+            int iters = 0, nnb = 0;
+            pre_target<D, T, TYPE, K>(a, i, run, active, hg, hs, src, &iters, &nnb);
         }
     }
 }
@@ -527,6 +705,10 @@ void run_pre(Ctx& c, bool initial)
     launch_pair_passes<PreArgs<T>>(c, (const void*)kern, a, tcap, sizeof(V4), sizeof(T),
         [](const void* k, int grid, int block, size_t smem, cudaStream_t st, PreArgs<T>& args) {
             reinterpret_cast<void (*)(PreArgs<T>)>(const_cast<void*>(k))<<<grid, block, smem, st>>>(args);
+        },
+        (const void*)pre_tpp_kernel<D, T, TYPE, K>,
+        [](const void* k, int grid, int block, cudaStream_t st, PreArgs<T>& args) {
+            reinterpret_cast<void (*)(PreArgs<T>)>(const_cast<void*>(k))<<<grid, block, 0, st>>>(args);
         });
 }
 

@@ -205,3 +205,29 @@ def test_group_sizes(gpu_lib, case, group_warps):
             ref.step()
         sim.step(3)
         _compare(sim, ref, _fields(p) + ["pos", "vel", "ene"], "fp32", f"{case} gw={group_warps} 3 steps")
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("sched", [1, 2, 3])
+@pytest.mark.parametrize("case", CASES)
+def test_pair_schedules(gpu_lib, case, sched, prec):
+    """The thread-per-particle schedule (each target walks the octree itself, knob 28): after
+    the first or second group pass (1, 2) or for every target (3), with the tolerances of the
+    group schedule against the oracle."""
+    from oracle import pyoracle
+    from sphcode_gb300 import sphgpu
+    p, f = _cases()[case]()
+    ref = pyoracle.OracleSim(p, f, kind="port")
+    ref.initialize()
+    with sphgpu.GpuSimulation(p, f, precision=prec) as sim:
+        sim.set_tuning("autotune", 0)
+        sim.set_tuning("pair_sched", sched)
+        sim.initialize()
+        assert sim.get_tuning("pair_sched") == sched
+        _compare(sim, ref, _fields(p), prec, f"{case} sched={sched} initialize")
+        for _ in range(3):
+            ref.step()
+        sim.step(3)
+        _compare(sim, ref, _fields(p) + ["pos", "vel", "ene"], prec, f"{case} sched={sched} 3 steps")
+        assert_counts_match(sim.get("neighbor"), ref.get("neighbor"), ref.get("pos"), ref.get("sml"),
+                            p, 1e-12 if prec == "fp64" else 2e-5)
