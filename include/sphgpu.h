@@ -227,7 +227,10 @@ const char* sphgpu_last_error(const sphgpu_ctx* ctx);
  * ranges a pass cannot fit, halved down to single targets; 1 and 2 the first one or two group
  * passes, then the thread-per-particle kernel (each target walks the octree itself) for the
  * ranges left; 3 thread-per-particle only (PreInteraction and FluidForce alike; the tuner tries
- * all four on its chosen groups and tiles). */
+ * all four on its chosen groups and tiles);
+ * 29 tile staging of the group schedule by bulk asynchronous copies on/off: the particle records
+ * of the walked leaves reach shared memory by one cp.async.bulk per leaf (mbarrier completion,
+ * bounded waits) and are filtered in place, where they all fit the tile. */
 int sphgpu_set_tuning(sphgpu_ctx* ctx, int which, int value);
 int sphgpu_get_tuning(sphgpu_ctx* ctx, int which, int* value);
 

@@ -193,6 +193,7 @@ unsigned err_bits_to_status(unsigned bits)
     if (bits & ERR_NODE_POOL) return SPHGPU_ERR_NODE_POOL;
     if (bits & (ERR_STACK | ERR_LEAVES | ERR_TILE | ERR_LIST | ERR_GSTACK)) return SPHGPU_ERR_CAPACITY;
     if (bits & ERR_NOT_FINITE) return SPHGPU_ERR_NOT_FINITE;
+    if (bits & ERR_TIMEOUT) return SPHGPU_ERR_CUDA;
     return SPHGPU_OK;
 }
 
@@ -206,6 +207,7 @@ std::string err_bits_text(unsigned bits)
     if (bits & ERR_LIST) s += "neighbour list longer than the caller's capacity; ";
     if (bits & ERR_GSTACK) s += "gravity walk stack overflow; ";
     if (bits & ERR_NOT_FINITE) s += "non-finite value in the particle state; ";
+    if (bits & ERR_TIMEOUT) s += "a bounded wait on a bulk copy into shared memory ran out; ";
     return s;
 }
 
@@ -1255,6 +1257,7 @@ int sphgpu_set_tuning(sphgpu_ctx* h, int which, int value)
         if (value < 0 || value > 3) return SPHGPU_ERR_ARG;
         c.pair_sched = value;
         break;
+    case 29: c.bulk_stage = value != 0; break;
     case 18: c.fixed_dt = value != 0; break;
     case 19: c.aos_reuse = value != 0; break;
     case 5: c.timing = value != 0; break;
@@ -1295,6 +1298,7 @@ int sphgpu_get_tuning(sphgpu_ctx* h, int which, int* value)
     case 25: *value = c.count_work ? 1 : 0; break;
     case 27: *value = c.leaf_cap1; break;
     case 28: *value = c.pair_sched; break;
+    case 29: *value = c.bulk_stage; break;
     case 13: case 14: case 15: case 16: case 17: {
         cudaStreamSynchronize(c.stream);
         cudaMemcpy(value, c.d_work + sphgpu::FAIL_INFO_SLOT + (which - 13), sizeof(int), cudaMemcpyDeviceToHost);

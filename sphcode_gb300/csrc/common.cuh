@@ -26,6 +26,7 @@ enum ErrBit : unsigned {
     ERR_LIST = 16u,
     ERR_GSTACK = 32u,
     ERR_NOT_FINITE = 64u,
+    ERR_TIMEOUT = 128u,   // a bounded wait on an asynchronous copy ran out
 };
 
 // ------------------------------------------------------------------------------------------

@@ -147,6 +147,7 @@ struct Ctx {
     bool count_work = false;
     int leaf_cap1 = 0;              // leaf-list capacity of the first pair pass (knob 27; 0: by dimension)
     int pair_sched = 0;             // pair-kernel schedule (knob 28, see launch_pair_passes)
+    int bulk_stage = 0;             // tile staging by bulk asynchronous copies (knob 29)
     unsigned long long* d_counters = nullptr;   // PAIR_COUNTERS entries
 
     // adjoint scratch (allocated on the first adjoint call)

@@ -37,6 +37,7 @@ struct FluidArgs {
     int gsph_2nd;
     const double* dt_run;
     unsigned long long* counters;   // PairCounter slots, or nullptr (not counted)
+    int bulk_stage;                 // stage the tile with bulk asynchronous copies (knob 29)
 };
 
 // van Leer limiter (src/gsph/g_fluid_force.cpp:28-36).
@@ -315,6 +316,7 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
     const State& st = a.st;
     const int t = threadIdx.x;
     const int GT = blockDim.x;
+    if (a.bulk_stage) bulk_stage_init(gm);
 
     for (;;) {
         int gb, gn;
@@ -341,7 +343,7 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
             const int ntile = stage_sources<D, T>(smem, L, gm, a.xrel, tile, [&](int j, const T* off) {
                 const T hj = hmir[j];
                 return box(off, Rt > hj ? Rt : hj);
-            }, [&](int j) { return a.rec0[j].w; });
+            }, [&](int j) { return a.rec0[j].w; }, a.bulk_stage != 0, a.work.err);
             if (ntile < 0) { report_overflow(a.work, gb, gn, gm); continue; }
             gm->ntile = ntile;
         }
@@ -526,6 +528,7 @@ void run_fluid(Ctx& c)
     a.gsph_2nd = c.p.gsph_2nd_order;
     a.dt_run = c.d_dt;
     a.counters = c.count_work ? c.d_counters : nullptr;
+    a.bulk_stage = c.bulk_stage;
     const int tcap = c.tile_cap ? c.tile_cap : fluid_default_tile_cap<D>();
     launch_pair_passes<FluidArgs<T>>(c, (const void*)kern, a, tcap, sizeof(V4), sizeof(T),
         [](const void* k, int grid, int block, size_t smem, cudaStream_t st, FluidArgs<T>& args) {

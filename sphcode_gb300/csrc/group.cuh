@@ -68,6 +68,8 @@ struct SmemLayout {
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
 struct GroupMisc {
+    unsigned long long mbar;   // mbarrier of the bulk-copy staging (initialised by bulk_stage_init)
+    unsigned mbar_phase;       // parity of its current phase
     double gc[3];
     double he[3];
     double R;           // group search radius (max over targets)
@@ -494,15 +496,51 @@ struct BoxAccept {
     }
 };
 
+// ---- bulk copies (cp.async.bulk with mbarrier completion) ----------------------------------------
+__device__ __forceinline__ unsigned smem_addr(const void* p)
+{
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+
+// Once per CTA, before the first group (block-wide).
+__device__ __forceinline__ void bulk_stage_init(GroupMisc* gm)
+{
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(&gm->mbar)) : "memory");
+        gm->mbar_phase = 0u;
+    }
+    __syncthreads();
+}
+
+// Bounded wait for the given phase of the staging mbarrier; false when it ran out.
+__device__ __forceinline__ bool bulk_wait(const GroupMisc* gm, unsigned phase, int limit)
+{
+    const unsigned addr = smem_addr(&gm->mbar);
+    for (int it = 0; it < limit; ++it) {
+        unsigned done;
+        asm volatile("{\n\t.reg .pred p;\n\t"
+                     "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(done) : "r"(addr), "r"(phase) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
 // ---- 3. staging -------------------------------------------------------------------------------
 // Flattens the leaf ranges and calls, for each particle j (key slot) in deterministic order,
 // accept(j, off) with off[k] = (leaf centre - gc) + (x_j - leaf centre) in T; accepted sources
 // get consecutive tile slots with their offsets, mass (xrel[j].w) and aux(j).  Returns the tile
 // count, or -1 on overflow.
+// With bulk (the CTA ran bulk_stage_init) and when all particles of the walked leaves fit the tile,
+// the leaves' records are brought into the tile by bulk asynchronous copies (one cp.async.bulk per
+// leaf, completion counted on the CTA's mbarrier) and filtered in place, instead of by each thread's
+// own loads; the accepted sources, their slots and their order are the same.  A copy wait that
+// runs out (bounded twice) raises ERR_TIMEOUT in *err and sends the range to a later pass.
 template <int D, typename T, class Accept, class Aux>
 __device__ int stage_sources(unsigned char* smem, const SmemLayout& L, GroupMisc* gm,
                              const typename Vec4<T>::type* xrel, const Tile<T>& tile,
-                             Accept accept, Aux aux)
+                             Accept accept, Aux aux, bool bulk = false, unsigned* err = nullptr)
 {
     using V4 = typename Vec4<T>::type;
     int2* leaves = reinterpret_cast<int2*>(smem + L.off_leaves);
@@ -529,6 +567,35 @@ __device__ int stage_sources(unsigned char* smem, const SmemLayout& L, GroupMisc
     const int total = lpre[nl];
     int* wcnt = reinterpret_cast<int*>(&gm->wred[0][0]);
     int base = 0;
+    const bool in_place = bulk && total <= L.tcap;
+    if (in_place) {
+        // thread 0 announces the bytes, then warp 0 issues one copy per leaf into the tile at the
+        // leaf's prefix position (the tile's earlier readers finished at next_group's barrier)
+        const unsigned phase = gm->mbar_phase;
+        if (w == 0) {
+            if (lane == 0) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                             :: "r"(smem_addr(&gm->mbar)), "r"((unsigned)(total * (int)sizeof(V4))) : "memory");
+            }
+            __syncwarp();
+            for (int l = lane; l < nl; l += 32) {
+                const int2 lf = leaves[l];
+                asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                             :: "r"(smem_addr(tile.pm + lpre[l])), "l"(xrel + lf.x),
+                                "r"((unsigned)(lf.y * (int)sizeof(V4))), "r"(smem_addr(&gm->mbar))
+                             : "memory");
+            }
+        }
+        bool ok = bulk_wait(gm, phase, 1 << 20);
+        // the copies are this CTA's own: a second bounded wait before giving the range up
+        if (!ok) ok = bulk_wait(gm, phase, 1 << 20);
+        if (!ok) {
+            if (threadIdx.x == 0 && err) atomicOr(err, (unsigned)ERR_TIMEOUT);
+            __syncthreads();
+            return -1;
+        }
+    }
     // U sources per thread between barriers: their loads overlap, and the slot order (by f) is the
     // same as one source per thread per barrier
     constexpr int U = 4;
@@ -553,7 +620,7 @@ __device__ int stage_sources(unsigned char* smem, const SmemLayout& L, GroupMisc
                 }
                 const int j = leaves[lo].x + (f - lpre[lo]);
                 const V4 a = loff[lo];
-                const V4 q = xrel[j];
+                const V4 q = in_place ? tile.pm[f] : xrel[j];
                 off[u][0] = a.x + q.x;
                 if (D > 1) off[u][D > 1 ? 1 : 0] = a.y + q.y;
                 if (D > 2) off[u][D > 2 ? 2 : 0] = a.z + q.z;
@@ -598,6 +665,7 @@ __device__ int stage_sources(unsigned char* smem, const SmemLayout& L, GroupMisc
         if (base > L.tcap) break;
     }
     __syncthreads();
+    if (in_place && threadIdx.x == 0) gm->mbar_phase ^= 1u;
     if (base > L.tcap) {
         if (threadIdx.x == 0) gm->overflow = 1000000 + base;   // diagnostic: sources needed (at least)
         return -1;

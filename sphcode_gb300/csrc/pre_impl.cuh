@@ -43,6 +43,7 @@ struct PreArgs {
     double* hguess;   // per-particle guess: the first pass stores it, later passes reuse it
     double nn_over_a; // neighborNumber / A_D
     unsigned long long* counters;   // PairCounter slots, or nullptr (not counted)
+    int bulk_stage;                 // stage the tile with bulk asynchronous copies (knob 29)
 };
 
 template <int D>
@@ -500,6 +501,7 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
     const int t = threadIdx.x;
     const int GT = blockDim.x;
     constexpr double A = volume_const<D>();
+    if (a.bulk_stage) bulk_stage_init(gm);
 
     for (;;) {
         int gb, gn;
@@ -534,7 +536,7 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
             const T* mu = a.mu;
             const int ntile = stage_sources<D, T>(smem, L, gm, a.xrel, tile, [&](int, const T* off) {
                 return box(off, Rt);
-            }, [&](int j) { return mu[j]; });
+            }, [&](int j) { return mu[j]; }, a.bulk_stage != 0, a.work.err);
             if (ntile < 0) { report_overflow(a.work, gb, gn, gm); continue; }
             gm->ntile = ntile;   // every thread writes the same value
         }
@@ -701,6 +703,7 @@ void run_pre(Ctx& c, bool initial)
     a.hguess = (double*)c.mir[8];
     a.nn_over_a = (double)c.p.neighbor_number / volume_const<D>();
     a.counters = c.count_work ? c.d_counters : nullptr;
+    a.bulk_stage = c.bulk_stage;
     const int tcap = c.tile_cap_pre ? c.tile_cap_pre : default_tile_cap<D>();
     launch_pair_passes<PreArgs<T>>(c, (const void*)kern, a, tcap, sizeof(V4), sizeof(T),
         [](const void* k, int grid, int block, size_t smem, cudaStream_t st, PreArgs<T>& args) {

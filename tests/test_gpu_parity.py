@@ -231,3 +231,26 @@ def test_pair_schedules(gpu_lib, case, sched, prec):
         _compare(sim, ref, _fields(p) + ["pos", "vel", "ene"], prec, f"{case} sched={sched} 3 steps")
         assert_counts_match(sim.get("neighbor"), ref.get("neighbor"), ref.get("pos"), ref.get("sml"),
                             p, 1e-12 if prec == "fp64" else 2e-5)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("case", CASES)
+def test_bulk_copy_staging(gpu_lib, case, prec):
+    """Tile staging by bulk asynchronous copies (cp.async.bulk per leaf, mbarrier completion,
+    knob 29) gives the oracle's fields with the tolerances of the ordinary staging."""
+    from oracle import pyoracle
+    from sphcode_gb300 import sphgpu
+    p, f = _cases()[case]()
+    ref = pyoracle.OracleSim(p, f, kind="port")
+    ref.initialize()
+    with sphgpu.GpuSimulation(p, f, precision=prec) as sim:
+        sim.set_tuning("bulk_stage", 1)
+        sim.initialize()
+        assert sim.get_tuning("bulk_stage") == 1
+        _compare(sim, ref, _fields(p), prec, f"{case} bulk initialize")
+        for _ in range(3):
+            ref.step()
+        sim.step(3)
+        _compare(sim, ref, _fields(p) + ["pos", "vel", "ene"], prec, f"{case} bulk 3 steps")
+        assert_counts_match(sim.get("neighbor"), ref.get("neighbor"), ref.get("pos"), ref.get("sml"),
+                            p, 1e-12 if prec == "fp64" else 2e-5)
