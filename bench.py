@@ -452,6 +452,7 @@ def main():
                 "tile_fluid": sim.get_tuning("tile_cap"), "pass2_scale": sim.get_tuning("pass2_scale"),
                 "pair_sched": ["groups", "groups+tpp after pass 1", "groups+tpp after pass 2",
                                "thread-per-particle"][sim.get_tuning("pair_sched")],
+                "group_rule": ["chunks", "key blocks"][sim.get_tuning("group_rule")],
                 "autotuned": bool(sim.get_tuning("autotune")),
                 "rejected_candidate_status_bits": sim.get_tuning("tune_rejects")}
     sim.set_tuning("timing", 0)
@@ -680,7 +681,14 @@ def workload_summary(name, make_sim=None, steps=20, steps64=4):
                 sim.set_tuning("timing", 1)
                 sim.step(1)
                 out["fp32_stage_ms"] = {kk: round(v, 4) for kk, v in sim.stage_times().items()}
+                out["fp32_overflow_groups"] = {"pre": sim.get_tuning("overflow_pre"),
+                                               "fluid": sim.get_tuning("overflow_fluid")}
                 sim.set_tuning("timing", 0)
+                out["fp32_schedule"] = {"group_warps": sim.get_tuning("group_warps"),
+                                        "tile_pre": sim.get_tuning("tile_cap_pre"),
+                                        "tile_fluid": sim.get_tuning("tile_cap"),
+                                        "pair_sched": sim.get_tuning("pair_sched"),
+                                        "group_rule": sim.get_tuning("group_rule")}
     out["ratio"] = out["fp32"] / out["fp64"]
     return out
 

@@ -182,6 +182,11 @@ int sphgpu_energy(sphgpu_ctx* ctx, int run, double* out);
  * out[66+L] leaves at level L (130 ints). */
 int sphgpu_tree_stats(sphgpu_ctx* ctx, int* out);
 
+/* Target groups of the pair kernels formed by the last tree build (no reference counterpart: the
+ * reference walks the tree once per particle): group_of[id] = group of the particle with caller
+ * index id (groups numbered in key order), *n_groups = their number (n ints in group_of). */
+int sphgpu_target_groups(sphgpu_ctx* ctx, int* group_of, int* n_groups);
+
 /* Particles whose smoothing-length Newton iteration did not converge in the last
  * PreInteraction (the reference logs them, src/pre_interaction.cpp:277-280). */
 int sphgpu_newton_failures(sphgpu_ctx* ctx, int* count);
@@ -230,7 +235,12 @@ const char* sphgpu_last_error(const sphgpu_ctx* ctx);
  * all four on its chosen groups and tiles);
  * 29 tile staging of the group schedule by bulk asynchronous copies on/off: the particle records
  * of the walked leaves reach shared memory by one cp.async.bulk per leaf (mbarrier completion,
- * bounded waits) and are filtered in place, where they all fit the tile. */
+ * bounded waits) and are filtered in place, where they all fit the tile;
+ * 30 target-group formation: 1 (default in 2D and 3D) the largest aligned key blocks (octree
+ * cells and their halves, one key bit at a time) of at most 32 x knob 0 particles of one run,
+ * compact in space; 0 (default in 1D, where such a chunk is an interval) fixed chunks of the key
+ * order of that size, each split once where it straddles two distant cells.  Targets of a group smaller than the CTA fill whole warps first; the other warps skip
+ * the group's pair work. */
 int sphgpu_set_tuning(sphgpu_ctx* ctx, int which, int value);
 int sphgpu_get_tuning(sphgpu_ctx* ctx, int which, int* value);
 

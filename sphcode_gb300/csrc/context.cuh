@@ -63,6 +63,11 @@ struct Ctx {
     int* ck_count = nullptr;
     int num_chunks = 0;
     int *part_begin = nullptr, *part_count = nullptr, *part_n = nullptr;   // split scratch
+    unsigned char* g_flag = nullptr;   // key-block groups: group-start flag per particle
+    // group formation (knob 30): 1 the largest aligned key blocks of at most group_threads
+    // particles (default in 2D and 3D), 0 fixed chunks of group_threads particles, each split once
+    // where it straddles two distant cells (default in 1D, where a chunk is an interval)
+    int group_rule = 1;
 
     // per-run scalars on the device
     double* d_time = nullptr;
@@ -260,6 +265,7 @@ void launch_pair_passes(Ctx& c, const void* kern, Args& a, int tcap, int elt4, i
     if (sched == 3) {
         a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 0, nullptr, nullptr, c.ovf_cap,
                            nullptr, nullptr, 0, 0, c.d_err, c.d_work + FAIL_INFO_SLOT};
+        a.work.pieces = gt / 32;
         launch_tpp(tpp_kern, tpp_grid, 128, c.stream, a);
         return;
     }
@@ -299,6 +305,7 @@ void launch_pair_passes(Ctx& c, const void* kern, Args& a, int tcap, int elt4, i
         a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 2 * group_passes, lists[last & 1],
                            c.d_work + 2 * last + 1, c.ovf_cap, nullptr, nullptr, 0, 0, c.d_err,
                            c.d_work + FAIL_INFO_SLOT};
+        a.work.pieces = gt / 32;
         launch_tpp(tpp_kern, tpp_grid, 128, c.stream, a);
     }
 }

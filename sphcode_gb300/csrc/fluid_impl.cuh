@@ -322,9 +322,12 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
         int gb, gn;
         if (!next_group(gm, a.work, gb, gn)) break;
         if (gn == 0) continue;   // the unused half of an unsplit chunk
-        // targets interleaved over the CTA's warps (warp w takes every (GT/32)-th target), so
-        // that the warps meet at the next group's barrier with similar amounts of work
-        const int tl = (t & 31) * (GT >> 5) + (t >> 5);
+        // targets interleaved over the warps the group fills (warp w of nwa takes every nwa-th
+        // target), so that they meet at the next group's barrier with similar amounts of work; the
+        // CTA's other warps skip the group's pair work
+        const int nwa = (gn + 31) >> 5;
+        const bool warp_on = (t >> 5) < nwa;
+        const int tl = warp_on ? (t & 31) * nwa + (t >> 5) : gn;
         const bool active = tl < gn;
         const int i = gb + (active ? tl : 0);
         double xi[D];
@@ -375,7 +378,7 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
             // the word's smallest 1/h_j bounds every source's 1/max(h_i, h_j) from below
             const T wmin = D == 3 ? tile.wbox[2 * w].w : hinv_i;
             const T Hw = hinv_i < wmin ? hinv_i : wmin;
-            if (word_box_r2<D, T>(xo, tile, w) * (Hw * Hw) < dhi) {
+            if (warp_on && word_box_r2<D, T>(xo, tile, w) * (Hw * Hw) < dhi) {
                 const int smax = min(32, ntile - w * 32);
                 for (int b = 0; b < smax; ++b) {
                     const int s = w * 32 + b;
@@ -412,18 +415,21 @@ __global__ void __launch_bounds__(128) fluid_tpp_kernel(FluidArgs<T> a)
     const State& st = a.st;
     const int lane = threadIdx.x & 31;
     for (;;) {
+        // a work item is one piece of 32 targets of a range, so that the few ranges a group pass
+        // leaves spread over many warps instead of running one after another in one warp
         int k = 0;
         if (lane == 0) k = atomicAdd(a.work.counter, 1);
         k = __shfl_sync(FULL, k, 0);
+        const int kr = k / a.work.pieces, o = 32 * (k % a.work.pieces);
         int gb = -1, gn = 0;
         if (a.work.list) {
-            if (k < min(*a.work.list_count, a.work.list_cap)) { const int2 r = a.work.list[k]; gb = r.x; gn = r.y; }
-        } else if (k < *a.work.n_groups) {
-            gb = a.work.g_begin[k];
-            gn = a.work.g_count[k];
+            if (kr < min(*a.work.list_count, a.work.list_cap)) { const int2 r = a.work.list[kr]; gb = r.x; gn = r.y; }
+        } else if (kr < *a.work.n_groups) {
+            gb = a.work.g_begin[kr];
+            gn = a.work.g_count[kr];
         }
         if (gb < 0) break;
-        for (int o = 0; o < gn; o += 32) {
+        if (o < gn) {
             const bool active = o + lane < gn;
             const int i = gb + (active ? o + lane : 0);
             double xi[D];

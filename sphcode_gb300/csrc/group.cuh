@@ -245,6 +245,7 @@ struct GroupWork {
     int halve;                // pass a failing range on as its two halves
     unsigned* err;
     int* fail_info;           // last pass: {begin, count, R in units of 1e-9, leaves, sources}
+    int pieces = 1;           // thread-per-particle kernels: work items of 32 targets per range
 };
 
 // Next work item for this CTA (block-uniform); false when done.

@@ -705,6 +705,84 @@ __global__ void compact_groups_kernel(const int* part_begin, const int* part_cou
     }
 }
 
+// ---- target groups by key-block bisection -------------------------------------------------------
+// The groups are the largest aligned key blocks (a key prefix: an octree cell, or the half, quarter
+// ... of one, taking one key bit at a time) that hold at most G particles of one run; a block of
+// more than G equal keys is cut every G particles.  Unlike fixed chunks of the key order, which
+// start anywhere and straddle cells, such a block is compact in space, so its source tile and the
+// sources each target tests stay close to the minimum for its size.  Particle i (key order) starts
+// a group when it starts a run or when the block of the common key prefix of i - 1 and i holds
+// more than G particles (then i - 1 and i fall in different halves of a block that is split).
+constexpr int GF_THREADS = 256;
+
+__device__ __forceinline__ bool group_start(const unsigned long long* keys, const int* run, int n, int G, int i)
+{
+    if (i == 0 || run[i] != run[i - 1]) return true;
+    const unsigned long long ki = keys[i];
+    const unsigned long long x = keys[i - 1] ^ ki;
+    const int L = __clzll((long long)x);   // common leading bits (64: equal keys)
+    const unsigned long long mask = L >= 64 ? ~0ull : (L == 0 ? 0ull : (~0ull << (64 - L)));
+    // the block [s, e) of the common prefix holds i - 1 and i; it holds more than G particles when
+    // i - 1 - G shares the prefix, or else when s + G does
+    const int lo = i - 1 - G;
+    if (lo >= 0 && ((keys[lo] ^ ki) & mask) == 0ull) {
+        if (x != 0ull) return true;
+        int a = 0, b = lo;   // a run of more than G equal keys: its first index
+        while (a < b) {
+            const int m = (a + b) >> 1;
+            if (keys[m] == ki) b = m; else a = m + 1;
+        }
+        return (i - a) % G == 0;
+    }
+    int a = lo + 1 > 0 ? lo + 1 : 0, b = i - 1;
+    while (a < b) {
+        const int m = (a + b) >> 1;
+        if (((keys[m] ^ ki) & mask) == 0ull) b = m; else a = m + 1;
+    }
+    if (!(a + G < n && ((keys[a + G] ^ ki) & mask) == 0ull)) return false;
+    return x != 0ull || (i - a) % G == 0;
+}
+
+// One flag per particle and the flag count of each block of GF_THREADS particles.
+__global__ void group_flags_kernel(const unsigned long long* keys, const int* run, int n, int G,
+                                   unsigned char* flag, int* blk_count)
+{
+    __shared__ int wc[GF_THREADS / 32];
+    const int i = blockIdx.x * GF_THREADS + threadIdx.x;
+    const bool f = i < n && group_start(keys, run, n, G, i);
+    if (i < n) flag[i] = f ? 1 : 0;
+    const unsigned bal = __ballot_sync(FULL, f);
+    if ((threadIdx.x & 31) == 0) wc[threadIdx.x >> 5] = __popc(bal);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int s = 0;
+        for (int w = 0; w < GF_THREADS / 32; ++w) s += wc[w];
+        blk_count[blockIdx.x] = s;
+    }
+}
+
+// Group list from the flags: each flagged particle writes its group at the block's offset (the
+// exclusive scan of the block counts) plus its rank in the block; the group ends at the next flag
+// (at most G particles on).
+__global__ void group_write_kernel(const unsigned char* flag, const int* blk_off, int n, int G,
+                                   int* g_begin, int* g_count)
+{
+    __shared__ int wc[GF_THREADS / 32];
+    const int i = blockIdx.x * GF_THREADS + threadIdx.x;
+    const bool f = i < n && flag[i];
+    const unsigned bal = __ballot_sync(FULL, f);
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) wc[w] = __popc(bal);
+    __syncthreads();
+    if (!f) return;
+    int o = blk_off[blockIdx.x] + __popc(bal & lanemask_lt());
+    for (int q = 0; q < w; ++q) o += wc[q];
+    int e = i + 1;
+    while (e < n && e < i + G && !flag[e]) ++e;
+    g_begin[o] = i;
+    g_count[o] = e - i;
+}
+
 // ---- FP32 node copies and leaf-relative particle offsets ------------------------------------
 
 struct NodeMirrors {
@@ -828,14 +906,16 @@ int tree_alloc(Ctx& c)
     A((void**)&c.bbox, sizeof(long long) * 2 * 3 * c.R);
     A((void**)&c.node_total, sizeof(int));
     const int max_chunks = n / 32 + c.R + 1;
-    c.max_groups = GROUP_PARTS * max_chunks;
+    // key-block groups: at most one per particle; chunk splits: GROUP_PARTS per chunk
+    c.max_groups = n + c.R + 1;
     A((void**)&c.g_begin, sizeof(int) * c.max_groups);
     A((void**)&c.g_count, sizeof(int) * c.max_groups);
     A((void**)&c.ck_begin, sizeof(int) * max_chunks);
     A((void**)&c.ck_count, sizeof(int) * max_chunks);
-    A((void**)&c.part_begin, sizeof(int) * c.max_groups);
-    A((void**)&c.part_count, sizeof(int) * c.max_groups);
-    A((void**)&c.part_n, sizeof(int) * max_chunks);
+    A((void**)&c.part_begin, sizeof(int) * GROUP_PARTS * (size_t)max_chunks);
+    A((void**)&c.part_count, sizeof(int) * GROUP_PARTS * (size_t)max_chunks);
+    A((void**)&c.part_n, sizeof(int) * max_chunks);   // also the block counts of the key-block flags
+    A((void**)&c.g_flag, sizeof(unsigned char) * ((size_t)n + 1));
     A((void**)&c.n_groups, sizeof(int));
     if (e != cudaSuccess) {
         c.last_error = std::string("tree allocation: ") + cudaGetErrorString(e);
@@ -853,7 +933,7 @@ void tree_free(Ctx& c)
                     c.nd_edge, c.nd_mass, c.nd_ksize, c.lvl_start, c.lvl_tmp, c.chunk_sum, c.bbox,
                     c.node_total, c.g_begin, c.g_count, c.n_groups, c.nd_cf[0], c.nd_cf[1],
                     c.nd_cf[2], c.nd_ef, c.nd_kf, c.ck_begin, c.ck_count, c.radix_dtot, c.nd_grav, c.nd_bnd, c.part_begin,
-                    c.part_count, c.part_n};
+                    c.part_count, c.part_n, c.g_flag};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -954,13 +1034,22 @@ static void make_tree_d(Ctx& c, bool reorder_all, bool full_depth)
     }
     cudaMemcpyAsync(c.node_total, c.lvl_start + lv + 2, sizeof(int), cudaMemcpyDeviceToDevice, s);
     if (c.p.use_gravity) launch_node_moments(c);   // node masses and centres of mass serve gravity only
-    split_groups_kernel<D><<<ceil_div(c.num_chunks, 8), 256, 0, s>>>(c.st, c.keys, c.ck_begin, c.ck_count,
-                                                                   c.num_chunks, c.part_begin, c.part_count,
-                                                                   c.part_n);
-    scan_parts_kernel<<<1, 1024, 0, s>>>(c.part_n, c.num_chunks, c.n_groups);
-    compact_groups_kernel<<<ceil_div(c.num_chunks, 128), 128, 0, s>>>(c.part_begin, c.part_count, c.part_n,
-                                                                     c.n_groups, c.num_chunks, c.g_begin,
-                                                                     c.g_count);
+    if (c.group_rule == 1) {
+        // key-block groups of at most group_threads particles
+        const int nblk = ceil_div(n, GF_THREADS);
+        group_flags_kernel<<<nblk, GF_THREADS, 0, s>>>(c.keys, c.st.run, n, c.group_threads, c.g_flag, c.part_n);
+        scan_parts_kernel<<<1, 1024, 0, s>>>(c.part_n, nblk, c.n_groups);
+        group_write_kernel<<<nblk, GF_THREADS, 0, s>>>(c.g_flag, c.part_n, n, c.group_threads, c.g_begin, c.g_count);
+    } else {
+        // fixed chunks, each split once where it straddles two distant cells
+        split_groups_kernel<D><<<ceil_div(c.num_chunks, 8), 256, 0, s>>>(c.st, c.keys, c.ck_begin, c.ck_count,
+                                                                       c.num_chunks, c.part_begin, c.part_count,
+                                                                       c.part_n);
+        scan_parts_kernel<<<1, 1024, 0, s>>>(c.part_n, c.num_chunks, c.n_groups);
+        compact_groups_kernel<<<ceil_div(c.num_chunks, 128), 128, 0, s>>>(c.part_begin, c.part_count, c.part_n,
+                                                                         c.n_groups, c.num_chunks, c.g_begin,
+                                                                         c.g_count);
+    }
     tv = tree_view(c);
     NodeMirrors nm{};
     for (int k = 0; k < 3; ++k) {

@@ -33,7 +33,8 @@ TUNING = {"group_warps": 0, "fluid_warps": 1, "gravity_warps": 2, "tile_cap": 3,
           "timing": 5, "graph": 6, "graph_kernels": 7, "overflow_pre": 8, "overflow_fluid": 9,
           "tile_cap_pre": 10, "tune_rejects": 11, "pass2_scale": 12, "fixed_dt": 18, "aos_reuse": 19,
           "tree_levels": 20, "depth_cap": 21, "tile_limit": 22, "node_limit": 23,
-          "tune_fail_mask": 24, "count_work": 25, "leaf_cap1": 27, "pair_sched": 28, "bulk_stage": 29}
+          "tune_fail_mask": 24, "count_work": 25, "leaf_cap1": 27, "pair_sched": 28, "bulk_stage": 29,
+          "group_rule": 30}
 
 
 class SphGpuError(RuntimeError):
@@ -79,6 +80,7 @@ _SIGS = {
     "sphgpu_neighbors": (ctypes.c_int, [_P, ctypes.c_int, _P, _P, ctypes.c_int]),
     "sphgpu_energy": (ctypes.c_int, [_P, ctypes.c_int, _P]),
     "sphgpu_tree_stats": (ctypes.c_int, [_P, _P]),
+    "sphgpu_target_groups": (ctypes.c_int, [_P, _P, _P]),
     "sphgpu_newton_failures": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
     "sphgpu_last_error": (ctypes.c_char_p, [_P]),
     "sphgpu_set_tuning": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
@@ -281,6 +283,14 @@ class GpuSimulation:
         out = np.zeros(4 + self.dim)
         _check(self.lib.sphgpu_energy(self._h, run, out.ctypes.data), "energy", self._h)
         return out
+
+    def target_groups(self):
+        """Group index of every particle (caller order) in the pair kernels' group list of the
+        last tree build, and the number of groups."""
+        g = np.zeros(self.n, dtype=np.int32)
+        ng = ctypes.c_int()
+        _check(self.lib.sphgpu_target_groups(self._h, g.ctypes.data, ctypes.byref(ng)), "target_groups", self._h)
+        return g, ng.value
 
     def tree_stats(self) -> np.ndarray:
         out = np.zeros(130, dtype=np.int32)

@@ -19,8 +19,10 @@ pytestmark = pytest.mark.gpu
 
 FP64_TOL = 1e-9
 # Neighbour-count mismatches are allowed only at r = h ties within 1e-12 (FP64) or 2e-5 (FP32)
-# relative to h.
-FP32_TOL = {"dens": 2e-5, "sml": 2e-5, "pres": 2e-5, "gradh": 1e-4, "alpha": 1e-4, "balsara": 5e-3,
+# relative to h.  The Balsara switch |div v| / (|div v| + |rot v| + ...) divides sums that cancel
+# to ~1e-4 of their terms in a nearly divergence-free flow (the Gresho vortex), so FP32 rounding
+# of the terms reaches ~5e-3 of its largest value there, depending on the summation order.
+FP32_TOL = {"dens": 2e-5, "sml": 2e-5, "pres": 2e-5, "gradh": 1e-4, "alpha": 1e-4, "balsara": 1e-2,
             "acc": 5e-3, "dene": 5e-3, "phi": 1e-5, "pos": 1e-6, "vel": 5e-3, "ene": 1e-4,
             "grad_d": 1e-3, "grad_p": 1e-3, "grad_v": 1e-3, "sound": 1e-4}
 
