@@ -239,8 +239,8 @@ const char* sphgpu_last_error(const sphgpu_ctx* ctx);
  * 30 target-group formation: 1 (default in 2D and 3D) the largest aligned key blocks (octree
  * cells and their halves, one key bit at a time) of at most 32 x knob 0 particles of one run,
  * compact in space; 0 (default in 1D, where such a chunk is an interval) fixed chunks of the key
- * order of that size, each split once where it straddles two distant cells.  Targets of a group smaller than the CTA fill whole warps first; the other warps skip
- * the group's pair work. */
+ * order of that size, each split once where it straddles two distant cells.  Targets of a group
+ * smaller than the CTA fill whole warps first; the other warps skip the group's pair work. */
 int sphgpu_set_tuning(sphgpu_ctx* ctx, int which, int value);
 int sphgpu_get_tuning(sphgpu_ctx* ctx, int which, int* value);
 

@@ -243,6 +243,12 @@ struct Kern {
     }
 };
 
+// Bring the 128-byte line holding p into L1 (no register result, so it never stalls the warp).
+__device__ __forceinline__ void prefetch_l1(const void* p)
+{
+    asm volatile("prefetch.global.L1 [%0];" :: "l"(p));
+}
+
 // 1/sqrt in T (the FP32 pair kernels are compiled with approximate division and square root).
 __device__ __forceinline__ float rsqrt_t(float x) { return rsqrtf(x); }
 __device__ __forceinline__ double rsqrt_t(double x) { return 1.0 / sqrt(x); }

@@ -70,7 +70,6 @@ __global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
 {
     using V4 = typename Vec4<T>::type;
     extern __shared__ __align__(16) int2 gstack[];
-    __shared__ int s_group;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int2* stack = gstack + (size_t)w * a.stack_cap;
     const State& st = a.st;
@@ -78,18 +77,17 @@ __global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
     const T G = (T)a.G;
     constexpr bool exact_pairs = sizeof(T) == 8;
 
+    // each warp takes its own work items (32 targets of a group) from the counter: warps share no
+    // data, so none waits at a barrier for the slowest walk of its block
     for (;;) {
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            const int k = atomicAdd(a.work.counter, 1);
-            s_group = k < *a.work.n_groups ? k : -1;
-        }
-        __syncthreads();
-        const int g = s_group;
-        if (g < 0) break;
+        int k = 0;
+        if (lane == 0) k = atomicAdd(a.work.counter, 1);
+        k = __shfl_sync(FULL, k, 0);
+        const int g = k / a.work.pieces, o = 32 * (k % a.work.pieces);
+        if (g >= *a.work.n_groups) break;
         const int gb = a.work.g_begin[g], gn = a.work.g_count[g];
-        if (w * 32 >= gn) continue;
-        const int t = w * 32 + lane;
+        if (o >= gn) continue;
+        const int t = o + lane;
         const bool active = t < gn;
         const int i = gb + (active ? t : 0);
         double xi[D];
@@ -181,7 +179,7 @@ __global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
                         T r2 = T(0);
 #pragma unroll
                         for (int k = 0; k < D; ++k) r2 += dT[k] * dT[k];
-                        const T r_inv = T(1) / sqrt(r2);
+                        const T r_inv = rsqrt_t(r2);
                         const T gmr = G * (T)M * r_inv;
                         phi.add(-gmr);
                         const T c = gmr * r_inv * r_inv;
@@ -235,7 +233,7 @@ __global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
                         if (r2 >= hmax * hmax && r2 > T(0)) {
                             // beyond both softening lengths (u = 2 r / h >= 2 for h_i and h_j):
                             // f = 1/r and g = 1/r^3 for both (src/bhtree.cpp:282-283,296-297)
-                            const T rinv = T(1) / sqrt(r2);
+                            const T rinv = rsqrt_t(r2);
                             fsum = T(2) * rinv;
                             gsum = fsum * rinv * rinv;
                         } else {
@@ -265,7 +263,11 @@ __global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
             } else {
                 const int nc = link.y;
                 if (sp + nc > a.stack_cap) { overflow = true; break; }
-                if (lane < nc) stack[sp + nc - 1 - lane] = make_int2(fc + lane, (int)om);
+                if (lane < nc) {
+                    stack[sp + nc - 1 - lane] = make_int2(fc + lane, (int)om);
+                    // the children's records come in while the first child's subtree is walked
+                    prefetch_l1(tv.gn + fc + lane);
+                }
                 sp += nc;
                 __syncwarp();
             }
@@ -303,7 +305,8 @@ void run_gravity(Ctx& c)
     a.stack_cap = 256;
     a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 0, nullptr, nullptr, 0, nullptr,
                        nullptr, 0, 0, c.d_err, nullptr};
-    const int gt = c.group_threads;
+    a.work.pieces = c.group_threads / 32;
+    const int gt = 128;   // four independent warps per block
     const size_t smem = sizeof(int2) * (size_t)a.stack_cap * (gt / 32);
     auto kern = gravity_kernel<D, T>;
     cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

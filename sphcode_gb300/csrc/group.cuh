@@ -227,6 +227,22 @@ struct MaskWordIter {
         return true;
     }
     __device__ __forceinline__ void clear(int s) { mask[(s >> 5) * gt + t] &= ~(1u << (s & 31)); }
+    // the next word holding candidates and its bits (a word-level walk; do not mix with next())
+    __device__ __forceinline__ bool next_word(int& wo, unsigned& bo)
+    {
+        if (nw > 64) {
+            while (++w < nw) {
+                const unsigned m = mask[w * gt + t];
+                if (m) { wo = w; bo = m; return true; }
+            }
+            return false;
+        }
+        if (pw < 0) return false;
+        wo = pw;
+        bo = pbits;
+        advance();
+        return true;
+    }
 };
 
 // Work distribution.  A work item is a range of key-consecutive targets (begin, count).  The

@@ -99,13 +99,25 @@ struct TilePreSource {
         const T lo_t = to_T_down<T>(hf2 - band), hi_t = to_T_up<T>(hf2 + band);
         bool in_band = false;
         {
+            // word by word: two candidates per trip (independent shared loads and tests), one
+            // store of the word's remaining bits
             MaskWordIter it(tile->mask, gt, t, nw, wmask);
-            int s;
-            while (it.next(s)) {
-                T r[D];
-                const T r2 = tile_r2<D, T>(xo, tile->pm[s], r);
-                if (r2 > hi_t) it.clear(s);
-                else in_band |= !(r2 < lo_t);
+            int w;
+            unsigned cb;
+            while (it.next_word(w, cb)) {
+                unsigned keep = cb, rem = cb;
+                while (rem) {
+                    const int b0 = __ffs(rem) - 1;
+                    rem &= rem - 1;
+                    const int b1 = rem ? __ffs(rem) - 1 : b0;
+                    rem &= rem - 1;
+                    T r[D];
+                    const T r2a = tile_r2<D, T>(xo, tile->pm[w * 32 + b0], r);
+                    const T r2b = tile_r2<D, T>(xo, tile->pm[w * 32 + b1], r);
+                    if (r2a > hi_t) keep &= ~(1u << b0); else in_band |= !(r2a < lo_t);
+                    if (r2b > hi_t) keep &= ~(1u << b1); else in_band |= !(r2b < lo_t);
+                }
+                if (keep != cb) tile->mask[w * gt + t] = keep;
             }
         }
         if (in_band) {
