@@ -613,10 +613,87 @@ __device__ int stage_sources(unsigned char* smem, const SmemLayout& L, GroupMisc
             return -1;
         }
     }
-    // U sources per thread between barriers: their loads overlap, and the slot order (by f) is the
-    // same as one source per thread per barrier
+    if (!in_place) {
+        // each thread takes a contiguous run of at most 64 flattened positions per chunk (one leaf
+        // search per run, then the leaf index only advances), marks the sources it accepts in a
+        // bit mask, and writes them after a block-wide scan of the accepted counts: the slots
+        // follow f, as in the strided loop below
+        const int T_ = blockDim.x;
+        for (int c0 = 0; c0 < total; c0 += 64 * T_) {
+            const int csz = min(total - c0, 64 * T_);
+            const int K = (csz + T_ - 1) / T_;
+            const int fb = c0 + min(csz, threadIdx.x * K), fe = c0 + min(csz, threadIdx.x * K + K);
+            int l0 = 0;
+            if (fb < fe) {
+                int hi = nl;   // last leaf with lpre <= fb
+                while (hi - l0 > 1) {
+                    const int mid = (l0 + hi) >> 1;
+                    if (lpre[mid] <= fb) l0 = mid; else hi = mid;
+                }
+            }
+            unsigned long long acc = 0ull;
+            {
+                int l = l0, lend = lpre[l0 + 1];
+                for (int f = fb; f < fe; ++f) {
+                    while (f >= lend) { ++l; lend = lpre[l + 1]; }
+                    const int j = leaves[l].x + (f - lpre[l]);
+                    const V4 a = loff[l];
+                    const V4 q = xrel[j];
+                    T off[D];
+                    off[0] = a.x + q.x;
+                    if (D > 1) off[D > 1 ? 1 : 0] = a.y + q.y;
+                    if (D > 2) off[D > 2 ? 2 : 0] = a.z + q.z;
+                    if (accept(j, off)) acc |= 1ull << (f - fb);
+                }
+            }
+            // block-wide exclusive scan of the accepted counts
+            const int cnt = __popcll(acc);
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o) incl += v;
+            }
+            __syncthreads();   // earlier readers of wcnt are done
+            if (lane == 31) wcnt[w] = incl;
+            __syncthreads();
+            int woff = 0, tot = 0;
+            for (int ww = 0; ww < nw; ++ww) {
+                const int v = wcnt[ww];
+                if (ww < w) woff += v;
+                tot += v;
+            }
+            int slot = base + woff + incl - cnt;
+            if (base + tot <= L.tcap) {
+                int l = l0, lend = lpre[l0 + 1];
+                while (acc) {
+                    const int k = __ffsll((long long)acc) - 1;
+                    acc &= acc - 1;
+                    const int f = fb + k;
+                    while (f >= lend) { ++l; lend = lpre[l + 1]; }
+                    const int j = leaves[l].x + (f - lpre[l]);
+                    const V4 a = loff[l];
+                    const V4 q = xrel[j];
+                    V4 v;
+                    v.x = a.x + q.x;
+                    v.y = D > 1 ? a.y + q.y : T(0);
+                    v.z = D > 2 ? a.z + q.z : T(0);
+                    v.w = q.w;
+                    tile.pm[slot] = v;
+                    tile.aux[slot] = aux(j);
+                    tile.idx[slot] = j;
+                    ++slot;
+                }
+            }
+            base += tot;
+            // the range goes to a later pass: no need to count the rest (base is block-uniform)
+            if (base > L.tcap) break;
+        }
+    }
+    // (bulk copies in place) U sources per thread between barriers: their loads overlap, and the
+    // slot order (by f) is the same as one source per thread per barrier
     constexpr int U = 4;
-    for (int f0 = 0; f0 < total; f0 += U * blockDim.x) {
+    for (int f0 = 0; in_place && f0 < total; f0 += U * blockDim.x) {
         bool ok[U];
         int jj[U];
         T off[U][D];
