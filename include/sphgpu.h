@@ -240,7 +240,10 @@ const char* sphgpu_last_error(const sphgpu_ctx* ctx);
  * cells and their halves, one key bit at a time) of at most 32 x knob 0 particles of one run,
  * compact in space; 0 (default in 1D, where such a chunk is an interval) fixed chunks of the key
  * order of that size, each split once where it straddles two distant cells.  Targets of a group
- * smaller than the CTA fill whole warps first; the other warps skip the group's pair work. */
+ * smaller than the CTA fill whole warps first; the other warps skip the group's pair work;
+ * 31 group plans, bit 0 FluidForce, bit 1 PreInteraction (default 0): a walk kernel ahead of the
+ * stage's first pass forms every group's box and leaf list with one warp per group, so that the
+ * pass itself neither reduces the box nor walks the octree (groups without a plan walk there). */
 int sphgpu_set_tuning(sphgpu_ctx* ctx, int which, int value);
 int sphgpu_get_tuning(sphgpu_ctx* ctx, int which, int* value);
 

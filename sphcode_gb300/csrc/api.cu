@@ -1290,6 +1290,10 @@ int sphgpu_set_tuning(sphgpu_ctx* h, int which, int value)
         c.pair_sched = value;
         break;
     case 29: c.bulk_stage = value != 0; break;
+    case 31:
+        if (value < 0 || value > 3) return SPHGPU_ERR_ARG;
+        c.prewalk = value;
+        break;
     case 30:
         if (value < 0 || value > 1) return SPHGPU_ERR_ARG;
         c.group_rule = value;
@@ -1337,6 +1341,7 @@ int sphgpu_get_tuning(sphgpu_ctx* h, int which, int* value)
     case 28: *value = c.pair_sched; break;
     case 29: *value = c.bulk_stage; break;
     case 30: *value = c.group_rule; break;
+    case 31: *value = c.prewalk; break;
     case 13: case 14: case 15: case 16: case 17: {
         cudaStreamSynchronize(c.stream);
         cudaMemcpy(value, c.d_work + sphgpu::FAIL_INFO_SLOT + (which - 13), sizeof(int), cudaMemcpyDeviceToHost);

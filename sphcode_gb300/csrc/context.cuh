@@ -153,6 +153,16 @@ struct Ctx {
     int leaf_cap1 = 0;              // leaf-list capacity of the first pair pass (knob 27; 0: by dimension)
     int pair_sched = 0;             // pair-kernel schedule (knob 28, see launch_pair_passes)
     int bulk_stage = 0;             // tile staging by bulk asynchronous copies (knob 29)
+    // group plans (knob 31, bit 0 FluidForce, bit 1 PreInteraction): the first pair pass takes each
+    // group's box and leaves from a walk kernel launched ahead of it (one warp per group), instead
+    // of walking with one warp of its CTA.  Off by default: measured equal or slower (the walk of
+    // one CTA is hidden behind the pair work of the SM's other CTAs)
+    int prewalk = 0;
+    GroupPlan* plan = nullptr;
+    int plan_cap = 0;
+    int2* pool_leaves = nullptr;
+    void* pool_loff = nullptr;      // pool_cap four-vectors of the pair type (sized for FP64)
+    int pool_cap = 0;
     unsigned long long* d_counters = nullptr;   // PAIR_COUNTERS entries
 
     // adjoint scratch (allocated on the first adjoint call)
@@ -225,6 +235,37 @@ void set_global_error(const std::string& text);   // text of sphgpu_last_error(N
 // capacity error bit and records itself in the work counters' diagnostic slots.  Args must carry
 // `L` (SmemLayout) and `work` (GroupWork).
 constexpr int MAX_PAIR_PASSES = 14;
+constexpr int PLAN_WORK_SLOT = 56;   // d_work[56]: work counter of the plan walk, [57] its pool counter
+
+// Leaf-list capacity of the first pair pass (walk stacks hold at least 128 entries).
+inline int first_pass_leaf_cap(const Ctx& c)
+{
+    return c.leaf_cap1 > 0 ? c.leaf_cap1 : (c.dim == 3 ? 256 : 96);
+}
+
+template <typename T>
+PlanView<T> plan_view(Ctx& c)
+{
+    PlanView<T> v;
+    v.plan = c.plan;
+    v.plan_cap = c.plan_cap;
+    v.leaves = c.pool_leaves;
+    v.loff = reinterpret_cast<typename Vec4<T>::type*>(c.pool_loff);
+    v.pool_cap = c.pool_cap;
+    v.pool_count = c.d_work + PLAN_WORK_SLOT + 1;
+    return v;
+}
+
+// Zeroes the plan walk's counters and launches it with four warps per block, as many blocks as fit.
+template <class F>
+void launch_plans(const void* kern, Ctx& c, size_t per_warp, F launch)
+{
+    cudaMemsetAsync(c.d_work + PLAN_WORK_SLOT, 0, 2 * sizeof(int), c.stream);
+    const size_t smem = 4 * per_warp;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int nb = std::max(1, kernel_occupancy(kern, 128, smem));
+    launch(nb * c.num_sms, smem);
+}
 constexpr int FAIL_INFO_SLOT = 48;   // d_work[48..52]: the last failing range
 constexpr int TREE_TRUNC_SLOT = 60;  // d_work[60]: a capped tree build left a splittable node
 template <class Args>
@@ -275,10 +316,10 @@ void launch_pair_passes(Ctx& c, const void* kern, Args& a, int tcap, int elt4, i
         const bool last_tier = pass >= passes - 2;
         if (pass == 0) {
             // walk capacities of the first pass: a 3D group's search box meets many more leaves
-            // than a 2D one's (knob 27 overrides)
+            // than a 2D one's (knob 27 overrides); the plan walk used the same
             cap = std::min(tcap, big);
-            leaf_cap = c.leaf_cap1 > 0 ? c.leaf_cap1 : (c.dim == 3 ? 256 : 96);
-            stack_cap = std::max(128, leaf_cap);
+            leaf_cap = first_pass_leaf_cap(c);
+            stack_cap = std::max(128, leaf_cap);   // groups without a plan walk here
         }
         else if (!last_tier) {
             // walk capacities sized so that a 2D or 3D CTA of the doubled tile keeps a third block

@@ -38,6 +38,7 @@ struct FluidArgs {
     const double* dt_run;
     unsigned long long* counters;   // PairCounter slots, or nullptr (not counted)
     int bulk_stage;                 // stage the tile with bulk asynchronous copies (knob 29)
+    PlanView<T> pv;                 // group plans of the first pass (pv.plan nullptr: none)
 };
 
 // van Leer limiter (src/gsph/g_fluid_force.cpp:28-36).
@@ -334,9 +335,13 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
 #pragma unroll
         for (int k = 0; k < D; ++k) xi[k] = st.f[F_POS + k][i];
         const double hi = st.f[F_SML][i];
-        group_box<D>(gm, xi, active, hi, a.pb);
         const int run = st.run[gb];
-        if (!group_walk<D, T>(smem, L, gm, a.tv, run, true, a.pb)) { report_overflow(a.work, gb, gn, gm); continue; }
+        const int planned = load_plan<T>(smem, L, gm, a.pv);
+        if (planned < 0) { report_overflow(a.work, gb, gn, gm); continue; }
+        if (planned == 0) {
+            group_box<D>(gm, xi, active, hi, a.pb);
+            if (!group_walk<D, T>(smem, L, gm, a.tv, run, true, a.pb)) { report_overflow(a.work, gb, gn, gm); continue; }
+        }
         {
             // keep sources within max(R, h_j) of the group box
             BoxAccept<D, T> box;
@@ -403,6 +408,15 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
             warp_count(a.counters + PC_FLUID_TESTS, active ? (unsigned long long)ntile : 0ull);
         }
     }
+}
+
+// The group plans of FluidForce's first pass (search radius h_i, walk with node kernel sizes).
+template <int D, typename T>
+__global__ void __launch_bounds__(128) fluid_walk_kernel(FluidArgs<T> a, int stack_cap, int cap)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const State& st = a.st;
+    walk_groups<D, T>(a.work, a.tv, a.pb, st, true, a.pv, stack_cap, cap, [&](int i) { return st.f[F_SML][i]; }, smem);
 }
 
 // The thread-per-particle schedule: a warp takes a target range (the group list, or the ranges
@@ -536,6 +550,15 @@ void run_fluid(Ctx& c)
     a.counters = c.count_work ? c.d_counters : nullptr;
     a.bulk_stage = c.bulk_stage;
     const int tcap = c.tile_cap ? c.tile_cap : fluid_default_tile_cap<D>();
+    a.pv = PlanView<T>{};
+    if ((c.prewalk & 1) && c.pair_sched != 3) {
+        a.pv = plan_view<T>(c);
+        const int cap = first_pass_leaf_cap(c), scap = std::max(128, cap);
+        a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + PLAN_WORK_SLOT, nullptr, nullptr, 0,
+                           nullptr, nullptr, 0, 0, c.d_err, nullptr};
+        launch_plans((const void*)fluid_walk_kernel<D, T>, c, plan_warp_bytes<T>(scap, cap),
+                     [&](int grid, size_t smem) { fluid_walk_kernel<D, T><<<grid, 128, smem, c.stream>>>(a, scap, cap); });
+    }
     launch_pair_passes<FluidArgs<T>>(c, (const void*)kern, a, tcap, sizeof(V4), sizeof(T),
         [](const void* k, int grid, int block, size_t smem, cudaStream_t st, FluidArgs<T>& args) {
             reinterpret_cast<void (*)(FluidArgs<T>)>(const_cast<void*>(k))<<<grid, block, smem, st>>>(args);

@@ -84,7 +84,31 @@ struct GroupMisc {
     int nleaves;
     int ntile;
     int overflow;
+    int gidx;           // index of the current work item in the group list (-1: a range of a later pass)
     double wred[8][8];  // per-warp reduction scratch (at most 8 warps per CTA)
+};
+
+// A group's box and walked leaves, formed for a pair kernel's first pass by walk_groups_kernel:
+// the GroupMisc fields that group_box and walk_group set, and where its leaves lie in the pool.
+struct GroupPlan {
+    double gc[3], he[3];
+    double R, rmin, span, scale, bmax;
+    float gcf[3], hef[3];
+    float Rf;
+    int nleaves;        // -1: the walk overflowed its capacities; -2: no room in the pool (walk in the pair kernel)
+    int leaf_off;       // first entry of the group's leaves in the pool
+};
+
+// Where walk_groups_kernel leaves its plans (plans for the first plan_cap groups of the list; the
+// leaves of all of them in one pool, taken by an atomic counter).
+template <typename T>
+struct PlanView {
+    GroupPlan* plan;                 // nullptr: no plans (the pair kernels walk themselves)
+    int plan_cap;
+    int2* leaves;                    // pool: (begin, count) of each leaf
+    typename Vec4<T>::type* loff;    // pool: leaf centre offsets from the group centre
+    int pool_cap;
+    int* pool_count;                 // device counter of the pool
 };
 
 // elt4 = sizeof(Vec4<T>), eltT = sizeof(T)
@@ -279,6 +303,7 @@ __device__ __forceinline__ bool next_group(GroupMisc* gm, const GroupWork& w, in
         }
         gm->group = b;
         gm->ntile = n;   // scratch: the range length
+        gm->gidx = w.list ? -1 : k;
     }
     __syncthreads();
     gb = gm->group;
@@ -315,6 +340,33 @@ __device__ __forceinline__ void report_overflow(const GroupWork& w, int gb, int 
 }
 
 // ---- 1. group bounding box (FP64), block-wide ------------------------------------------------
+// The box fields from the targets' coordinate minima lo and maxima hi, the largest search radius R
+// and the smallest Rm (one thread).
+template <int D>
+__device__ __forceinline__ void finish_box(GroupMisc* gm, const double* lo, const double* hi, double R, double Rm,
+                                           const Periodic& pb)
+{
+    double span = 0.0, sc = 0.0;
+    gm->rmin = Rm;
+    for (int k = 0; k < D; ++k) {
+        const double a = lo[k], b = hi[k];
+        gm->gc[k] = 0.5 * (a + b);
+        // half extent, rounded so that every target lies within gc +/- he
+        gm->he[k] = fmax(b - gm->gc[k], gm->gc[k] - a);
+        span = fmax(span, gm->he[k]);
+        sc = fmax(sc, fabs(gm->gc[k]) + (pb.on ? pb.len[k] : 0.0));
+        gm->gcf[k] = (float)gm->gc[k];
+        gm->hef[k] = __double2float_ru(gm->he[k]);
+    }
+    gm->R = R;
+    gm->Rf = __double2float_ru(R);
+    gm->span = span + R;
+    gm->scale = sc;
+    gm->bmax = 0.0;
+    gm->ntile = 0;
+    gm->overflow = 0;
+}
+
 template <int D>
 __device__ void group_box(GroupMisc* gm, const double* xi, bool active, double radius, const Periodic& pb)
 {
@@ -349,27 +401,15 @@ __device__ void group_box(GroupMisc* gm, const double* xi, bool active, double r
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double span = 0.0, R = 0.0, sc = 0.0, Rm = 1.7976931348623157e308;
+        double R = 0.0, Rm = 1.7976931348623157e308, lo_[3] = {0.0, 0.0, 0.0}, hi_[3] = {0.0, 0.0, 0.0};
         for (int ww = 0; ww < nw; ++ww) { R = fmax(R, gm->wred[ww][6]); Rm = fmin(Rm, gm->wred[ww][7]); }
-        gm->rmin = Rm;
         for (int k = 0; k < D; ++k) {
             double a = gm->wred[0][k], b = gm->wred[0][3 + k];
             for (int ww = 1; ww < nw; ++ww) { a = fmin(a, gm->wred[ww][k]); b = fmax(b, gm->wred[ww][3 + k]); }
-            gm->gc[k] = 0.5 * (a + b);
-            // half extent, rounded so that every target lies within gc +/- he
-            gm->he[k] = fmax(b - gm->gc[k], gm->gc[k] - a);
-            span = fmax(span, gm->he[k]);
-            sc = fmax(sc, fabs(gm->gc[k]) + (pb.on ? pb.len[k] : 0.0));
-            gm->gcf[k] = (float)gm->gc[k];
-            gm->hef[k] = __double2float_ru(gm->he[k]);
+            lo_[k] = a;
+            hi_[k] = b;
         }
-        gm->R = R;
-        gm->Rf = __double2float_ru(R);
-        gm->span = span + R;
-        gm->scale = sc;
-        gm->bmax = 0.0;
-        gm->ntile = 0;
-        gm->overflow = 0;
+        finish_box<D>(gm, lo_, hi_, R, Rm, pb);
     }
     __syncthreads();
 }
@@ -472,6 +512,144 @@ __device__ bool group_walk(unsigned char* smem, const SmemLayout& L, GroupMisc* 
     }
     __syncthreads();
     return gm->overflow == 0;
+}
+
+// Shared memory of one warp of walk_groups_kernel: its GroupMisc, walk stack, leaves and offsets.
+template <typename T>
+__host__ __device__ inline size_t plan_warp_bytes(int stack_cap, int cap)
+{
+    return align16(sizeof(GroupMisc)) + align16(sizeof(int) * (size_t)stack_cap) + align16(sizeof(int2) * (size_t)cap) +
+           align16(sizeof(typename Vec4<T>::type) * (size_t)cap);
+}
+
+// One warp per group of the list, ahead of a pair kernel's first pass: the group box (group_box's
+// arithmetic on the same minima and maxima), the octree walk (walk_group with the capacities of
+// that pass) and, through radius(i), whatever per-target values the stage prepares; the leaves go
+// to the pool and the box with the pool position to the group's plan.  Warps share nothing.
+template <int D, typename T, class Radius>
+__device__ void walk_groups(const GroupWork& work, const TreeView& tv, const Periodic& pb, const State& st,
+                            bool use_ksize, const PlanView<T>& pv, int stack_cap, int cap, Radius radius,
+                            unsigned char* smem)
+{
+    using V4 = typename Vec4<T>::type;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    unsigned char* base = smem + plan_warp_bytes<T>(stack_cap, cap) * w;
+    GroupMisc* gm = reinterpret_cast<GroupMisc*>(base);
+    int* stack = reinterpret_cast<int*>(base + align16(sizeof(GroupMisc)));
+    int2* leaves = reinterpret_cast<int2*>(base + align16(sizeof(GroupMisc)) + align16(sizeof(int) * (size_t)stack_cap));
+    V4* loff = reinterpret_cast<V4*>(base + align16(sizeof(GroupMisc)) + align16(sizeof(int) * (size_t)stack_cap) +
+                                     align16(sizeof(int2) * (size_t)cap));
+    const long long top = dbl_to_ord(1.7976931348623157e308), bottom = dbl_to_ord(-1.7976931348623157e308);
+    for (;;) {
+        int k = 0;
+        if (lane == 0) k = atomicAdd(work.counter, 1);
+        k = __shfl_sync(FULL, k, 0);
+        if (k >= *work.n_groups) break;
+        const int gb = work.g_begin[k], gn = work.g_count[k];
+        if (gn == 0) {
+            if (lane == 0 && k < pv.plan_cap) pv.plan[k].nleaves = -2;
+            continue;
+        }
+        long long lo[D], hi[D];
+        long long rr = 0, rm = top;
+#pragma unroll
+        for (int q = 0; q < D; ++q) { lo[q] = top; hi[q] = bottom; }
+        for (int q = lane; q < gn; q += 32) {
+            const int i = gb + q;
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                const long long o = dbl_to_ord(st.f[F_POS + d][i]);
+                lo[d] = min(lo[d], o);
+                hi[d] = max(hi[d], o);
+            }
+            const long long r = dbl_to_ord(radius(i));
+            rr = max(rr, r);
+            rm = min(rm, r);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                lo[d] = min(lo[d], __shfl_xor_sync(FULL, lo[d], o));
+                hi[d] = max(hi[d], __shfl_xor_sync(FULL, hi[d], o));
+            }
+            rr = max(rr, __shfl_xor_sync(FULL, rr, o));
+            rm = min(rm, __shfl_xor_sync(FULL, rm, o));
+        }
+        if (k >= pv.plan_cap) continue;   // no plan: the pair kernel forms the box and walks
+        if (lane == 0) {
+            double a[3] = {0.0, 0.0, 0.0}, b[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+            for (int d = 0; d < D; ++d) { a[d] = ord_to_dbl(lo[d]); b[d] = ord_to_dbl(hi[d]); }
+            finish_box<D>(gm, a, b, ord_to_dbl(rr), ord_to_dbl(rm), pb);
+        }
+        __syncwarp();
+        const int nl = walk_group<D, T>(tv, st.run[gb], gm, use_ksize, pb, stack, stack_cap, leaves, loff, cap);
+        __syncwarp();
+        int off = 0;
+        if (nl > 0) {
+            if (lane == 0) off = atomicAdd(pv.pool_count, nl);
+            off = __shfl_sync(FULL, off, 0);
+        }
+        const bool fits = nl >= 0 && off + nl <= pv.pool_cap;
+        if (fits) {
+            for (int q = lane; q < nl; q += 32) {
+                pv.leaves[off + q] = leaves[q];
+                pv.loff[off + q] = loff[q];
+            }
+        }
+        if (lane == 0) {
+            GroupPlan* P = pv.plan + k;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                P->gc[d] = gm->gc[d]; P->he[d] = gm->he[d]; P->gcf[d] = gm->gcf[d]; P->hef[d] = gm->hef[d];
+            }
+            P->R = gm->R; P->rmin = gm->rmin; P->span = gm->span; P->scale = gm->scale; P->bmax = gm->bmax;
+            P->Rf = gm->Rf;
+            P->nleaves = nl < 0 ? -1 : (fits ? nl : -2);
+            P->leaf_off = off;
+        }
+        __syncwarp();
+    }
+}
+
+// The plan of the CTA's current group into its shared layout (block-wide): 1 loaded, 0 no plan (box
+// and walk in the pair kernel), -1 the planned walk overflowed (the range goes to a later pass).
+template <typename T>
+__device__ int load_plan(unsigned char* smem, const SmemLayout& L, GroupMisc* gm, const PlanView<T>& pv)
+{
+    using V4 = typename Vec4<T>::type;
+    const int k = gm->gidx;
+    if (!pv.plan || k < 0 || k >= pv.plan_cap) return 0;
+    const GroupPlan* P = pv.plan + k;
+    const int nl = P->nleaves;
+    if (nl == -2 || nl > L.leaf_cap) return 0;
+    // every thread has taken the range length from gm->ntile (next_group's scratch) before the
+    // fields below are overwritten
+    __syncthreads();
+    if (nl < 0) {
+        if (threadIdx.x == 0) { gm->R = P->R; gm->nleaves = 0; gm->overflow = 1; }
+        __syncthreads();
+        return -1;
+    }
+    int2* leaves = reinterpret_cast<int2*>(smem + L.off_leaves);
+    V4* loff = reinterpret_cast<V4*>(smem + L.off_loff);
+    const int off = P->leaf_off;
+    for (int q = threadIdx.x; q < nl; q += blockDim.x) {
+        leaves[q] = pv.leaves[off + q];
+        loff[q] = pv.loff[off + q];
+    }
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) { gm->gc[d] = P->gc[d]; gm->he[d] = P->he[d]; gm->gcf[d] = P->gcf[d]; gm->hef[d] = P->hef[d]; }
+        gm->R = P->R; gm->rmin = P->rmin; gm->span = P->span; gm->scale = P->scale; gm->bmax = P->bmax;
+        gm->Rf = P->Rf;
+        gm->nleaves = nl;
+        gm->ntile = 0;
+        gm->overflow = 0;
+    }
+    __syncthreads();
+    return 1;
 }
 
 // Per-axis acceptance limit in T for staged offsets: |off_k| <= lim_k keeps every source whose

@@ -44,6 +44,7 @@ struct PreArgs {
     double nn_over_a; // neighborNumber / A_D
     unsigned long long* counters;   // PairCounter slots, or nullptr (not counted)
     int bulk_stage;                 // stage the tile with bulk asynchronous copies (knob 29)
+    PlanView<T> pv;                 // group plans of the first pass (pv.plan nullptr: none)
 };
 
 template <int D>
@@ -531,19 +532,23 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
 #pragma unroll
         for (int k = 0; k < D; ++k) xi[k] = st.f[F_POS + k][i];
         const double mi = st.f[F_MASS][i];
-        // the guess (FP64 pow / sqrt) once per particle and stage: passes after the first take
-        // the value the first pass stored (it takes every target before any later pass runs)
+        // the guess (FP64 pow / sqrt) once per particle and stage: the group walk ahead of the
+        // first pass, or else the first pass, stores it (for every target before any later pass)
         double hg;
-        if (a.work.list == nullptr) {
+        if (a.work.list == nullptr && a.pv.plan == nullptr) {
             hg = h_guess<D>((double)a.nn, mi, st.f[F_DENS][i]);
             if (active) a.hguess[i] = hg;
         } else {
             hg = a.hguess[i];
         }
         const double hs = a.initial ? hg : hg * a.ratio;
-        group_box<D>(gm, xi, active, hs, a.pb);
         const int run = st.run[gb];
-        if (!group_walk<D, T>(smem, L, gm, a.tv, run, false, a.pb)) { report_overflow(a.work, gb, gn, gm); continue; }
+        const int planned = load_plan<T>(smem, L, gm, a.pv);
+        if (planned < 0) { report_overflow(a.work, gb, gn, gm); continue; }
+        if (planned == 0) {
+            group_box<D>(gm, xi, active, hs, a.pb);
+            if (!group_walk<D, T>(smem, L, gm, a.tv, run, false, a.pb)) { report_overflow(a.work, gb, gn, gm); continue; }
+        }
         {
             BoxAccept<D, T> box;
             box.init(gm);
@@ -655,6 +660,20 @@ __global__ void __launch_bounds__(128) pre_tpp_kernel(PreArgs<T> a)
     }
 }
 
+// The group plans of PreInteraction's first pass: per target the smoothing-length guess (stored
+// for the pair passes) and the search radius h_s, then the group box and walk.
+template <int D, typename T>
+__global__ void __launch_bounds__(128) pre_walk_kernel(PreArgs<T> a, int stack_cap, int cap)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const State& st = a.st;
+    walk_groups<D, T>(a.work, a.tv, a.pb, st, false, a.pv, stack_cap, cap, [&](int i) {
+        const double hg = h_guess<D>((double)a.nn, st.f[F_MASS][i], st.f[F_DENS][i]);
+        a.hguess[i] = hg;
+        return a.initial ? hg : hg * a.ratio;
+    }, smem);
+}
+
 // Key-ordered T mirrors of the source fields Pre reads per pair.
 template <int D, typename T>
 __global__ void pre_mirror_kernel(State st, int n, typename Vec4<T>::type* mvel, T* mu)
@@ -723,6 +742,15 @@ void run_pre(Ctx& c, bool initial)
     a.counters = c.count_work ? c.d_counters : nullptr;
     a.bulk_stage = c.bulk_stage;
     const int tcap = c.tile_cap_pre ? c.tile_cap_pre : default_tile_cap<D>();
+    a.pv = PlanView<T>{};
+    if ((c.prewalk & 2) && c.pair_sched != 3) {
+        a.pv = plan_view<T>(c);
+        const int cap = first_pass_leaf_cap(c), scap = std::max(128, cap);
+        a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + PLAN_WORK_SLOT, nullptr, nullptr, 0,
+                           nullptr, nullptr, 0, 0, c.d_err, nullptr};
+        launch_plans((const void*)pre_walk_kernel<D, T>, c, plan_warp_bytes<T>(scap, cap),
+                     [&](int grid, size_t smem) { pre_walk_kernel<D, T><<<grid, 128, smem, c.stream>>>(a, scap, cap); });
+    }
     launch_pair_passes<PreArgs<T>>(c, (const void*)kern, a, tcap, sizeof(V4), sizeof(T),
         [](const void* k, int grid, int block, size_t smem, cudaStream_t st, PreArgs<T>& args) {
             reinterpret_cast<void (*)(PreArgs<T>)>(const_cast<void*>(k))<<<grid, block, smem, st>>>(args);

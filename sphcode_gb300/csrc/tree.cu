@@ -916,6 +916,13 @@ int tree_alloc(Ctx& c)
     A((void**)&c.part_count, sizeof(int) * GROUP_PARTS * (size_t)max_chunks);
     A((void**)&c.part_n, sizeof(int) * max_chunks);   // also the block counts of the key-block flags
     A((void**)&c.g_flag, sizeof(unsigned char) * ((size_t)n + 1));
+    // group plans of the first pair pass: plans for the first plan_cap groups, their leaves in a
+    // pool (groups beyond either walk in the pair kernel)
+    c.plan_cap = std::min(c.max_groups, n / 8 + c.R + 64);
+    c.pool_cap = (int)std::min<long long>(1LL << 30, (c.dim == 1 ? n / 4 : c.dim == 2 ? 2LL * n : 6LL * n) + 4096);
+    A((void**)&c.plan, sizeof(GroupPlan) * (size_t)c.plan_cap);
+    A((void**)&c.pool_leaves, sizeof(int2) * (size_t)c.pool_cap);
+    A((void**)&c.pool_loff, (c.precision == SPHGPU_FP32_PAIR ? 16 : 32) * (size_t)c.pool_cap);
     A((void**)&c.n_groups, sizeof(int));
     if (e != cudaSuccess) {
         c.last_error = std::string("tree allocation: ") + cudaGetErrorString(e);
@@ -933,7 +940,7 @@ void tree_free(Ctx& c)
                     c.nd_edge, c.nd_mass, c.nd_ksize, c.lvl_start, c.lvl_tmp, c.chunk_sum, c.bbox,
                     c.node_total, c.g_begin, c.g_count, c.n_groups, c.nd_cf[0], c.nd_cf[1],
                     c.nd_cf[2], c.nd_ef, c.nd_kf, c.ck_begin, c.ck_count, c.radix_dtot, c.nd_grav, c.nd_bnd, c.part_begin,
-                    c.part_count, c.part_n, c.g_flag};
+                    c.part_count, c.part_n, c.g_flag, c.plan, c.pool_leaves, c.pool_loff};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }

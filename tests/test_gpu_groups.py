@@ -50,10 +50,12 @@ def test_batch_groups_stay_in_their_run(gpu_lib):
         assert np.bincount(g).max() <= 128
 
 
+@pytest.mark.parametrize("knob", [("group_rule", 0), ("prewalk", 1), ("prewalk", 3)])
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
 @pytest.mark.parametrize("case", ["khi_disph_ac_2d", "evrard_disph_grav_3d"])
-def test_chunk_groups_parity(gpu_lib, case, prec):
-    """The former rule (fixed chunks split once) stays selectable and matches the oracle."""
+def test_alternative_group_setups_parity(gpu_lib, case, prec, knob):
+    """The former group rule (fixed chunks split once) and the group plans (a walk kernel ahead of
+    the first pass, for FluidForce or both stages) stay selectable and match the oracle."""
     from oracle import pyoracle
     from sphcode_gb300 import sphgpu
     from test_gpu_parity import FP32_TOL, FP64_TOL, _fields
@@ -62,7 +64,7 @@ def test_chunk_groups_parity(gpu_lib, case, prec):
     ref.initialize()
     ref.step()
     with sphgpu.GpuSimulation(p, f, precision=prec) as sim:
-        sim.set_tuning("group_rule", 0)
+        sim.set_tuning(*knob)
         sim.initialize()
         sim.step(1)
         for name in _fields(p):
