@@ -61,6 +61,12 @@ def pre_bytes_per_particle(D):
     return 8 * (2 * D + 6) + 32 * 2 + 8 * 6 + 4
 
 
+# GravityForce: reads pos(D), mass, sml and the FP32 leaf records (16 B), reads and writes acc(D),
+# writes phi; the node records are read from L2.
+def grav_bytes_per_particle(D):
+    return 8 * (D + 2) + 16 + 16 * D + 8
+
+
 def aggregate(ms_local, n_local, steps, dist=None, device="cpu"):
     """Whole-job throughput of independent replicas: the slowest rank's time (max over ranks)
     and the particles of all ranks.  Returns (ms_max, particle-steps/s)."""
@@ -558,7 +564,7 @@ def main():
     pre_flops = counters["pre_iter_pairs"] * fnew + counters["pre_pairs"] * fden
     tgt = max(counters["pre_targets"], 1)
     rooflines = {
-        "pre": line_for("pre_kernel (PreInteraction, FP32 pairs; 11 passes + mirror)", pre_flops, stages["pre"],
+        "pre": line_for("pre_kernel (PreInteraction, FP32 pairs; all passes + mirror)", pre_flops, stages["pre"],
                         pre_bytes_per_particle(D) * n,
                         {"newton_iterations_per_particle": counters["pre_iters"] / tgt,
                          "neighbours_per_particle": counters["pre_pairs"] / tgt,
@@ -566,13 +572,22 @@ def main():
                          "staged_sources_tested_per_particle": counters["pre_tests"] / tgt,
                          "flops_per_pair": {"newton": fnew, "density": fden},
                          "work_source": "device counters of one step (sphgpu_pair_counters)"}),
-        "fluid": line_for("fluid_kernel (FluidForce, FP32 pairs; 11 passes + mirror)", mean_pairs * n * flops_pair,
+        "fluid": line_for("fluid_kernel (FluidForce, FP32 pairs; all passes + mirror)", mean_pairs * n * flops_pair,
                           stages["fluid"], fluid_bytes_per_particle(D) * n,
                           {"pairs_per_particle": mean_pairs, "flops_per_pair": flops_pair,
                            "staged_sources_tested_per_particle": counters["fluid_tests"] / max(n, 1)}),
     }
-    dom = max(("pre", "fluid", "gravity", "tree"), key=lambda k: stages[k])
-    roofline = dict(rooflines.get(dom, rooflines["pre"]))
+    if p.use_gravity and counters.get("grav_nodes", 0) + counters.get("grav_pairs", 0) > 0:
+        gflops = counters["grav_nodes"] * GRAV_FLOPS_NODE + counters["grav_pairs"] * GRAV_FLOPS_LEAF
+        rooflines["gravity"] = line_for("gravity_kernel (Barnes-Hut walk, FP32 terms)", gflops, stages["gravity"],
+                                        grav_bytes_per_particle(D) * n,
+                                        {"monopoles_per_particle": counters["grav_nodes"] / max(n, 1),
+                                         "leaf_pairs_per_particle": counters["grav_pairs"] / max(n, 1),
+                                         "flops_per_term": {"monopole": GRAV_FLOPS_NODE, "leaf_pair": GRAV_FLOPS_LEAF},
+                                         "work_source": "device counters of one step (sphgpu_pair_counters)"})
+    # the dominant stage among those with a roofline entry
+    dom = max((k for k in ("pre", "fluid", "gravity") if k in rooflines), key=lambda k: stages[k])
+    roofline = dict(rooflines[dom])
     roofline["dominant_stage"] = dom
     if args.workload == "khi":
         # DRAM bytes of one launch of the dominant pair kernel from the committed ncu capture

@@ -253,7 +253,8 @@ int sphgpu_get_tuning(sphgpu_ctx* ctx, int which, int* value);
  * 2 sum of Newton iterations, 3 sum of iterations x |{j : r_ij < h_i}|, 4 sum of neighbour counts
  * |{j : r_ij < h_i}|, 5 staged sources tested per PreInteraction target (summed), 6 the same for
  * FluidForce, 7 PreInteraction target ranges processed (all passes), 8 FluidForce ranges,
- * 9..15 zero}.  reset != 0 zeroes them after the read. */
+ * 9 GravityForce monopole terms, 10 GravityForce leaf particle pairs (self terms included),
+ * 11..15 zero}.  reset != 0 zeroes them after the read. */
 int sphgpu_pair_counters(sphgpu_ctx* ctx, unsigned long long* out, int reset);
 
 /* Per-stage device time of the last sphgpu_step / stage call in milliseconds, measured with

@@ -290,6 +290,8 @@ enum PairCounter : int {
     PC_FLUID_TESTS = 6,      // the same for FluidForce
     PC_PRE_GROUPS = 7,       // target ranges processed by PreInteraction (all passes)
     PC_FLUID_GROUPS = 8,     // target ranges processed by FluidForce (all passes)
+    PC_GRAV_NODES = 9,       // Barnes-Hut monopole terms (accepted nodes), summed over targets
+    PC_GRAV_PAIRS = 10,      // Barnes-Hut leaf particle pairs (self terms included), summed over targets
     PAIR_COUNTERS = 16
 };
 

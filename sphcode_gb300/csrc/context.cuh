@@ -231,7 +231,9 @@ void set_global_error(const std::string& text);   // text of sphgpu_last_error(N
 // them with a larger tile (pass2_scale times the first) and larger walk capacities, passing a
 // range that still does not fit on as its two halves, so that ranges come down to single targets
 // (whose search box is just their own search sphere).  The last two passes run what is left with
-// the largest tile the shared memory holds, one CTA per SM.  A range that fits nowhere sets the
+// the largest tile the shared memory holds, one CTA per SM.  (Splitting a failing range into
+// pieces of 32 targets and then into single targets, with fewer passes, was measured slower:
+// single-target CTAs walk and stage for one target each.)  A range that fits nowhere sets the
 // capacity error bit and records itself in the work counters' diagnostic slots.  Args must carry
 // `L` (SmemLayout) and `work` (GroupWork).
 constexpr int MAX_PAIR_PASSES = 14;

@@ -35,6 +35,7 @@ struct GravArgs {
     double G;
     double theta2;
     int stack_cap;
+    unsigned long long* counters;   // PairCounter slots, or nullptr (not counted)
 };
 
 // Softened potential and force kernels (src/bhtree.cpp:273-299).
@@ -65,7 +66,9 @@ __device__ __forceinline__ T hk_g(T r, T h)
     return T(1) / (r * r * r);
 }
 
-template <int D, typename T>
+// COUNT: a separate instantiation counts the monopole terms and leaf pairs (knob 25), so that the
+// timed kernel carries no counter registers.
+template <int D, typename T, bool COUNT>
 __global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
 {
     using V4 = typename Vec4<T>::type;
@@ -114,6 +117,7 @@ __global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
 #pragma unroll
         for (int k = 0; k < D; ++k) acc[k].zero();
 
+        unsigned n_mono = 0, n_pair = 0;   // work counts of this lane (knob 25)
         const unsigned amask = __ballot_sync(FULL, active);
         if (lane == 0) stack[0] = make_int2(st.run[gb], (int)amask);
         int sp = 1;
@@ -175,6 +179,7 @@ __global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
                 if (!open) {
                     const T M = exact_pairs ? (T)tv.mass[node] : (T)gcomlo.w;
                     if (M != T(0)) {
+                        if (COUNT) ++n_mono;
                         // monopole: phi -= G M / r, acc -= d G M / r^3 (src/bhtree.cpp:327-329)
                         T r2 = T(0);
 #pragma unroll
@@ -194,6 +199,7 @@ __global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
             if (fc < 0) {
                 if (open) {
                     const int b = link.z, cnt = link.w;
+                    if (COUNT) n_pair += (unsigned)cnt;
                     T base[D];
                     if (!exact_pairs) {
                         // x_i - centre = (x_i - com) - (centre - com)
@@ -276,6 +282,10 @@ __global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
             if (lane == 0) atomicOr(a.work.err, (unsigned)ERR_GSTACK);
             continue;
         }
+        if (COUNT) {
+            warp_count(a.counters + PC_GRAV_NODES, active ? n_mono : 0u);
+            warp_count(a.counters + PC_GRAV_PAIRS, active ? n_pair : 0u);
+        }
         if (active) {
 #pragma unroll
             for (int k = 0; k < D; ++k) st.f[F_ACC + k][i] += (double)acc[k].get();
@@ -303,12 +313,13 @@ void run_gravity(Ctx& c)
     a.theta2 = c.p.theta * c.p.theta;
     // deepest stack: 2^D - 1 siblings waiting per level below the root, plus one node's children
     a.stack_cap = 256;
+    a.counters = c.count_work ? c.d_counters : nullptr;
     a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 0, nullptr, nullptr, 0, nullptr,
                        nullptr, 0, 0, c.d_err, nullptr};
     a.work.pieces = c.group_threads / 32;
     const int gt = 128;   // four independent warps per block
     const size_t smem = sizeof(int2) * (size_t)a.stack_cap * (gt / 32);
-    auto kern = gravity_kernel<D, T>;
+    auto kern = a.counters ? gravity_kernel<D, T, true> : gravity_kernel<D, T, false>;
     cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     const int nb = std::max(1, kernel_occupancy((const void*)kern, gt, smem));
     kern<<<nb * c.num_sms, gt, smem, s>>>(a);

@@ -578,6 +578,58 @@ __global__ void moments_level_kernel(State st, const int* lvl_start, int l, int 
     }
 }
 
+// The same sums bottom-up in one launch: every leaf sums its particles, then climbs: it counts
+// itself in at its parent after a fence that publishes its sums, and the child that arrives last
+// finishes the parent from all its children (in child order, as the level launches do) and climbs
+// on.  Every node is finished exactly once, after all its children, and no thread waits for
+// another; the counters return to zero.  The roots are not summed.
+template <int D>
+__global__ void moments_up_kernel(State st, const int* node_total_p, int R, const int* begin, const int* count,
+                                  const int* first, const int* nchild, const int* parent, int* arrive,
+                                  double* mass, double* mx0, double* mx1, double* mx2)
+{
+    double* mx[3] = {mx0, mx1, mx2};
+    const int total = *node_total_p;
+    for (int i = R + blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        if (first[i] >= 0) continue;
+        double m = 0.0, sx[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) sx[k] = 0.0;
+        const int b = begin[i], en = b + count[i];
+        for (int j = b; j < en; ++j) {
+            const double mj = st.f[F_MASS][j];
+            m += mj;
+#pragma unroll
+            for (int k = 0; k < D; ++k) sx[k] += st.f[F_POS + k][j] * mj;
+        }
+        mass[i] = m;
+#pragma unroll
+        for (int k = 0; k < D; ++k) mx[k][i] = sx[k];
+        int cur = i;
+        for (;;) {
+            const int p = parent[cur];
+            if (p < R) break;
+            __threadfence();
+            if (atomicAdd(&arrive[p], 1) != nchild[p] - 1) break;
+            __threadfence();
+            arrive[p] = 0;
+            const int fc = first[p], nc = nchild[p];
+            double mp = 0.0, sp[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) sp[k] = 0.0;
+            for (int c = 0; c < nc; ++c) {
+                mp += __ldcg(mass + fc + c);
+#pragma unroll
+                for (int k = 0; k < D; ++k) sp[k] += __ldcg(mx[k] + fc + c);
+            }
+            mass[p] = mp;
+#pragma unroll
+            for (int k = 0; k < D; ++k) mx[k][p] = sp[k];
+            cur = p;
+        }
+    }
+}
+
 // centre of mass = (sum m x) / m for every non-root node (src/bhtree.cpp:152).
 template <int D>
 __global__ void com_finalize_kernel(const int* node_total_p, int R, const double* mass,
@@ -592,7 +644,34 @@ __global__ void com_finalize_kernel(const int* node_total_p, int R, const double
     }
 }
 
-// Per-node maximum smoothing length (BHNode::set_kernel, src/bhtree.cpp:206-232).
+// Per-node maximum smoothing length (BHNode::set_kernel, src/bhtree.cpp:206-232), bottom-up in
+// one launch by the climb of moments_up_kernel (the maximum does not depend on the order).
+__global__ void ksize_up_kernel(const double* sml, const int* node_total_p, const int* begin, const int* count,
+                                const int* first, const int* nchild, const int* parent, int* arrive, double* ksize)
+{
+    const int total = *node_total_p;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        if (first[i] >= 0) continue;
+        double h = 0.0;
+        const int b = begin[i], en = b + count[i];
+        for (int j = b; j < en; ++j) h = fmax(h, sml[j]);
+        ksize[i] = h;
+        int cur = i;
+        for (;;) {
+            const int p = parent[cur];
+            if (p < 0) break;
+            __threadfence();
+            if (atomicAdd(&arrive[p], 1) != nchild[p] - 1) break;
+            __threadfence();
+            arrive[p] = 0;
+            const int fc = first[p], nc = nchild[p];
+            double hp = 0.0;
+            for (int c = 0; c < nc; ++c) hp = fmax(hp, __ldcg(ksize + fc + c));
+            ksize[p] = hp;
+            cur = p;
+        }
+    }
+}
 
 // ---- target groups ----------------------------------------------------------------------------
 // Each fixed chunk of key-consecutive particles is split at the highest key bit in which its
@@ -1094,14 +1173,12 @@ int tree_depth(Ctx& c)
 void launch_node_moments(Ctx& c)
 {
     const int grid = c.num_sms * 8;
-    for (int l = c.tree_levels + 1; l >= 2; --l) {
-        if (c.dim == 1)
-            moments_level_kernel<1><<<grid, 256, 0, c.stream>>>(c.st, c.lvl_start, l, c.R, c.nd_begin, c.nd_count, c.nd_first, c.nd_nchild, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
-        else if (c.dim == 2)
-            moments_level_kernel<2><<<grid, 256, 0, c.stream>>>(c.st, c.lvl_start, l, c.R, c.nd_begin, c.nd_count, c.nd_first, c.nd_nchild, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
-        else
-            moments_level_kernel<3><<<grid, 256, 0, c.stream>>>(c.st, c.lvl_start, l, c.R, c.nd_begin, c.nd_count, c.nd_first, c.nd_nchild, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
-    }
+    if (c.dim == 1)
+        moments_up_kernel<1><<<grid, 256, 0, c.stream>>>(c.st, c.node_total, c.R, c.nd_begin, c.nd_count, c.nd_first, c.nd_nchild, c.nd_parent, c.nd_arrive, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
+    else if (c.dim == 2)
+        moments_up_kernel<2><<<grid, 256, 0, c.stream>>>(c.st, c.node_total, c.R, c.nd_begin, c.nd_count, c.nd_first, c.nd_nchild, c.nd_parent, c.nd_arrive, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
+    else
+        moments_up_kernel<3><<<grid, 256, 0, c.stream>>>(c.st, c.node_total, c.R, c.nd_begin, c.nd_count, c.nd_first, c.nd_nchild, c.nd_parent, c.nd_arrive, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
     if (c.dim == 1) com_finalize_kernel<1><<<grid, 256, 0, c.stream>>>(c.node_total, c.R, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
     else if (c.dim == 2) com_finalize_kernel<2><<<grid, 256, 0, c.stream>>>(c.node_total, c.R, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
     else com_finalize_kernel<3><<<grid, 256, 0, c.stream>>>(c.node_total, c.R, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
@@ -1109,10 +1186,8 @@ void launch_node_moments(Ctx& c)
 
 void launch_set_kernel_size(Ctx& c)
 {
-    for (int l = c.tree_levels + 1; l >= 1; --l)
-        ksize_level_kernel<<<c.num_sms * 8, 256, 0, c.stream>>>(c.st.f[F_SML], c.lvl_start, l, c.nd_begin,
-                                                               c.nd_count, c.nd_first, c.nd_nchild,
-                                                               c.nd_ksize);
+    ksize_up_kernel<<<c.num_sms * 8, 256, 0, c.stream>>>(c.st.f[F_SML], c.node_total, c.nd_begin, c.nd_count,
+                                                        c.nd_first, c.nd_nchild, c.nd_parent, c.nd_arrive, c.nd_ksize);
     if (c.precision == SPHGPU_FP32_PAIR)
         kernel_size_mirror_kernel<float><<<c.num_sms * 8, 256, 0, c.stream>>>(c.node_total, c.nd_ksize, c.nd_kf, c.st.f[F_SML], c.n, (float*)c.mir[7]);
     else

@@ -326,7 +326,7 @@ class GpuSimulation:
         return dict(zip(["tree", "pre", "fluid", "gravity", "integrate"], out.tolist()))
 
     COUNTERS = ["pre_targets", "pre_candidates", "pre_iters", "pre_iter_pairs", "pre_pairs",
-                "pre_tests", "fluid_tests", "pre_groups", "fluid_groups"]
+                "pre_tests", "fluid_tests", "pre_groups", "fluid_groups", "grav_nodes", "grav_pairs"]
 
     def pair_counters(self, reset: bool = True) -> Dict[str, int]:
         """Work counters of the pair kernels collected while the count_work knob is on."""
