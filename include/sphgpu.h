@@ -243,7 +243,11 @@ const char* sphgpu_last_error(const sphgpu_ctx* ctx);
  * smaller than the CTA fill whole warps first; the other warps skip the group's pair work;
  * 31 group plans, bit 0 FluidForce, bit 1 PreInteraction (default 0): a walk kernel ahead of the
  * stage's first pass forms every group's box and leaf list with one warp per group, so that the
- * pass itself neither reduces the box nor walks the octree (groups without a plan walk there). */
+ * pass itself neither reduces the box nor walks the octree (groups without a plan walk there);
+ * 32 octree levels in one cooperative launch on/off (default on in 2D and 3D): the levels' split counts and
+ * child placement with a bounded grid-wide barrier between them, instead of two launches per level
+ * (a barrier wait that runs out stops the build and the step returns SPHGPU_ERR_CUDA with the text
+ * in sphgpu_last_error). */
 int sphgpu_set_tuning(sphgpu_ctx* ctx, int which, int value);
 int sphgpu_get_tuning(sphgpu_ctx* ctx, int which, int* value);
 

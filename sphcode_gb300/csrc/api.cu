@@ -207,7 +207,7 @@ std::string err_bits_text(unsigned bits)
     if (bits & ERR_LIST) s += "neighbour list longer than the caller's capacity; ";
     if (bits & ERR_GSTACK) s += "gravity walk stack overflow; ";
     if (bits & ERR_NOT_FINITE) s += "non-finite value in the particle state; ";
-    if (bits & ERR_TIMEOUT) s += "a bounded wait on a bulk copy into shared memory ran out; ";
+    if (bits & ERR_TIMEOUT) s += "a bounded device wait ran out (a bulk copy into shared memory or a grid barrier of the level build); ";
     return s;
 }
 
@@ -356,6 +356,9 @@ int create_impl(const sphgpu_params* params, int dim, int n_runs, const int* run
     c.dim = dim;
     // 1D: a chunk of the key order is an interval already; 2D and 3D: key blocks (knob 30)
     c.group_rule = dim == 1 ? 0 : 1;
+    // the cooperative level build pays in 2D and 3D; 1D trees (binary, deep, with levels of up
+    // to millions of nodes in a batch) build faster with one launch per level (knob 32)
+    c.fused_levels = dim >= 2 ? 1 : 0;
     c.n = (int)total;
     c.R = n_runs;
     c.precision = precision;
@@ -1290,6 +1293,7 @@ int sphgpu_set_tuning(sphgpu_ctx* h, int which, int value)
         c.pair_sched = value;
         break;
     case 29: c.bulk_stage = value != 0; break;
+    case 32: c.fused_levels = value != 0; c.tree_valid = false; break;
     case 31:
         if (value < 0 || value > 3) return SPHGPU_ERR_ARG;
         c.prewalk = value;
@@ -1342,6 +1346,7 @@ int sphgpu_get_tuning(sphgpu_ctx* h, int which, int* value)
     case 29: *value = c.bulk_stage; break;
     case 30: *value = c.group_rule; break;
     case 31: *value = c.prewalk; break;
+    case 32: *value = c.fused_levels; break;
     case 13: case 14: case 15: case 16: case 17: {
         cudaStreamSynchronize(c.stream);
         cudaMemcpy(value, c.d_work + sphgpu::FAIL_INFO_SLOT + (which - 13), sizeof(int), cudaMemcpyDeviceToHost);

@@ -158,6 +158,9 @@ struct Ctx {
     // of walking with one warp of its CTA.  Off by default: measured equal or slower (the walk of
     // one CTA is hidden behind the pair work of the SM's other CTAs)
     int prewalk = 0;
+    // the tree's levels in one cooperative launch with grid-wide barriers (knob 32), instead of two
+    // launches per level
+    int fused_levels = 1;
     GroupPlan* plan = nullptr;
     int plan_cap = 0;
     int2* pool_leaves = nullptr;
@@ -270,6 +273,7 @@ void launch_plans(const void* kern, Ctx& c, size_t per_warp, F launch)
 }
 constexpr int FAIL_INFO_SLOT = 48;   // d_work[48..52]: the last failing range
 constexpr int TREE_TRUNC_SLOT = 60;  // d_work[60]: a capped tree build left a splittable node
+constexpr int GRID_BAR_SLOT = 61;    // d_work[61..62]: grid barrier of the fused level build (count, generation)
 template <class Args>
 void launch_pair_passes(Ctx& c, const void* kern, Args& a, int tcap, int elt4, int eltT,
                         void (*launch)(const void*, int, int, size_t, cudaStream_t, Args&),

@@ -367,30 +367,26 @@ __device__ __forceinline__ void store_bounds(int* buf, int node, const int* bnd)
     for (int c = 1; c < NC; ++c) buf[(size_t)node * (NC - 1) + (c - 1)] = bnd[c];
 }
 
-// Split decision (src/bhtree.cpp:154-158), child boundaries and child count of every level-l node,
-// with the per-chunk (LEVEL_CHUNK nodes) totals accumulated into chunk_sum (zeroed beforehand).
-// Blocks of COUNT_THREADS threads take sub-chunks of as many nodes, spread over the block's warps
-// (the first nodes to lane 0 of each warp), so that the few large ranges of the upper levels are
-// searched by separate warps.
 constexpr int COUNT_THREADS = 256;
-template <int D>
-__global__ void __launch_bounds__(COUNT_THREADS) level_count_kernel(NodeArrays na, const unsigned long long* keys,
-                                   int n, const int* lvl_start, int l, int levels, int lv, int leaf_num,
-                                   int* lvl_tmp, int* chunk_sum, int* trunc)
+template <int D, int NT>
+__device__ __forceinline__ void count_level(const NodeArrays& na, const unsigned long long* keys, int n,
+                                            const int* lvl_start, int l, int levels, int lv, int leaf_num,
+                                            int* lvl_tmp, int* chunk_sum, int* trunc, int* red)
 {
     constexpr int NC = 1 << D;
-    __shared__ int red[COUNT_THREADS / 32];
-    const int s = lvl_start[l], e = lvl_start[l + 1];
-    const int nsub = (e - s + COUNT_THREADS - 1) / COUNT_THREADS;
-    const int spread = (threadIdx.x & 31) * (COUNT_THREADS / 32) + (threadIdx.x >> 5);
+    // loads of data another block may have written earlier in the same launch go to L2 (__ldcg):
+    // the fused build reads, after a grid barrier, what other SMs wrote before it
+    const int s = __ldcg(lvl_start + l), e = __ldcg(lvl_start + l + 1);
+    const int nsub = (e - s + NT - 1) / NT;
+    const int spread = (threadIdx.x & 31) * (NT / 32) + (threadIdx.x >> 5);
     for (int sub = blockIdx.x; sub < nsub; sub += gridDim.x) {
-        const int node = s + sub * COUNT_THREADS + spread;
+        const int node = s + sub * NT + spread;
         int nc = 0;
         bool split = false;
         int b = 0, cnt = 0;
         if (node < e) {
-            b = na.begin[node];
-            cnt = na.count[node];
+            b = __ldcg(na.begin + node);
+            cnt = __ldcg(na.count + node);
             // slots of a parent the node pool could not hold were not written (the error bit is set)
             if (b < 0 || cnt < 0 || b + cnt > n) { b = 0; cnt = 0; }
             split = (l == 1) || (cnt > leaf_num && l <= lv);
@@ -414,12 +410,26 @@ __global__ void __launch_bounds__(COUNT_THREADS) level_count_kernel(NodeArrays n
         if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
         __syncthreads();
         if (threadIdx.x < 32) {
-            int u = threadIdx.x < COUNT_THREADS / 32 ? red[threadIdx.x] : 0;
+            int u = threadIdx.x < NT / 32 ? red[threadIdx.x] : 0;
             for (int o = 16; o > 0; o >>= 1) u += __shfl_xor_sync(FULL, u, o);
-            if (threadIdx.x == 0 && u) atomicAdd(&chunk_sum[(sub * COUNT_THREADS) / LEVEL_CHUNK], u);
+            if (threadIdx.x == 0 && u) atomicAdd(&chunk_sum[(sub * NT) / LEVEL_CHUNK], u);
         }
         __syncthreads();
     }
+}
+
+// Split decision (src/bhtree.cpp:154-158), child boundaries and child count of every level-l node,
+// with the per-chunk (LEVEL_CHUNK nodes) totals accumulated into chunk_sum (zeroed beforehand).
+// Blocks of COUNT_THREADS threads take sub-chunks of as many nodes, spread over the block's warps
+// (the first nodes to lane 0 of each warp), so that the few large ranges of the upper levels are
+// searched by separate warps.
+template <int D>
+__global__ void __launch_bounds__(COUNT_THREADS) level_count_kernel(NodeArrays na, const unsigned long long* keys,
+                                   int n, const int* lvl_start, int l, int levels, int lv, int leaf_num,
+                                   int* lvl_tmp, int* chunk_sum, int* trunc)
+{
+    __shared__ int red[COUNT_THREADS / 32];
+    count_level<D, COUNT_THREADS>(na, keys, n, lvl_start, l, levels, lv, leaf_num, lvl_tmp, chunk_sum, trunc, red);
 }
 
 
@@ -429,21 +439,18 @@ __global__ void __launch_bounds__(COUNT_THREADS) level_count_kernel(NodeArrays n
 // launch also clears cs_clear, the totals that the count of level l + 2 fills.  Node indices are
 // breadth-first and, within a level, in key order.
 template <int D>
-__global__ void __launch_bounds__(LEVEL_CHUNK) level_build_kernel(NodeArrays na, int* lvl_start, int l,
-                                                                  const int* tmp_cur, const int* cs_cur,
-                                                                  int* cs_clear, int cs_cap, int node_cap,
-                                                                  unsigned* err)
+__device__ __forceinline__ void build_level(const NodeArrays& na, int* lvl_start, int l, const int* tmp_cur,
+                                            const int* cs_cur, int* cs_clear, int cs_cap, int node_cap,
+                                            unsigned* err, int* sc, int* red)
 {
     constexpr int NC = 1 << D;
-    __shared__ int sc[LEVEL_CHUNK];
-    __shared__ int red[32];
-    const int s = lvl_start[l], e = lvl_start[l + 1];
+    const int s = __ldcg(lvl_start + l), e = __ldcg(lvl_start + l + 1);
     const int nchunks = (e - s + LEVEL_CHUNK - 1) / LEVEL_CHUNK;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < cs_cap; q += gridDim.x * blockDim.x) cs_clear[q] = 0;
     // block sum of cs_cur[0, m)
     auto prefix = [&](int m) {
         int v = 0;
-        for (int q = threadIdx.x; q < m; q += blockDim.x) v += cs_cur[q];
+        for (int q = threadIdx.x; q < m; q += blockDim.x) v += __ldcg(cs_cur + q);
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
         if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
         __syncthreads();
@@ -465,7 +472,7 @@ __global__ void __launch_bounds__(LEVEL_CHUNK) level_build_kernel(NodeArrays na,
     for (int chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
         const int chunk_off = prefix(chunk);
         const int node = s + chunk * LEVEL_CHUNK + threadIdx.x;
-        const int nc = node < e ? tmp_cur[node - s] : 0;
+        const int nc = node < e ? __ldcg(tmp_cur + (node - s)) : 0;
         sc[threadIdx.x] = nc;
         __syncthreads();
         for (int o = 1; o < LEVEL_CHUNK; o <<= 1) {
@@ -477,12 +484,12 @@ __global__ void __launch_bounds__(LEVEL_CHUNK) level_build_kernel(NodeArrays na,
         const int off = sc[threadIdx.x] - nc + chunk_off;
         __syncthreads();
         if (node < e && nc > 0) {
-            const int b = na.begin[node], cnt = na.count[node];
+            const int b = __ldcg(na.begin + node), cnt = __ldcg(na.count + node);
             int bnd[NC + 1];
             bnd[0] = b;
             bnd[NC] = b + cnt;
 #pragma unroll
-            for (int c = 1; c < NC; ++c) bnd[c] = na.bnd[(size_t)node * (NC - 1) + (c - 1)];
+            for (int c = 1; c < NC; ++c) bnd[c] = __ldcg(na.bnd + (size_t)node * (NC - 1) + (c - 1));
             const int fc = cbase + off;
             if (full) {
                 na.first[node] = -1;
@@ -490,10 +497,10 @@ __global__ void __launch_bounds__(LEVEL_CHUNK) level_build_kernel(NodeArrays na,
             } else {
                 na.first[node] = fc;
                 na.nchild[node] = nc;
-                const double edge = na.edge[node];
+                const double edge = __ldcg(na.edge + node);
                 double cen[D];
 #pragma unroll
-                for (int k = 0; k < D; ++k) cen[k] = na.center[k][node];
+                for (int k = 0; k < D; ++k) cen[k] = __ldcg(na.center[k] + node);
                 int ci = fc;
                 for (int c = 0; c < NC; ++c) {
                     if (bnd[c + 1] <= bnd[c]) continue;
@@ -515,7 +522,71 @@ __global__ void __launch_bounds__(LEVEL_CHUNK) level_build_kernel(NodeArrays na,
     }
 }
 
+template <int D>
+__global__ void __launch_bounds__(LEVEL_CHUNK) level_build_kernel(NodeArrays na, int* lvl_start, int l,
+                                                                  const int* tmp_cur, const int* cs_cur,
+                                                                  int* cs_clear, int cs_cap, int node_cap,
+                                                                  unsigned* err)
+{
+    __shared__ int sc[LEVEL_CHUNK];
+    __shared__ int red[32];
+    build_level<D>(na, lvl_start, l, tmp_cur, cs_cur, cs_clear, cs_cap, node_cap, err, sc, red);
+}
 
+// Bounded grid-wide barrier of a cooperative launch (all blocks resident): the last block to
+// arrive resets the count and advances the generation; the others wait for the generation with a
+// bounded number of polls.  false when the wait ran out (ERR_TIMEOUT raised); the caller then stops.
+constexpr unsigned GRID_WAIT_POLLS = 1u << 22;
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned* err)
+{
+    __shared__ int ok;
+    __threadfence();   // this thread's writes of the phase, device-wide, before the arrival
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* vgen = bar + 1;
+        const unsigned gen = *vgen;
+        __threadfence();
+        ok = 1;
+        if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+            bar[0] = 0u;
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            unsigned it = 0;
+            while (*vgen == gen) {
+                if (++it > GRID_WAIT_POLLS) { atomicOr(err, (unsigned)ERR_TIMEOUT); ok = 0; break; }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// Every level of the build in one cooperative launch: the counts of the roots, then per level the
+// placement of its children and their counts, with a grid-wide barrier between the phases (the
+// same work as the per-level launches, without their launch gaps).
+template <int D>
+__global__ void __launch_bounds__(LEVEL_CHUNK) levels_fused_kernel(NodeArrays na, const unsigned long long* keys,
+                                                                   int n, int* lvl_start, int levels, int lv,
+                                                                   int leaf_num, int* tmp0, int* tmp1, int* cs0,
+                                                                   int* cs1, int* cs2, int cs_cap, int node_cap,
+                                                                   int* trunc, unsigned* err, unsigned* bar)
+{
+    __shared__ int sc[LEVEL_CHUNK];
+    __shared__ int red[32];
+    int* tmp[2] = {tmp0, tmp1};
+    int* cs[3] = {cs0, cs1, cs2};
+    count_level<D, LEVEL_CHUNK>(na, keys, n, lvl_start, 1, levels, lv, leaf_num, tmp[1], cs[1], trunc, red);
+    for (int l = 1; l <= lv; ++l) {
+        if (!grid_barrier(bar, err)) return;
+        build_level<D>(na, lvl_start, l, tmp[l & 1], cs[l % 3], cs[(l + 2) % 3], cs_cap, node_cap, err, sc, red);
+        if (!grid_barrier(bar, err)) return;
+        count_level<D, LEVEL_CHUNK>(na, keys, n, lvl_start, l + 1, levels, lv, leaf_num, tmp[(l + 1) & 1],
+                                    cs[(l + 1) % 3], trunc, red);
+    }
+}
 
 // ---- bottom-up reductions, one tree level per launch -------------------------------------------
 // Level l occupies the node range [lvl_start[l], lvl_start[l + 1]) of the breadth-first arrays;
@@ -1108,6 +1179,28 @@ static void make_tree_d(Ctx& c, bool reorder_all, bool full_depth)
         int* tmp[2] = {c.lvl_tmp, c.lvl_tmp + c.node_cap};
         int* cs[3] = {c.chunk_sum, c.chunk_sum + cs_cap, c.chunk_sum + 2 * cs_cap};
         cudaMemsetAsync(c.chunk_sum, 0, sizeof(int) * 3 * (size_t)cs_cap, s);
+        // one cooperative launch for all levels (knob 32), or one launch per level and phase
+        int fgrid = 0;
+        if (c.fused_levels) {
+            int nb = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, levels_fused_kernel<D>, LEVEL_CHUNK, 0) != cudaSuccess) {
+                cudaGetLastError();
+                nb = 0;
+            }
+            fgrid = std::min(nb * c.num_sms, std::max(1, ceil_div(c.node_cap, LEVEL_CHUNK)));
+        }
+        if (fgrid > 0) {
+            cudaMemsetAsync(c.d_work + GRID_BAR_SLOT, 0, 2 * sizeof(unsigned), s);
+            const unsigned long long* a_keys = c.keys;
+            int a_n = n, a_levels = levels, a_lv = lv, a_leaf = c.p.leaf_num, a_cs_cap = cs_cap, a_pool = pool;
+            int* a_lvl = c.lvl_start;
+            int* a_tr = c.d_work + TREE_TRUNC_SLOT;
+            unsigned* a_err = c.d_err;
+            unsigned* a_bar = reinterpret_cast<unsigned*>(c.d_work + GRID_BAR_SLOT);
+            void* args[] = {&na, &a_keys, &a_n, &a_lvl, &a_levels, &a_lv, &a_leaf, &tmp[0], &tmp[1],
+                            &cs[0], &cs[1], &cs[2], &a_cs_cap, &a_pool, &a_tr, &a_err, &a_bar};
+            cudaLaunchCooperativeKernel((const void*)levels_fused_kernel<D>, dim3(fgrid), dim3(LEVEL_CHUNK), args, 0, s);
+        } else {
         level_count_kernel<D><<<cgrid, COUNT_THREADS, 0, s>>>(na, c.keys, n, c.lvl_start, 1, levels, lv,
                                                              c.p.leaf_num, tmp[1], cs[1], c.d_work + TREE_TRUNC_SLOT);
         for (int l = 1; l <= lv; ++l) {
@@ -1116,6 +1209,7 @@ static void make_tree_d(Ctx& c, bool reorder_all, bool full_depth)
             level_count_kernel<D><<<cgrid, COUNT_THREADS, 0, s>>>(na, c.keys, n, c.lvl_start, l + 1, levels, lv,
                                                                  c.p.leaf_num, tmp[(l + 1) & 1], cs[(l + 1) % 3],
                                                                  c.d_work + TREE_TRUNC_SLOT);
+        }
         }
     }
     cudaMemcpyAsync(c.node_total, c.lvl_start + lv + 2, sizeof(int), cudaMemcpyDeviceToDevice, s);
@@ -1186,8 +1280,17 @@ void launch_node_moments(Ctx& c)
 
 void launch_set_kernel_size(Ctx& c)
 {
-    ksize_up_kernel<<<c.num_sms * 8, 256, 0, c.stream>>>(c.st.f[F_SML], c.node_total, c.nd_begin, c.nd_count,
-                                                        c.nd_first, c.nd_nchild, c.nd_parent, c.nd_arrive, c.nd_ksize);
+    if (c.dim >= 2) {
+        ksize_up_kernel<<<c.num_sms * 8, 256, 0, c.stream>>>(c.st.f[F_SML], c.node_total, c.nd_begin, c.nd_count,
+                                                            c.nd_first, c.nd_nchild, c.nd_parent, c.nd_arrive, c.nd_ksize);
+    } else {
+        // 1D trees are binary and deep, with leaves of a few particles: the climb's fence and atomic per
+        // node cost more there than one launch per level
+        for (int l = c.tree_levels + 1; l >= 1; --l)
+            ksize_level_kernel<<<c.num_sms * 8, 256, 0, c.stream>>>(c.st.f[F_SML], c.lvl_start, l, c.nd_begin,
+                                                                   c.nd_count, c.nd_first, c.nd_nchild,
+                                                                   c.nd_ksize);
+    }
     if (c.precision == SPHGPU_FP32_PAIR)
         kernel_size_mirror_kernel<float><<<c.num_sms * 8, 256, 0, c.stream>>>(c.node_total, c.nd_ksize, c.nd_kf, c.st.f[F_SML], c.n, (float*)c.mir[7]);
     else
