@@ -246,8 +246,11 @@ const char* sphgpu_last_error(const sphgpu_ctx* ctx);
  * pass itself neither reduces the box nor walks the octree (groups without a plan walk there);
  * 32 octree levels in one cooperative launch on/off (default on in 2D and 3D): the levels' split counts and
  * child placement with a bounded grid-wide barrier between them, instead of two launches per level
- * (a barrier wait that runs out stops the build and the step returns SPHGPU_ERR_CUDA with the text
- * in sphgpu_last_error). */
+ * (a barrier wait that runs out stops the build, the kernels that use the tree return at once and
+ * the step returns SPHGPU_ERR_CUDA with the text in sphgpu_last_error);
+ * 33 fault injection for the tests of that bounded wait: with 1, the next fused level build's
+ * first block leaves without arriving at the first barrier, so the other blocks' wait runs out
+ * (one build only; the knob then reads 0). */
 int sphgpu_set_tuning(sphgpu_ctx* ctx, int which, int value);
 int sphgpu_get_tuning(sphgpu_ctx* ctx, int which, int* value);
 

@@ -146,6 +146,7 @@ __device__ __forceinline__ sphadj::PreWeights<T> adj_weights(const AdjArgs<T>& a
 template <int D, typename T, int K, int TYPE>
 __global__ void __launch_bounds__(256) adj_pass1_kernel(AdjArgs<T> a)
 {
+    if (tree_failed(a.work.err)) return;   // the octree of this step was not completed
     extern __shared__ __align__(16) unsigned char smem[];
     const SmemLayout L = a.L;
     GroupMisc* gm = reinterpret_cast<GroupMisc*>(smem + L.off_misc);
@@ -274,6 +275,7 @@ __global__ void __launch_bounds__(256) adj_pass1_kernel(AdjArgs<T> a)
 template <int D, typename T, int K, int TYPE>
 __global__ void __launch_bounds__(256) adj_pass2_kernel(AdjArgs<T> a)
 {
+    if (tree_failed(a.work.err)) return;   // the octree of this step was not completed
     using V4 = typename Vec4<T>::type;
     extern __shared__ __align__(16) unsigned char smem[];
     const SmemLayout L = a.L;

@@ -295,6 +295,13 @@ enum PairCounter : int {
     PAIR_COUNTERS = 16
 };
 
+// The octree build of this step stopped early (a grid-barrier wait of the level build ran out):
+// the kernels that use the tree return at once and the step reports the status.
+__device__ __forceinline__ bool tree_failed(const unsigned* err)
+{
+    return (*(const volatile unsigned*)err & ERR_TIMEOUT) != 0u;
+}
+
 // Adds v over the 32 lanes of a converged warp into *p (lane 0 issues one atomic).
 __device__ __forceinline__ void warp_count(unsigned long long* p, unsigned long long v)
 {

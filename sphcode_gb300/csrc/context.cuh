@@ -161,6 +161,7 @@ struct Ctx {
     // the tree's levels in one cooperative launch with grid-wide barriers (knob 32), instead of two
     // launches per level
     int fused_levels = 1;
+    int inject_barrier_timeout = 0; // knob 33: the next fused level build's block 0 leaves early (tests)
     GroupPlan* plan = nullptr;
     int plan_cap = 0;
     int2* pool_leaves = nullptr;

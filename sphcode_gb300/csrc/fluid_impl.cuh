@@ -308,6 +308,7 @@ struct WalkSource {
 template <int D, typename T, int TYPE, int K>
 __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
 {
+    if (tree_failed(a.work.err)) return;   // the octree of this step was not completed
     using V4 = typename Vec4<T>::type;
     using KF = Kern<D, K, T>;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -414,6 +415,7 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
 template <int D, typename T>
 __global__ void __launch_bounds__(128) fluid_walk_kernel(FluidArgs<T> a, int stack_cap, int cap)
 {
+    if (tree_failed(a.work.err)) return;   // the octree of this step was not completed
     extern __shared__ __align__(16) unsigned char smem[];
     const State& st = a.st;
     walk_groups<D, T>(a.work, a.tv, a.pb, st, true, a.pv, stack_cap, cap, [&](int i) { return st.f[F_SML][i]; }, smem);
@@ -426,6 +428,7 @@ __global__ void __launch_bounds__(128) fluid_walk_kernel(FluidArgs<T> a, int sta
 template <int D, typename T, int TYPE, int K>
 __global__ void __launch_bounds__(128) fluid_tpp_kernel(FluidArgs<T> a)
 {
+    if (tree_failed(a.work.err)) return;   // the octree of this step was not completed
     const State& st = a.st;
     const int lane = threadIdx.x & 31;
     for (;;) {

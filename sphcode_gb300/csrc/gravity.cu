@@ -71,6 +71,7 @@ __device__ __forceinline__ T hk_g(T r, T h)
 template <int D, typename T, bool COUNT>
 __global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
 {
+    if (tree_failed(a.work.err)) return;   // the octree of this step was not completed
     using V4 = typename Vec4<T>::type;
     extern __shared__ __align__(16) int2 gstack[];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;

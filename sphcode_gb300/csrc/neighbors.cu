@@ -26,6 +26,7 @@ struct NbArgs {
 template <int D, typename T>
 __global__ void __launch_bounds__(256) neighbors_kernel(NbArgs<T> a)
 {
+    if (tree_failed(a.work.err)) return;   // the octree of this step was not completed
     extern __shared__ __align__(16) unsigned char smem[];
     const SmemLayout L = a.L;
     GroupMisc* gm = reinterpret_cast<GroupMisc*>(smem + L.off_misc);

@@ -504,6 +504,7 @@ __device__ __forceinline__ void pre_target(const PreArgs<T>& a, int i, int run, 
 template <int D, typename T, int TYPE, int K>
 __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
 {
+    if (tree_failed(a.work.err)) return;   // the octree of this step was not completed
     using V4 = typename Vec4<T>::type;
     using KF = Kern<D, K, T>;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -621,6 +622,7 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
 template <int D, typename T, int TYPE, int K>
 __global__ void __launch_bounds__(128) pre_tpp_kernel(PreArgs<T> a)
 {
+    if (tree_failed(a.work.err)) return;   // the octree of this step was not completed
     const State& st = a.st;
     const int lane = threadIdx.x & 31;
     for (;;) {
@@ -665,6 +667,7 @@ __global__ void __launch_bounds__(128) pre_tpp_kernel(PreArgs<T> a)
 template <int D, typename T>
 __global__ void __launch_bounds__(128) pre_walk_kernel(PreArgs<T> a, int stack_cap, int cap)
 {
+    if (tree_failed(a.work.err)) return;   // the octree of this step was not completed
     extern __shared__ __align__(16) unsigned char smem[];
     const State& st = a.st;
     walk_groups<D, T>(a.work, a.tv, a.pb, st, false, a.pv, stack_cap, cap, [&](int i) {

@@ -536,7 +536,7 @@ __global__ void __launch_bounds__(LEVEL_CHUNK) level_build_kernel(NodeArrays na,
 // Bounded grid-wide barrier of a cooperative launch (all blocks resident): the last block to
 // arrive resets the count and advances the generation; the others wait for the generation with a
 // bounded number of polls.  false when the wait ran out (ERR_TIMEOUT raised); the caller then stops.
-constexpr unsigned GRID_WAIT_POLLS = 1u << 22;
+constexpr unsigned GRID_WAIT_POLLS = 1u << 20;   // about half a second of 64 ns sleeps and polls
 __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned* err)
 {
     __shared__ int ok;
@@ -572,13 +572,17 @@ __global__ void __launch_bounds__(LEVEL_CHUNK) levels_fused_kernel(NodeArrays na
                                                                    int n, int* lvl_start, int levels, int lv,
                                                                    int leaf_num, int* tmp0, int* tmp1, int* cs0,
                                                                    int* cs1, int* cs2, int cs_cap, int node_cap,
-                                                                   int* trunc, unsigned* err, unsigned* bar)
+                                                                   int* trunc, unsigned* err, unsigned* bar,
+                                                                   int inject_leave)
 {
     __shared__ int sc[LEVEL_CHUNK];
     __shared__ int red[32];
     int* tmp[2] = {tmp0, tmp1};
     int* cs[3] = {cs0, cs1, cs2};
     count_level<D, LEVEL_CHUNK>(na, keys, n, lvl_start, 1, levels, lv, leaf_num, tmp[1], cs[1], trunc, red);
+    // fault injection for the tests of the barrier's bounded wait (knob 33): block 0 leaves
+    // without arriving, so that the other blocks' first wait runs out
+    if (inject_leave && blockIdx.x == 0) return;
     for (int l = 1; l <= lv; ++l) {
         if (!grid_barrier(bar, err)) return;
         build_level<D>(na, lvl_start, l, tmp[l & 1], cs[l % 3], cs[(l + 2) % 3], cs_cap, node_cap, err, sc, red);
@@ -657,9 +661,10 @@ __global__ void moments_level_kernel(State st, const int* lvl_start, int l, int 
 template <int D>
 __global__ void moments_up_kernel(State st, const int* node_total_p, int R, const int* begin, const int* count,
                                   const int* first, const int* nchild, const int* parent, int* arrive,
-                                  double* mass, double* mx0, double* mx1, double* mx2)
+                                  double* mass, double* mx0, double* mx1, double* mx2, const unsigned* err)
 {
     double* mx[3] = {mx0, mx1, mx2};
+    if (tree_failed(err)) return;
     const int total = *node_total_p;
     for (int i = R + blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
         if (first[i] >= 0) continue;
@@ -718,8 +723,10 @@ __global__ void com_finalize_kernel(const int* node_total_p, int R, const double
 // Per-node maximum smoothing length (BHNode::set_kernel, src/bhtree.cpp:206-232), bottom-up in
 // one launch by the climb of moments_up_kernel (the maximum does not depend on the order).
 __global__ void ksize_up_kernel(const double* sml, const int* node_total_p, const int* begin, const int* count,
-                                const int* first, const int* nchild, const int* parent, int* arrive, double* ksize)
+                                const int* first, const int* nchild, const int* parent, int* arrive, double* ksize,
+                                const unsigned* err)
 {
+    if (tree_failed(err)) return;
     const int total = *node_total_p;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
         if (first[i] >= 0) continue;
@@ -1197,8 +1204,10 @@ static void make_tree_d(Ctx& c, bool reorder_all, bool full_depth)
             int* a_tr = c.d_work + TREE_TRUNC_SLOT;
             unsigned* a_err = c.d_err;
             unsigned* a_bar = reinterpret_cast<unsigned*>(c.d_work + GRID_BAR_SLOT);
+            int a_inject = c.inject_barrier_timeout;
+            c.inject_barrier_timeout = 0;   // one build only
             void* args[] = {&na, &a_keys, &a_n, &a_lvl, &a_levels, &a_lv, &a_leaf, &tmp[0], &tmp[1],
-                            &cs[0], &cs[1], &cs[2], &a_cs_cap, &a_pool, &a_tr, &a_err, &a_bar};
+                            &cs[0], &cs[1], &cs[2], &a_cs_cap, &a_pool, &a_tr, &a_err, &a_bar, &a_inject};
             cudaLaunchCooperativeKernel((const void*)levels_fused_kernel<D>, dim3(fgrid), dim3(LEVEL_CHUNK), args, 0, s);
         } else {
         level_count_kernel<D><<<cgrid, COUNT_THREADS, 0, s>>>(na, c.keys, n, c.lvl_start, 1, levels, lv,
@@ -1268,11 +1277,11 @@ void launch_node_moments(Ctx& c)
 {
     const int grid = c.num_sms * 8;
     if (c.dim == 1)
-        moments_up_kernel<1><<<grid, 256, 0, c.stream>>>(c.st, c.node_total, c.R, c.nd_begin, c.nd_count, c.nd_first, c.nd_nchild, c.nd_parent, c.nd_arrive, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
+        moments_up_kernel<1><<<grid, 256, 0, c.stream>>>(c.st, c.node_total, c.R, c.nd_begin, c.nd_count, c.nd_first, c.nd_nchild, c.nd_parent, c.nd_arrive, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2], c.d_err);
     else if (c.dim == 2)
-        moments_up_kernel<2><<<grid, 256, 0, c.stream>>>(c.st, c.node_total, c.R, c.nd_begin, c.nd_count, c.nd_first, c.nd_nchild, c.nd_parent, c.nd_arrive, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
+        moments_up_kernel<2><<<grid, 256, 0, c.stream>>>(c.st, c.node_total, c.R, c.nd_begin, c.nd_count, c.nd_first, c.nd_nchild, c.nd_parent, c.nd_arrive, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2], c.d_err);
     else
-        moments_up_kernel<3><<<grid, 256, 0, c.stream>>>(c.st, c.node_total, c.R, c.nd_begin, c.nd_count, c.nd_first, c.nd_nchild, c.nd_parent, c.nd_arrive, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
+        moments_up_kernel<3><<<grid, 256, 0, c.stream>>>(c.st, c.node_total, c.R, c.nd_begin, c.nd_count, c.nd_first, c.nd_nchild, c.nd_parent, c.nd_arrive, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2], c.d_err);
     if (c.dim == 1) com_finalize_kernel<1><<<grid, 256, 0, c.stream>>>(c.node_total, c.R, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
     else if (c.dim == 2) com_finalize_kernel<2><<<grid, 256, 0, c.stream>>>(c.node_total, c.R, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
     else com_finalize_kernel<3><<<grid, 256, 0, c.stream>>>(c.node_total, c.R, c.nd_mass, c.nd_com[0], c.nd_com[1], c.nd_com[2]);
@@ -1282,7 +1291,8 @@ void launch_set_kernel_size(Ctx& c)
 {
     if (c.dim >= 2) {
         ksize_up_kernel<<<c.num_sms * 8, 256, 0, c.stream>>>(c.st.f[F_SML], c.node_total, c.nd_begin, c.nd_count,
-                                                            c.nd_first, c.nd_nchild, c.nd_parent, c.nd_arrive, c.nd_ksize);
+                                                            c.nd_first, c.nd_nchild, c.nd_parent, c.nd_arrive, c.nd_ksize,
+                                                            c.d_err);
     } else {
         // 1D trees are binary and deep, with leaves of a few particles: the climb's fence and atomic per
         // node cost more there than one launch per level

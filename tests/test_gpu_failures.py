@@ -140,3 +140,27 @@ def test_tuner_rejects_failing_trials(gpu_lib):
         assert sim.get_tuning("tune_rejects") & 8   # the tile bit of the injected failures
         sim.step(1)
         assert np.all(np.isfinite(sim.get("acc")))
+
+
+def test_level_build_barrier_wait_runs_out(gpu_lib):
+    """The fused octree build waits at grid-wide barriers with a bounded number of polls.  Host-side
+    injection (knob 33) makes its first block leave without arriving: the other blocks' wait runs
+    out (about half a second), the kernels that use the tree return at once, the step reports the
+    timeout as SPHGPU_ERR_CUDA with its text, and the same context steps on with complete trees
+    (the failed step's forces were not computed, so its results are not the reference's)."""
+    from sphcode_gb300 import ics, sphgpu
+    p, f = ics.khi(64, 45)
+    with sphgpu.GpuSimulation(p, f, precision="fp64") as sim:
+        assert sim.get_tuning("fused_levels") == 1
+        sim.initialize()
+        counts0 = sim.tree_stats()
+        sim.set_tuning("inject_barrier_timeout", 1)
+        with pytest.raises(sphgpu.SphGpuError) as e:
+            sim.step(1)
+        assert e.value.code == 2, str(e.value)
+        assert "bounded device wait" in str(e.value)
+        assert sim.get_tuning("inject_barrier_timeout") == 0
+        sim.step(2)
+        assert np.all(np.isfinite(sim.get("dens"))) and np.all(np.isfinite(sim.get("acc")))
+        assert sim.tree_stats()[0] > 0 and counts0[0] > 0
+    _device_still_usable()
