@@ -386,13 +386,20 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
             const T Hw = hinv_i < wmin ? hinv_i : wmin;
             if (warp_on && word_box_r2<D, T>(xo, tile, w) * (Hw * Hw) < dhi) {
                 const int smax = min(32, ntile - w * 32);
-                for (int b = 0; b < smax; ++b) {
+                auto test = [&](int b) -> unsigned {
                     const int s = w * 32 + b;
                     T r[D];
                     const T r2 = tile_r2<D, T>(xo, tile.pm[s], r);
                     const T hinv_j = tile.aux[s];
                     const T Hinv = hinv_i < hinv_j ? hinv_i : hinv_j;   // 1 / max(h_i, h_j)
-                    if (r2 * (Hinv * Hinv) < dhi) bits |= 1u << b;
+                    return r2 * (Hinv * Hinv) < dhi ? (1u << b) : 0u;
+                };
+                if (smax == 32) {
+                    // a full word: unrolled, with constant bit positions
+#pragma unroll
+                    for (int b = 0; b < 32; ++b) bits |= test(b);
+                } else {
+                    for (int b = 0; b < smax; ++b) bits |= test(b);
                 }
             }
             if (!active) bits = 0u;

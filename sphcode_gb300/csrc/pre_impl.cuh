@@ -578,12 +578,26 @@ __global__ void __launch_bounds__(256) pre_kernel(PreArgs<T> a)
                 unsigned bits = 0, band = 0;
                 if (warp_on && word_box_r2<D, T>(xo, tile, w) <= hi_t) {   // else no source of the word is in
                     const int smax = min(32, ntile - w * 32);
-                    for (int b = 0; b < smax; ++b) {
-                        T r[D];
-                        const T r2 = tile_r2<D, T>(xo, tile.pm[w * 32 + b], r);
-                        bits |= (unsigned)(r2 < lo_t) << b;
-                        band |= (unsigned)(!(r2 < lo_t) && r2 <= hi_t) << b;
+                    unsigned inner = 0u;   // r2 <= hi_t
+                    if (smax == 32) {
+                        // a full word: unrolled, with constant bit positions and all its shared loads
+                        // free to issue ahead
+#pragma unroll
+                        for (int b = 0; b < 32; ++b) {
+                            T r[D];
+                            const T r2 = tile_r2<D, T>(xo, tile.pm[w * 32 + b], r);
+                            bits |= r2 < lo_t ? (1u << b) : 0u;
+                            inner |= r2 <= hi_t ? (1u << b) : 0u;
+                        }
+                    } else {
+                        for (int b = 0; b < smax; ++b) {
+                            T r[D];
+                            const T r2 = tile_r2<D, T>(xo, tile.pm[w * 32 + b], r);
+                            bits |= r2 < lo_t ? (1u << b) : 0u;
+                            inner |= r2 <= hi_t ? (1u << b) : 0u;
+                        }
                     }
+                    band = inner & ~bits;
                     // the guard band after the word, as a loop: a test inside the loop above is
                     // if-converted, which issues the FP64 re-decision for every source
                     while (band) {
