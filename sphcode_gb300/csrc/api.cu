@@ -100,6 +100,12 @@ __global__ void fill_ord_kernel(long long* p, int n, double v)
     if (i < n) p[i] = dbl_to_ord(v);
 }
 
+__global__ void fill_int_kernel(int* p, int n, int v)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+
 struct AosMap {
     long off[16];     // byte offsets of FP64 members (-1 absent), field ids F_* in order below
     int slot[16];
@@ -282,7 +288,7 @@ void free_ctx(Ctx& c)
     free_state(c.st, true);
     c.alt.run = nullptr;
     free_state(c.alt, false);
-    void* ptrs[] = {c.d_run_begin, c.d_time, c.d_dt, c.d_hvs, c.d_dtmin, c.d_sums, c.d_err,
+    void* ptrs[] = {c.d_run_begin, c.d_time, c.d_dt, c.d_hvs, c.d_dtmin, c.d_emin, c.d_sums, c.d_err,
                     c.d_newton_fail, c.d_work, c.d_counters, c.d_ovf_list, c.d_ovf_list2, c.d_stage, c.d_aos, c.d_flush,
                     c.adj_buf, c.adj_mir, c.adj_partials};
     for (void* p : ptrs)
@@ -392,6 +398,7 @@ int create_impl(const sphgpu_params* params, int dim, int n_runs, const int* run
         A((void**)&c.d_dt, sizeof(double) * R);
         A((void**)&c.d_hvs, sizeof(long long) * R);
         A((void**)&c.d_dtmin, sizeof(long long) * R);
+        A((void**)&c.d_emin, sizeof(int) * R);
         A((void**)&c.d_sums, sizeof(double) * (R * maxc * 7 + R * 7));
         A((void**)&c.d_err, sizeof(unsigned));
         A((void**)&c.d_newton_fail, sizeof(int));
@@ -427,6 +434,7 @@ int create_impl(const sphgpu_params* params, int dim, int n_runs, const int* run
         cudaMemset(c.d_counters, 0, sizeof(unsigned long long) * PAIR_COUNTERS);
         fill_ord_kernel<<<ceil_div(c.R, 128), 128>>>(c.d_hvs, c.R, 1.7976931348623157e308);
         fill_ord_kernel<<<ceil_div(c.R, 128), 128>>>(c.d_dtmin, c.R, 1.7976931348623157e308);
+        fill_int_kernel<<<ceil_div(c.R, 128), 128>>>(c.d_emin, c.R, 0x7f800000);
         init_ids_kernel<<<ceil_div(c.n, THREADS), THREADS>>>(c.st.id, c.st.run, c.d_run_begin, c.R, c.n);
         e = cudaDeviceSynchronize();
         if (e == cudaSuccess) e = cudaGetLastError();

@@ -74,6 +74,7 @@ struct Ctx {
     double* d_dt = nullptr;
     long long* d_hvs = nullptr;     // h / v_sig minimum (ordered-int image)
     long long* d_dtmin = nullptr;   // force-criterion minimum (ordered-int image)
+    int* d_emin = nullptr;          // FP32 estimate of the force-criterion minimum (float bits)
     double* d_sums = nullptr;       // energy/momentum partial sums
     unsigned* d_err = nullptr;      // status bits
     int* d_newton_fail = nullptr;

@@ -491,20 +491,30 @@ __global__ void fluid_mirror_kernel(State st, int n, typename Vec4<T>::type* rec
     v.x = (T)st.f[F_VEL][i];
     v.y = D > 1 ? (T)st.f[F_VEL + (D > 1 ? 1 : 0)][i] : T(0);
     v.z = D > 2 ? (T)st.f[F_VEL + (D > 2 ? 2 : 0)][i] : T(0);
-    v.w = (T)(1.0 / st.f[F_SML][i]);
-    rec0[i] = v;
     const double rho = st.f[F_DENS][i], p = st.f[F_PRES][i];
     typename Vec4<T>::type b;
     b.x = (T)rho;
     b.y = (T)p;
     b.z = (T)st.f[F_SOUND][i];
-    b.w = TYPE == 0 ? (T)(p / (rho * rho) * st.f[F_GRADH][i]) : TYPE == 1 ? (T)st.f[F_GRADH][i] : T(0);
-    rec1[i] = b;
     typename Vec4<T>::type c;
     c.x = (T)st.f[F_ALPHA][i];
     c.y = (T)st.f[F_BALSARA][i];
     c.z = (T)st.f[F_ENE][i];
-    c.w = TYPE == 1 ? (T)(st.f[F_ENE][i] / p) : T(0);
+    if constexpr (std::is_same<T, float>::value) {
+        // FP32 records: the quotients in FP32 (IEEE reciprocal and division) from the rounded
+        // operands; FP64 divisions run at 1/64 of the FP32 rate and bound this kernel otherwise.
+        // 1/h is within one FP32 ulp of 1/h_j, inside the membership test's guard band.
+        v.w = __frcp_rn((float)st.f[F_SML][i]);
+        b.w = TYPE == 0 ? __fdiv_rn(__fdiv_rn(b.y, b.x), b.x) * (float)st.f[F_GRADH][i]
+            : TYPE == 1 ? (float)st.f[F_GRADH][i] : 0.0f;
+        c.w = TYPE == 1 ? __fdiv_rn(c.z, b.y) : 0.0f;
+    } else {
+        v.w = (T)(1.0 / st.f[F_SML][i]);
+        b.w = TYPE == 0 ? (T)(p / (rho * rho) * st.f[F_GRADH][i]) : TYPE == 1 ? (T)st.f[F_GRADH][i] : T(0);
+        c.w = TYPE == 1 ? (T)(st.f[F_ENE][i] / p) : T(0);
+    }
+    rec0[i] = v;
+    rec1[i] = b;
     rec2[i] = c;
     if (TYPE == 2 && gsph_2nd) {
         T* g = grad + (size_t)i * 16;

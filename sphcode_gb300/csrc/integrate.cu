@@ -10,20 +10,84 @@ namespace {
 
 constexpr int THREADS = 256;
 
-// dt_force_i = cflForce * sqrt(h_i / |a_i|) for |a_i| > 0, minimum per run.
+// The force criterion dt_force_i = cflForce * sqrt(h_i / |a_i|) costs two FP64 square roots and
+// one FP64 division per particle, and the FP64 pipe (1/64 of the FP32 rate) is what bounds the
+// reduction.  The minimum is found exactly in two passes instead:
+//  1. e_i = sqrt(h_i / |a_i|) in FP32 (IEEE division and square root, no contraction) and its
+//     minimum per run.  Every FP32 rounding is at most 2^-24 relative and the sum of squares
+//     has positive terms only, so |e_i / sqrt(h_i / |a_i|) - 1| < 4 * 2^-24 while h_i and the
+//     largest |a_k| lie in [2^-60, 2^60] (no FP32 overflow, and a square below the normal range
+//     only for components 2^30 times smaller than the largest); particles outside that range are
+//     "wide" and always take the FP64 expression.
+//  2. The FP64 expression only for the wide particles and those with e_i <= emin * (1 + 2^-12).
+//     The FP64 values are within 2^-49 of cflForce * sqrt(h / |a|), so the particle of the FP64
+//     minimum has an exact value at most 2^-48 above that of any other particle, its e_i at most
+//     2^-20 above emin, and it is always evaluated: the minimum is the same FP64 number as the
+//     minimum over all particles.
+// A particle with all components of a_i zero keeps the empty value (|a_i| = 0 is skipped).
+struct DtEstimate {
+    float e;       // FP32 estimate of sqrt(h / |a|), +inf when a_i = 0
+    bool wide;     // outside the estimate's range: evaluate in FP64
+};
+
 template <int D>
-__global__ void timestep_min_kernel(State st, int n, double cfl_force, long long* dtmin)
+__device__ __forceinline__ DtEstimate dt_estimate(const State& st, int i)
+{
+    float a2 = 0.0f, amax = 0.0f;
+    bool zero = true;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        const double a = st.f[F_ACC + k][i];
+        zero = zero && (__double_as_longlong(a) << 1) == 0;
+        const float af = (float)a;
+        a2 += af * af;
+        amax = fmaxf(amax, fabsf(af));
+    }
+    const float hf = (float)st.f[F_SML][i];
+    constexpr float LO = 8.673617379884035e-19f, HI = 1.152921504606847e18f;   // 2^-60, 2^60
+    DtEstimate d;
+    d.wide = !zero && !(amax >= LO && amax <= HI && hf >= LO && hf <= HI);
+    d.e = zero ? __int_as_float(0x7f800000) : sqrtf(hf / sqrtf(a2));
+    return d;
+}
+
+template <int D>
+__global__ void timestep_estimate_kernel(State st, int n, int* emin)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int v = 0x7f800000;   // +inf; non-negative floats order like their bit patterns
+    int r = -1;
+    if (i < n) {
+        r = st.run[i];
+        const DtEstimate d = dt_estimate<D>(st, i);
+        if (!d.wide && d.e >= 0.0f) v = __float_as_int(d.e);   // NaN stays out
+    }
+    const unsigned same = __match_any_sync(FULL, r);
+    if (same == FULL) {
+        for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(FULL, v, o));
+        if ((threadIdx.x & 31) == 0 && r >= 0) atomicMin(&emin[r], v);
+    } else if (r >= 0) {
+        atomicMin(&emin[r], v);
+    }
+}
+
+template <int D>
+__global__ void timestep_min_kernel(State st, int n, double cfl_force, const int* emin, long long* dtmin)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double v = 1.7976931348623157e308;
     int r = -1;
     if (i < n) {
         r = st.run[i];
-        double a2 = 0.0;
+        const DtEstimate d = dt_estimate<D>(st, i);
+        const float bound = __int_as_float(emin[r]) * 1.000244140625f;   // * (1 + 2^-12)
+        if (d.wide || d.e <= bound) {
+            double a2 = 0.0;
 #pragma unroll
-        for (int k = 0; k < D; ++k) { const double a = st.f[F_ACC + k][i]; a2 += a * a; }
-        const double a = sqrt(a2);
-        if (a > 0.0) v = cfl_force * sqrt(st.f[F_SML][i] / a);
+            for (int k = 0; k < D; ++k) { const double a = st.f[F_ACC + k][i]; a2 += a * a; }
+            const double a = sqrt(a2);
+            if (a > 0.0) v = cfl_force * sqrt(st.f[F_SML][i] / a);
+        }
     }
     const unsigned same = __match_any_sync(FULL, r);
     if (same == FULL) {
@@ -36,7 +100,7 @@ __global__ void timestep_min_kernel(State st, int n, double cfl_force, long long
 
 // dt = min(cflSound * h_per_v_sig, dt_force); resets the minimum for the next call.
 __global__ void timestep_final_kernel(int R, double cfl_sound, const long long* hvs,
-                                      long long* dtmin, double* dt)
+                                      long long* dtmin, int* emin, double* dt)
 {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= R) return;
@@ -44,6 +108,7 @@ __global__ void timestep_final_kernel(int R, double cfl_sound, const long long* 
     const double df = ord_to_dbl(dtmin[r]);
     dt[r] = ds < df ? ds : df;
     dtmin[r] = dbl_to_ord(1.7976931348623157e308);
+    emin[r] = 0x7f800000;
 }
 
 template <int D>
@@ -162,10 +227,18 @@ __global__ void energy_final_kernel(const int* run_begin, int R, int chunks_per_
 void launch_timestep(Ctx& c)
 {
     const int g = ceil_div(c.n, THREADS);
-    if (c.dim == 1) timestep_min_kernel<1><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.p.cfl_force, c.d_dtmin);
-    else if (c.dim == 2) timestep_min_kernel<2><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.p.cfl_force, c.d_dtmin);
-    else timestep_min_kernel<3><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.p.cfl_force, c.d_dtmin);
-    timestep_final_kernel<<<ceil_div(c.R, 128), 128, 0, c.stream>>>(c.R, c.p.cfl_sound, c.d_hvs, c.d_dtmin, c.d_dt);
+    if (c.dim == 1) {
+        timestep_estimate_kernel<1><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.d_emin);
+        timestep_min_kernel<1><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.p.cfl_force, c.d_emin, c.d_dtmin);
+    } else if (c.dim == 2) {
+        timestep_estimate_kernel<2><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.d_emin);
+        timestep_min_kernel<2><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.p.cfl_force, c.d_emin, c.d_dtmin);
+    } else {
+        timestep_estimate_kernel<3><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.d_emin);
+        timestep_min_kernel<3><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.p.cfl_force, c.d_emin, c.d_dtmin);
+    }
+    timestep_final_kernel<<<ceil_div(c.R, 128), 128, 0, c.stream>>>(c.R, c.p.cfl_sound, c.d_hvs, c.d_dtmin,
+                                                                     c.d_emin, c.d_dt);
 }
 
 void launch_predict(Ctx& c)
