@@ -359,6 +359,99 @@ __device__ __forceinline__ void find_bounds(const unsigned long long* keys, bool
     }
 }
 
+// First index in [lo, hi) whose level digit (the D bits at shift) is >= c, or hi, searched by a
+// group of G lanes (G a power of two from 4 to 32; gl the lane's index in the group, gmask the
+// group's lanes in the warp, gshift the group's first lane): each round probes G evenly spaced keys
+// and keeps the interval between the last probe below c and the first at or above it, so a range
+// of 2^14 particles takes two to four dependent rounds instead of fourteen.
+template <int D>
+__device__ __forceinline__ int group_first_ge(const unsigned long long* keys, int lo, int hi, int shift, int c,
+                                              int G, int gl, unsigned gmask, int gshift)
+{
+    constexpr int NC = 1 << D;
+    const unsigned gbits = G == 32 ? FULL : ((1u << G) - 1u);
+    while (hi - lo > G) {
+        const int step = (hi - lo + G - 1) / G;
+        const int pos = lo + gl * step;
+        const bool ge = pos >= hi || (int)((keys[pos] >> shift) & (NC - 1)) >= c;
+        const unsigned m = (__ballot_sync(gmask, ge) >> gshift) & gbits;
+        if (m == 0) {
+            lo = lo + (G - 1) * step + 1;
+        } else {
+            const int f = __ffs(m) - 1;
+            if (f == 0) return lo;
+            const int pf = lo + f * step;
+            lo = lo + (f - 1) * step + 1;
+            hi = pf < hi ? pf : hi;
+        }
+    }
+    if (hi > lo) {
+        const int pos = lo + gl;
+        const bool ge = pos >= hi || (int)((keys[pos] >> shift) & (NC - 1)) >= c;
+        const unsigned m = (__ballot_sync(gmask, ge) >> gshift) & gbits;
+        lo = m ? lo + __ffs(m) - 1 : hi;
+    }
+    return lo;
+}
+
+// Counting for a level with few nodes (the upper levels): one task per (node, inner child
+// boundary), each searched by a group of G lanes, with G the largest power of two (at most 32,
+// at least 4) for which every task has its own group in the grid.  The last task of a node to
+// finish (counted on the node's arrival counter, which returns to zero) forms the child count
+// from the boundaries the other groups stored.  Returns false, with nothing done, when the level
+// has too many nodes for groups of four lanes; every thread of the grid takes the same branch.
+template <int D, int NT>
+__device__ __forceinline__ bool count_level_grouped(const NodeArrays& na, const unsigned long long* keys, int n,
+                                                    int s, int e, int l, int levels, int lv, int leaf_num,
+                                                    int* lvl_tmp, int* chunk_sum, int* trunc)
+{
+    constexpr int NC = 1 << D;
+    const long long tasks = (long long)(e - s) * (NC - 1);
+    const long long lanes = (long long)gridDim.x * NT;
+    int G = 32;
+    while (G >= 4 && tasks * G > lanes) G >>= 1;
+    if (G < 4) return false;
+    const int lane = threadIdx.x & 31, gl = lane & (G - 1), gshift = lane & ~(G - 1);
+    const unsigned gmask = (G == 32 ? FULL : ((1u << G) - 1u)) << gshift;
+    const long long ngroups = lanes / G;
+    const int shift = D * (levels - l);
+    for (long long q = ((long long)blockIdx.x * NT + threadIdx.x) / G; q < tasks; q += ngroups) {
+        const int node = s + (int)(q / (NC - 1));
+        const int c = 1 + (int)(q % (NC - 1));
+        int b = __ldcg(na.begin + node), cnt = __ldcg(na.count + node);
+        if (b < 0 || cnt < 0 || b + cnt > n) { b = 0; cnt = 0; }
+        const bool split = (l == 1) || (cnt > leaf_num && l <= lv);
+        if (!split || cnt == 0) {
+            if (c == 1 && gl == 0) {
+                if (!split && cnt > leaf_num && l <= levels) atomicOr(trunc, 1);
+                if (!split) { na.first[node] = -1; na.nchild[node] = 0; }
+                lvl_tmp[node - s] = 0;
+            }
+            continue;
+        }
+        const int pos = group_first_ge<D>(keys, b, b + cnt, shift, c, G, gl, gmask, gshift);
+        if (gl == 0) {
+            int* slot = na.bnd + (size_t)node * (NC - 1);
+            slot[c - 1] = pos;
+            __threadfence();
+            if (atomicAdd(na.arrive + node, 1) == NC - 2) {
+                __threadfence();
+                int prev = b, nc = 0;
+                for (int k = 1; k < NC; ++k) {
+                    const int x = k == c ? pos : __ldcg(slot + (k - 1));
+                    nc += x > prev;
+                    prev = x;
+                }
+                nc += b + cnt > prev;
+                lvl_tmp[node - s] = nc;
+                atomicAdd(&chunk_sum[(node - s) / LEVEL_CHUNK], nc);
+                na.arrive[node] = 0;
+            }
+        }
+    }
+    return true;
+}
+
 template <int D>
 __device__ __forceinline__ void store_bounds(int* buf, int node, const int* bnd)
 {
@@ -377,6 +470,7 @@ __device__ __forceinline__ void count_level(const NodeArrays& na, const unsigned
     // loads of data another block may have written earlier in the same launch go to L2 (__ldcg):
     // the fused build reads, after a grid barrier, what other SMs wrote before it
     const int s = __ldcg(lvl_start + l), e = __ldcg(lvl_start + l + 1);
+    if (count_level_grouped<D, NT>(na, keys, n, s, e, l, levels, lv, leaf_num, lvl_tmp, chunk_sum, trunc)) return;
     const int nsub = (e - s + NT - 1) / NT;
     const int spread = (threadIdx.x & 31) * (NT / 32) + (threadIdx.x >> 5);
     for (int sub = blockIdx.x; sub < nsub; sub += gridDim.x) {
@@ -469,7 +563,13 @@ __device__ __forceinline__ void build_level(const NodeArrays& na, int* lvl_start
         if (full) atomicOr(err, (unsigned)ERR_NODE_POOL);
         lvl_start[l + 2] = full ? cbase : cbase + total;
     }
-    for (int chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
+    // a level of few chunks shares each chunk among S blocks: every block of a chunk forms the
+    // chunk's offsets (a block scan) and writes the children of its own 1/S of the nodes, so that
+    // the child records of the upper levels are written by the whole grid
+    const int S = nchunks > 0 ? max(1, (int)gridDim.x / nchunks) : 1;
+    for (int job = blockIdx.x; job < nchunks * S; job += gridDim.x) {
+        const int chunk = job / S, part = job - chunk * S;
+        const bool mine = (int)threadIdx.x >= part * LEVEL_CHUNK / S && (int)threadIdx.x < (part + 1) * LEVEL_CHUNK / S;
         const int chunk_off = prefix(chunk);
         const int node = s + chunk * LEVEL_CHUNK + threadIdx.x;
         const int nc = node < e ? __ldcg(tmp_cur + (node - s)) : 0;
@@ -483,7 +583,7 @@ __device__ __forceinline__ void build_level(const NodeArrays& na, int* lvl_start
         }
         const int off = sc[threadIdx.x] - nc + chunk_off;
         __syncthreads();
-        if (node < e && nc > 0) {
+        if (mine && node < e && nc > 0) {
             const int b = __ldcg(na.begin + node), cnt = __ldcg(na.count + node);
             int bnd[NC + 1];
             bnd[0] = b;
@@ -587,6 +687,13 @@ __global__ void __launch_bounds__(LEVEL_CHUNK) levels_fused_kernel(NodeArrays na
         if (!grid_barrier(bar, err)) return;
         build_level<D>(na, lvl_start, l, tmp[l & 1], cs[l % 3], cs[(l + 2) % 3], cs_cap, node_cap, err, sc, red);
         if (!grid_barrier(bar, err)) return;
+        // an empty level l + 1 leaves every deeper level empty: their starts are its end
+        const int end = __ldcg(lvl_start + l + 2);
+        if (end == __ldcg(lvl_start + l + 1)) {
+            if (blockIdx.x == 0)
+                for (int q = l + 3 + (int)threadIdx.x; q <= lv + 2; q += (int)blockDim.x) lvl_start[q] = end;
+            return;
+        }
         count_level<D, LEVEL_CHUNK>(na, keys, n, lvl_start, l + 1, levels, lv, leaf_num, tmp[(l + 1) & 1],
                                     cs[(l + 1) % 3], trunc, red);
     }
