@@ -452,6 +452,74 @@ __device__ __forceinline__ bool count_level_grouped(const NodeArrays& na, const 
     return true;
 }
 
+// First index in [lo, hi) whose level digit is >= c, or hi: one thread's binary search.
+template <int D>
+__device__ __forceinline__ int first_ge(const unsigned long long* keys, int lo, int hi, int shift, int c)
+{
+    constexpr int NC = 1 << D;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if ((int)((keys[mid] >> shift) & (NC - 1)) < c) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+// Counting of the nodes [lo_node, hi_node) of level l by the threads of one block (the nodes this
+// block has just placed): one task per (node, inner child boundary), each searched by a group of
+// G lanes (G a power of two up to 32, the largest that gives every task its own group in the
+// block; a thread per task below two lanes).  Split decision, boundaries, child counts and
+// per-chunk totals are those of count_level; the last task of a node forms its child count.
+template <int D>
+__device__ __forceinline__ void count_nodes_block(const NodeArrays& na, const unsigned long long* keys, int n,
+                                                  int lo_node, int hi_node, int s, int l, int levels, int lv,
+                                                  int leaf_num, int* lvl_tmp, int* chunk_sum, int* trunc)
+{
+    constexpr int NC = 1 << D;
+    const int tasks = (hi_node - lo_node) * (NC - 1);
+    if (tasks <= 0) return;
+    int G = 32;
+    while (G >= 2 && tasks * G > (int)blockDim.x) G >>= 1;
+    const int lane = threadIdx.x & 31, gl = lane & (G - 1), gshift = lane & ~(G - 1);
+    const unsigned gmask = (G == 32 ? FULL : ((1u << G) - 1u)) << gshift;
+    const int ngroups = (int)blockDim.x / G;
+    const int shift = D * (levels - l);
+    for (int q = (int)threadIdx.x / G; q < tasks; q += ngroups) {
+        const int node = lo_node + q / (NC - 1);
+        const int c = 1 + q % (NC - 1);
+        int b = __ldcg(na.begin + node), cnt = __ldcg(na.count + node);
+        if (b < 0 || cnt < 0 || b + cnt > n) { b = 0; cnt = 0; }
+        const bool split = cnt > leaf_num && l <= lv;
+        if (!split || cnt == 0) {
+            if (c == 1 && gl == 0) {
+                if (!split && cnt > leaf_num && l <= levels) atomicOr(trunc, 1);
+                if (!split) { na.first[node] = -1; na.nchild[node] = 0; }
+                lvl_tmp[node - s] = 0;
+            }
+            continue;
+        }
+        const int pos = G >= 2 ? group_first_ge<D>(keys, b, b + cnt, shift, c, G, gl, gmask, gshift)
+                               : first_ge<D>(keys, b, b + cnt, shift, c);
+        if (gl == 0) {
+            int* slot = na.bnd + (size_t)node * (NC - 1);
+            slot[c - 1] = pos;
+            __threadfence();
+            if (atomicAdd(na.arrive + node, 1) == NC - 2) {
+                __threadfence();
+                int prev = b, nc = 0;
+                for (int k = 1; k < NC; ++k) {
+                    const int x = k == c ? pos : __ldcg(slot + (k - 1));
+                    nc += x > prev;
+                    prev = x;
+                }
+                nc += b + cnt > prev;
+                lvl_tmp[node - s] = nc;
+                atomicAdd(&chunk_sum[(node - s) / LEVEL_CHUNK], nc);
+                na.arrive[node] = 0;
+            }
+        }
+    }
+}
+
 template <int D>
 __device__ __forceinline__ void store_bounds(int* buf, int node, const int* bnd)
 {
@@ -532,12 +600,24 @@ __global__ void __launch_bounds__(COUNT_THREADS) level_count_kernel(NodeArrays n
 // tmp_cur / cs_cur hold the child counts of the level-l nodes and their per-chunk totals; the
 // launch also clears cs_clear, the totals that the count of level l + 2 fills.  Node indices are
 // breadth-first and, within a level, in key order.
-template <int D>
+// With COUNT, each block also counts the children it has just placed (count_nodes_block: split
+// decision, boundaries, child counts into nx.lvl_tmp and nx.chunk_sum), so that the fused build
+// needs one grid barrier per level.
+struct NextCount {
+    const unsigned long long* keys;
+    int n, levels, lv, leaf_num;
+    int* lvl_tmp;
+    int* chunk_sum;
+    int* trunc;
+};
+
+template <int D, bool COUNT>
 __device__ __forceinline__ void build_level(const NodeArrays& na, int* lvl_start, int l, const int* tmp_cur,
                                             const int* cs_cur, int* cs_clear, int cs_cap, int node_cap,
-                                            unsigned* err, int* sc, int* red)
+                                            unsigned* err, int* sc, int* red, const NextCount& nx)
 {
     constexpr int NC = 1 << D;
+    static_assert(LEVEL_CHUNK == 1024, "the chunk scan takes 32 warps of 32 nodes");
     const int s = __ldcg(lvl_start + l), e = __ldcg(lvl_start + l + 1);
     const int nchunks = (e - s + LEVEL_CHUNK - 1) / LEVEL_CHUNK;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < cs_cap; q += gridDim.x * blockDim.x) cs_clear[q] = 0;
@@ -566,22 +646,41 @@ __device__ __forceinline__ void build_level(const NodeArrays& na, int* lvl_start
     // a level of few chunks shares each chunk among S blocks: every block of a chunk forms the
     // chunk's offsets (a block scan) and writes the children of its own 1/S of the nodes, so that
     // the child records of the upper levels are written by the whole grid
-    const int S = nchunks > 0 ? max(1, (int)gridDim.x / nchunks) : 1;
+    const int S = nchunks > 0 ? min(LEVEL_CHUNK, max(1, (int)gridDim.x / nchunks)) : 1;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int job = blockIdx.x; job < nchunks * S; job += gridDim.x) {
         const int chunk = job / S, part = job - chunk * S;
-        const bool mine = (int)threadIdx.x >= part * LEVEL_CHUNK / S && (int)threadIdx.x < (part + 1) * LEVEL_CHUNK / S;
+        const int lo_t = part * LEVEL_CHUNK / S, hi_t = (part + 1) * LEVEL_CHUNK / S;
+        const bool mine = (int)threadIdx.x >= lo_t && (int)threadIdx.x < hi_t;
         const int chunk_off = prefix(chunk);
         const int node = s + chunk * LEVEL_CHUNK + threadIdx.x;
         const int nc = node < e ? __ldcg(tmp_cur + (node - s)) : 0;
-        sc[threadIdx.x] = nc;
-        __syncthreads();
-        for (int o = 1; o < LEVEL_CHUNK; o <<= 1) {
-            const int v = (int)threadIdx.x >= o ? sc[threadIdx.x - o] : 0;
-            __syncthreads();
-            sc[threadIdx.x] += v;
-            __syncthreads();
+        // child offsets within the chunk: warp scans, then a scan of the 32 warp totals
+        int incl = nc;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += y;
         }
-        const int off = sc[threadIdx.x] - nc + chunk_off;
+        if (lane == 31) sc[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            int w = sc[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(FULL, w, o);
+                if (lane >= o) w += y;
+            }
+            sc[lane] = w;
+        }
+        __syncthreads();
+        incl += warp > 0 ? sc[warp - 1] : 0;
+        const int off = incl - nc + chunk_off;
+        if (COUNT) {
+            // the children of this block's nodes occupy [cbase + sc[32], cbase + sc[33])
+            if ((int)threadIdx.x == lo_t) sc[32] = off;
+            if ((int)threadIdx.x == hi_t - 1) sc[33] = incl + chunk_off;
+        }
         __syncthreads();
         if (mine && node < e && nc > 0) {
             const int b = __ldcg(na.begin + node), cnt = __ldcg(na.count + node);
@@ -619,6 +718,11 @@ __device__ __forceinline__ void build_level(const NodeArrays& na, int* lvl_start
                 }
             }
         }
+        if (COUNT && !full) {
+            __syncthreads();   // this block's child records, visible to all its threads
+            count_nodes_block<D>(na, nx.keys, nx.n, cbase + sc[32], cbase + sc[33], cbase, l + 1, nx.levels,
+                                 nx.lv, nx.leaf_num, nx.lvl_tmp, nx.chunk_sum, nx.trunc);
+        }
     }
 }
 
@@ -628,9 +732,9 @@ __global__ void __launch_bounds__(LEVEL_CHUNK) level_build_kernel(NodeArrays na,
                                                                   int* cs_clear, int cs_cap, int node_cap,
                                                                   unsigned* err)
 {
-    __shared__ int sc[LEVEL_CHUNK];
+    __shared__ int sc[34];
     __shared__ int red[32];
-    build_level<D>(na, lvl_start, l, tmp_cur, cs_cur, cs_clear, cs_cap, node_cap, err, sc, red);
+    build_level<D, false>(na, lvl_start, l, tmp_cur, cs_cur, cs_clear, cs_cap, node_cap, err, sc, red, NextCount{});
 }
 
 // Bounded grid-wide barrier of a cooperative launch (all blocks resident): the last block to
@@ -665,8 +769,8 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned* err)
 }
 
 // Every level of the build in one cooperative launch: the counts of the roots, then per level the
-// placement of its children and their counts, with a grid-wide barrier between the phases (the
-// same work as the per-level launches, without their launch gaps).
+// placement of its children, each block counting the children it placed, with one grid-wide
+// barrier per level (the same nodes as the per-level launches, without their launch gaps).
 template <int D>
 __global__ void __launch_bounds__(LEVEL_CHUNK) levels_fused_kernel(NodeArrays na, const unsigned long long* keys,
                                                                    int n, int* lvl_start, int levels, int lv,
@@ -675,7 +779,7 @@ __global__ void __launch_bounds__(LEVEL_CHUNK) levels_fused_kernel(NodeArrays na
                                                                    int* trunc, unsigned* err, unsigned* bar,
                                                                    int inject_leave)
 {
-    __shared__ int sc[LEVEL_CHUNK];
+    __shared__ int sc[34];
     __shared__ int red[32];
     int* tmp[2] = {tmp0, tmp1};
     int* cs[3] = {cs0, cs1, cs2};
@@ -685,17 +789,17 @@ __global__ void __launch_bounds__(LEVEL_CHUNK) levels_fused_kernel(NodeArrays na
     if (inject_leave && blockIdx.x == 0) return;
     for (int l = 1; l <= lv; ++l) {
         if (!grid_barrier(bar, err)) return;
-        build_level<D>(na, lvl_start, l, tmp[l & 1], cs[l % 3], cs[(l + 2) % 3], cs_cap, node_cap, err, sc, red);
-        if (!grid_barrier(bar, err)) return;
-        // an empty level l + 1 leaves every deeper level empty: their starts are its end
-        const int end = __ldcg(lvl_start + l + 2);
-        if (end == __ldcg(lvl_start + l + 1)) {
+        // an empty level l leaves every deeper level empty: their starts are its end
+        const int end = __ldcg(lvl_start + l + 1);
+        if (l > 1 && end == __ldcg(lvl_start + l)) {
             if (blockIdx.x == 0)
-                for (int q = l + 3 + (int)threadIdx.x; q <= lv + 2; q += (int)blockDim.x) lvl_start[q] = end;
+                for (int q = l + 2 + (int)threadIdx.x; q <= lv + 2; q += (int)blockDim.x) lvl_start[q] = end;
             return;
         }
-        count_level<D, LEVEL_CHUNK>(na, keys, n, lvl_start, l + 1, levels, lv, leaf_num, tmp[(l + 1) & 1],
-                                    cs[(l + 1) % 3], trunc, red);
+        // the children of level l, and their counts (level l + 1) by the blocks that placed them
+        const NextCount nx{keys, n, levels, lv, leaf_num, tmp[(l + 1) & 1], cs[(l + 1) % 3], trunc};
+        build_level<D, true>(na, lvl_start, l, tmp[l & 1], cs[l % 3], cs[(l + 2) % 3], cs_cap, node_cap, err,
+                             sc, red, nx);
     }
 }
 
