@@ -163,28 +163,41 @@ __global__ void radix_hist_kernel(const unsigned long long* keys, int n, int shi
 // digit; the digit totals go to dtot.
 __global__ void radix_scan_columns_kernel(int* hist, int nblocks, int* dtot)
 {
-    __shared__ int part[1024];
+    __shared__ int part[32];
     int* col = hist + (size_t)blockIdx.x * nblocks;
     const int t = threadIdx.x;
     const int per = (nblocks + 1023) / 1024;
     const int b = t * per, e = min(nblocks, b + per);
     int sum = 0;
     for (int i = b; i < e; ++i) sum += col[i];
-    part[t] = sum;
-    __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {
-        const int v = t >= o ? part[t - o] : 0;
-        __syncthreads();
-        part[t] += v;
-        __syncthreads();
+    // block scan of the 1024 partial sums: warp scans, then a scan of the 32 warp totals
+    const int lane = t & 31, w = t >> 5;
+    int incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += y;
     }
-    int run = t > 0 ? part[t - 1] : 0;
+    if (lane == 31) part[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        int x = part[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(FULL, x, o);
+            if (lane >= o) x += y;
+        }
+        part[lane] = x;
+    }
+    __syncthreads();
+    incl += w > 0 ? part[w - 1] : 0;
+    int run = incl - sum;
     for (int i = b; i < e; ++i) {
         const int v = col[i];
         col[i] = run;
         run += v;
     }
-    if (t == 1023) dtot[blockIdx.x] = part[1023];
+    if (t == 1023) dtot[blockIdx.x] = incl;
 }
 
 __global__ void radix_scatter_kernel(const unsigned long long* kin, const int* vin,
@@ -206,10 +219,20 @@ __global__ void radix_scatter_kernel(const unsigned long long* kin, const int* v
     const int excl = base[t] - dtot[t];
     __syncthreads();
     base[t] = excl + hist[t * nblocks + blockIdx.x];
+    // the tile's keys and values in registers first: one load latency for the tile, not one per round
+    unsigned long long kr[RADIX_ITEMS];
+    int vr[RADIX_ITEMS];
+#pragma unroll
+    for (int round = 0; round < RADIX_ITEMS; ++round) {
+        const int idx = blockIdx.x * RADIX_TILE + round * RADIX_THREADS + t;
+        kr[round] = idx < n ? kin[idx] : 0ull;
+        vr[round] = idx < n ? vin[idx] : 0;
+    }
+#pragma unroll
     for (int round = 0; round < RADIX_ITEMS; ++round) {
         const int idx = blockIdx.x * RADIX_TILE + round * RADIX_THREADS + t;
         const bool valid = idx < n;
-        const unsigned long long k = valid ? kin[idx] : 0ull;
+        const unsigned long long k = kr[round];
         const int d = valid ? (int)((k >> shift) & 255) : 256;
 #pragma unroll
         for (int ww = 0; ww < RADIX_THREADS / 32; ++ww) wcnt[ww][t] = 0;
@@ -229,7 +252,7 @@ __global__ void radix_scatter_kernel(const unsigned long long* kin, const int* v
         if (valid) {
             const int pos = base[d] + wcnt[w][d] + rank;
             kout[pos] = k;
-            vout[pos] = vin[idx];
+            vout[pos] = vr[round];
         }
         __syncthreads();
         base[t] += s;
@@ -1135,18 +1158,35 @@ __global__ void group_flags_kernel(const unsigned long long* keys, const int* ru
 __global__ void group_write_kernel(const unsigned char* flag, const int* blk_off, int n, int G,
                                    int* g_begin, int* g_count)
 {
-    __shared__ int wc[GF_THREADS / 32];
+    constexpr int NW = GF_THREADS / 32;
+    __shared__ int wc[NW];
+    __shared__ int wfirst[NW + 1];   // first group start of each warp of the block (n when none)
     const int i = blockIdx.x * GF_THREADS + threadIdx.x;
     const bool f = i < n && flag[i];
     const unsigned bal = __ballot_sync(FULL, f);
-    const int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) wc[w] = __popc(bal);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        wc[w] = __popc(bal);
+        wfirst[w] = bal ? (i + __ffs(bal) - 1) : n;
+    }
     __syncthreads();
     if (!f) return;
     int o = blk_off[blockIdx.x] + __popc(bal & lanemask_lt());
     for (int q = 0; q < w; ++q) o += wc[q];
-    int e = i + 1;
-    while (e < n && e < i + G && !flag[e]) ++e;
+    // the group ends at the next start: later in this warp, else in a later warp of the block, else
+    // (the block's last group) found by a scan past the block of at most G flags
+    const unsigned above = lane < 31 ? bal & (FULL << (lane + 1)) : 0u;
+    int e = n;
+    if (above) {
+        e = i - lane + __ffs(above) - 1;
+    } else {
+        for (int q = w + 1; q < NW && e == n; ++q) e = wfirst[q];
+        if (e == n) {
+            e = (blockIdx.x + 1) * GF_THREADS;
+            while (e < n && e < i + G && !flag[e]) ++e;
+        }
+    }
+    e = min(e, min(n, i + G));
     g_begin[o] = i;
     g_count[o] = e - i;
 }
