@@ -244,13 +244,17 @@ const char* sphgpu_last_error(const sphgpu_ctx* ctx);
  * 31 group plans, bit 0 FluidForce, bit 1 PreInteraction (default 0): a walk kernel ahead of the
  * stage's first pass forms every group's box and leaf list with one warp per group, so that the
  * pass itself neither reduces the box nor walks the octree (groups without a plan walk there);
- * 32 octree levels in one cooperative launch on/off (default on in 2D and 3D): the levels' split counts and
- * child placement with a bounded grid-wide barrier between them, instead of two launches per level
+ * 32 octree levels in one cooperative launch on/off (default on in 2D and 3D): per level the child
+ * placement and the children's split counts with one bounded grid-wide barrier, instead of two launches per level
  * (a barrier wait that runs out stops the build, the kernels that use the tree return at once and
  * the step returns SPHGPU_ERR_CUDA with the text in sphgpu_last_error);
  * 33 fault injection for the tests of that bounded wait: with 1, the next fused level build's
  * first block leaves without arriving at the first barrier, so the other blocks' wait runs out
- * (one build only; the knob then reads 0). */
+ * (one build only; the knob then reads 0);
+ * 34 key table: 0 off, 1 from 2^18 particles on (default), 2 always (reads 0 when a batch has too
+ * many runs for its 64 MB): the first eight levels of each run's octree-centre recursion replayed
+ * once per tree build into a table that the key computation searches with integer comparisons
+ * (the same keys, fewer FP64 additions). */
 int sphgpu_set_tuning(sphgpu_ctx* ctx, int which, int value);
 int sphgpu_get_tuning(sphgpu_ctx* ctx, int which, int* value);
 

@@ -1303,6 +1303,11 @@ int sphgpu_set_tuning(sphgpu_ctx* h, int which, int value)
     case 29: c.bulk_stage = value != 0; break;
     case 32: c.fused_levels = value != 0; c.tree_valid = false; break;
     case 33: c.inject_barrier_timeout = value != 0; break;
+    case 34:
+        if (value < 0 || value > 2) return SPHGPU_ERR_ARG;
+        c.key_table_on = value;
+        c.tree_valid = false;
+        break;
     case 31:
         if (value < 0 || value > 3) return SPHGPU_ERR_ARG;
         c.prewalk = value;
@@ -1357,6 +1362,7 @@ int sphgpu_get_tuning(sphgpu_ctx* h, int which, int* value)
     case 31: *value = c.prewalk; break;
     case 32: *value = c.fused_levels; break;
     case 33: *value = c.inject_barrier_timeout; break;
+    case 34: *value = c.key_table ? c.key_table_on : 0; break;
     case 13: case 14: case 15: case 16: case 17: {
         cudaStreamSynchronize(c.stream);
         cudaMemcpy(value, c.d_work + sphgpu::FAIL_INFO_SLOT + (which - 13), sizeof(int), cudaMemcpyDeviceToHost);

@@ -99,11 +99,46 @@ __global__ void roots_kernel(TreeView tv, double* center0, double* center1, doub
 
 // ---- keys -------------------------------------------------------------------------------
 
+// Centres of the first KEY_TABLE_LEVELS levels of every run's split, per axis: the centre
+// recursion of keys_kernel replayed once per node of a complete binary tree (heap order: node k
+// has children 2k (x <= c) and 2k + 1 (x > c)), with the same FP64 operations in the same order,
+// so a particle's path through the table equals its path through the recursion.  Entries
+// k < 2^T hold the ordered-integer image of the centre (compared against), entries 2^T <= k < 2^(T+1)
+// the centre itself (where the particle's recursion continues).
+constexpr int KEY_TABLE_LEVELS = 8;
+constexpr int KEY_TABLE_SIZE = 2 << KEY_TABLE_LEVELS;   // entries 1 .. 2^(T+1) - 1 used
+
+__global__ void key_table_kernel(TreeView tv, int R, int D, int T, long long* table)
+{
+    const int ts = 2 << T;
+    const long long total = (long long)R * D * ts;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(q % ts);
+        const int ax = (int)((q / ts) % D);
+        const int r = (int)(q / ((long long)ts * D));
+        if (k == 0) { table[q] = 0; continue; }
+        const int depth = 31 - __clz(k);
+        double c = tv.center[ax][r] + 0.0;
+        const double e0 = tv.edge[r];
+        const bool scale = e0 > 0.0;
+        long long qb = scale ? __double_as_longlong(e0) - (2LL << 52) : 0;
+        for (int l = 0; l < depth; ++l) {
+            const double qd = scale ? __longlong_as_double(qb) : 0.0;
+            const bool up = (k >> (depth - 1 - l)) & 1;
+            c = __dadd_rn(c, up ? qd : -qd);
+            qb -= 1LL << 52;
+        }
+        table[q] = depth < T ? dbl_to_ord(c) : __double_as_longlong(c);
+    }
+}
+
 // The path of a particle through the reference's recursive split, one D-bit digit per level,
-// most significant first, with the run index above the digits.
+// most significant first, with the run index above the digits.  With a table (T > 0) the first
+// T levels are a search through it (integer comparisons, no FP64 arithmetic) and the recursion
+// continues from the level-T centre the search ends at.
 template <int D>
 __global__ void keys_kernel(State st, int n, TreeView tv, int levels, int nd, int run_shift,
-                            unsigned long long* keys, int* perm)
+                            unsigned long long* keys, int* perm, const long long* table, int T)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -122,8 +157,30 @@ __global__ void keys_kernel(State st, int n, TreeView tv, int levels, int nd, in
 #pragma unroll
     for (int k = 0; k < D; ++k) xo[k] = dbl_to_ord(x[k]);
     unsigned long long key = 0;
+    int l0 = 0;
+    if (T > 0) {
+        const int ts = 2 << T;
+        const long long* tb = table + (size_t)r * D * ts;
+        int kk[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) kk[k] = 1;
+        for (int l = 0; l < T; ++l) {
+            unsigned digit = 0;
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+                const bool up = xo[k] > __ldg(tb + k * ts + kk[k]);
+                digit |= (up ? 1u : 0u) << k;
+                kk[k] = 2 * kk[k] + (up ? 1 : 0);
+            }
+            key = (key << D) | digit;
+        }
+#pragma unroll
+        for (int k = 0; k < D; ++k) c[k] = __longlong_as_double(__ldg(tb + k * ts + kk[k]));
+        q -= (long long)T << 52;
+        l0 = T;
+    }
     // the first nd digits (the levels a capped build splits); deeper digits stay 0
-    for (int l = 0; l < nd; ++l) {
+    for (int l = l0; l < nd; ++l) {
         unsigned digit = 0;
         const double qd = scale ? __longlong_as_double(q) : 0.0;
 #pragma unroll
@@ -1289,6 +1346,9 @@ int tree_alloc(Ctx& c)
     c.radix_blocks = ceil_div(n, RADIX_TILE);
     A((void**)&c.radix_hist, sizeof(int) * 256 * c.radix_blocks);
     A((void**)&c.radix_dtot, sizeof(int) * 256);
+    // key tables (R runs x dim axes x 2^(T+1) entries), skipped for batches too large for 64 MB
+    const size_t kt = (size_t)c.R * c.dim * KEY_TABLE_SIZE;
+    if (kt * sizeof(long long) <= (64u << 20)) A((void**)&c.key_table, sizeof(long long) * kt);
     A((void**)&c.nd_begin, sizeof(int) * nc);
     A((void**)&c.nd_count, sizeof(int) * nc);
     A((void**)&c.nd_first, sizeof(int) * nc);
@@ -1342,7 +1402,7 @@ int tree_alloc(Ctx& c)
 
 void tree_free(Ctx& c)
 {
-    void* ptrs[] = {c.keys, c.keys_alt, c.perm, c.perm_alt, c.radix_hist, c.nd_begin, c.nd_count,
+    void* ptrs[] = {c.keys, c.keys_alt, c.perm, c.perm_alt, c.radix_hist, c.key_table, c.nd_begin, c.nd_count,
                     c.nd_first, c.nd_nchild, c.nd_parent, c.nd_level, c.nd_arrive, c.nd_center[0],
                     c.nd_center[1], c.nd_center[2], c.nd_com[0], c.nd_com[1], c.nd_com[2],
                     c.nd_edge, c.nd_mass, c.nd_ksize, c.lvl_start, c.lvl_tmp, c.chunk_sum, c.bbox,
@@ -1405,7 +1465,18 @@ static void make_tree_d(Ctx& c, bool reorder_all, bool full_depth)
     // at most depth_cap otherwise
     const int lv = (full_depth || c.p.use_gravity || c.depth_cap <= 0) ? levels : std::min(levels, c.depth_cap);
     c.tree_levels = lv;
-    keys_kernel<D><<<ceil_div(n, 256), 256, 0, s>>>(c.st, n, tv, levels, lv, run_shift, c.keys, c.perm);
+    // the first levels of every run's centre recursion as a table (knob 34), when it fits; below
+    // 2^18 particles the table's launch costs more than the FP64 additions it saves (Gresho 65k:
+    // +0.4 % per step with it; KHI 786k -1.4 %, the 10.6M-particle ensemble -1.6 %)
+    const bool table = c.key_table && (c.key_table_on == 2 || (c.key_table_on == 1 && n >= (1 << 18)));
+    const int T = table ? std::min(KEY_TABLE_LEVELS, lv) : 0;
+    if (T > 0) {
+        const long long total = (long long)R * D * (2 << T);
+        key_table_kernel<<<(int)std::min<long long>(ceil_div((int)std::min<long long>(total, 1LL << 30), 256), 4096), 256, 0, s>>>(
+            tv, R, D, T, c.key_table);
+    }
+    keys_kernel<D><<<ceil_div(n, 256), 256, 0, s>>>(c.st, n, tv, levels, lv, run_shift, c.keys, c.perm,
+                                                   c.key_table, T);
     // radix sort on the significant bits: the lv digits computed and the run index
     const int shift0 = D * (levels - lv);
     const int bits = D * lv + c.run_bits;
