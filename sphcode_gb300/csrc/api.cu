@@ -608,7 +608,10 @@ void run_step(Ctx& c, bool timed)
     cudaStream_t s = c.stream;
     if (timed) cudaEventRecord(c.ev[0], s);
     if (!c.fixed_dt) launch_timestep(c);
-    launch_predict(c);
+    // the sound speed of the predicted u is formed by the Pre and Fluid mirrors (the same value)
+    // and stored by correct at the end of the step
+    launch_predict(c, false);
+    c.sound_from_ene = true;
     if (timed) cudaEventRecord(c.ev[1], s);
     launch_make_tree(c, false);
     if (timed) cudaEventRecord(c.ev[2], s);
@@ -624,6 +627,7 @@ void run_step(Ctx& c, bool timed)
     }
     if (c.p.use_gravity) launch_gravity(c);
     if (timed) cudaEventRecord(c.ev[5], s);
+    c.sound_from_ene = false;
     launch_correct(c);
     launch_update_time(c);
 }

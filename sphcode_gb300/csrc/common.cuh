@@ -302,6 +302,19 @@ __device__ __forceinline__ bool tree_failed(const unsigned* err)
     return (*(const volatile unsigned*)err & ERR_TIMEOUT) != 0u;
 }
 
+// Sound speed of a mirror record: inside a whole step (c_sound > 0) sqrt(c_sound u) from the
+// predicted u, the value predict would have stored (the same FP64 expression in FP64 records;
+// in FP32 records the IEEE FP32 root of the rounded product); otherwise the stored field.
+template <typename T>
+__device__ __forceinline__ T mirror_sound(const State& st, int i, double u, double c_sound)
+{
+    if (c_sound > 0.0) {
+        if constexpr (std::is_same<T, float>::value) return __fsqrt_rn((float)(c_sound * u));
+        else return sqrt(c_sound * u);
+    }
+    return (T)st.f[F_SOUND][i];
+}
+
 // Adds v over the 32 lanes of a converged warp into *p (lane 0 issues one atomic).
 __device__ __forceinline__ void warp_count(unsigned long long* p, unsigned long long v)
 {

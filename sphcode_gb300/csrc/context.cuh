@@ -164,6 +164,8 @@ struct Ctx {
     // the tree's levels in one cooperative launch with grid-wide barriers (knob 32), instead of two
     // launches per level
     int fused_levels = 1;
+    // inside run_step: predict leaves the sound speed to the mirror kernels of Pre and Fluid
+    bool sound_from_ene = false;
     int inject_barrier_timeout = 0; // knob 33: the next fused level build's block 0 leaves early (tests)
     GroupPlan* plan = nullptr;
     int plan_cap = 0;
@@ -219,7 +221,7 @@ void launch_adjoint_dim(Ctx& c, double* adj, const double* dens_bar, double* alp
 
 // ---- integrate.cu
 void launch_timestep(Ctx& c);
-void launch_predict(Ctx& c);
+void launch_predict(Ctx& c, bool store_sound = true);
 void launch_correct(Ctx& c);
 void launch_init_fields(Ctx& c);
 void launch_update_time(Ctx& c);

@@ -483,7 +483,7 @@ __global__ void __launch_bounds__(128) fluid_tpp_kernel(FluidArgs<T> a)
 template <int D, typename T, int TYPE>
 __global__ void fluid_mirror_kernel(State st, int n, typename Vec4<T>::type* rec0,
                                     typename Vec4<T>::type* rec1, typename Vec4<T>::type* rec2,
-                                    T* grad, int gsph_2nd)
+                                    T* grad, int gsph_2nd, double c_sound)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -495,7 +495,7 @@ __global__ void fluid_mirror_kernel(State st, int n, typename Vec4<T>::type* rec
     typename Vec4<T>::type b;
     b.x = (T)rho;
     b.y = (T)p;
-    b.z = (T)st.f[F_SOUND][i];
+    b.z = mirror_sound<T>(st, i, st.f[F_ENE][i], c_sound);
     typename Vec4<T>::type c;
     c.x = (T)st.f[F_ALPHA][i];
     c.y = (T)st.f[F_BALSARA][i];
@@ -549,7 +549,8 @@ void run_fluid(Ctx& c)
     V4* rec1 = (V4*)c.mir[3];
     V4* rec2 = (V4*)c.mir[4];
     T* grad = (T*)c.mir[5];
-    fluid_mirror_kernel<D, T, TYPE><<<ceil_div(c.n, 256), 256, 0, s>>>(c.st, c.n, rec0, rec1, rec2, grad, c.p.gsph_2nd_order);
+    fluid_mirror_kernel<D, T, TYPE><<<ceil_div(c.n, 256), 256, 0, s>>>(
+        c.st, c.n, rec0, rec1, rec2, grad, c.p.gsph_2nd_order, c.sound_from_ene ? c.p.gamma * (c.p.gamma - 1.0) : 0.0);
     reset_work_counters(c);
     FluidArgs<T> a{};
     a.st = c.st;

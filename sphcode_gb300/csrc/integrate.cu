@@ -111,7 +111,9 @@ __global__ void timestep_final_kernel(int R, double cfl_sound, const long long* 
     emin[r] = 0x7f800000;
 }
 
-template <int D>
+// SOUND false (inside a whole step): the sound speed is not stored here; the stages that follow
+// form sqrt(c_sound u) from the predicted u in their mirror kernels, and correct stores it.
+template <int D, bool SOUND>
 __global__ void predict_kernel(State st, int n, const double* dt_run, double c_sound, Periodic pb)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -134,7 +136,7 @@ __global__ void predict_kernel(State st, int n, const double* dt_run, double c_s
     st.f[F_ENEP][i] = u + du * (0.5 * dt);
     const double un = u + du * dt;
     st.f[F_ENE][i] = un;
-    st.f[F_SOUND][i] = sqrt(c_sound * un);
+    if (SOUND) st.f[F_SOUND][i] = sqrt(c_sound * un);
 }
 
 template <int D>
@@ -241,13 +243,19 @@ void launch_timestep(Ctx& c)
                                                                      c.d_emin, c.d_dt);
 }
 
-void launch_predict(Ctx& c)
+void launch_predict(Ctx& c, bool store_sound)
 {
     const int g = ceil_div(c.n, THREADS);
     const double cs = c.p.gamma * (c.p.gamma - 1.0);
-    if (c.dim == 1) predict_kernel<1><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.d_dt, cs, c.pb);
-    else if (c.dim == 2) predict_kernel<2><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.d_dt, cs, c.pb);
-    else predict_kernel<3><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.d_dt, cs, c.pb);
+    if (store_sound) {
+        if (c.dim == 1) predict_kernel<1, true><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.d_dt, cs, c.pb);
+        else if (c.dim == 2) predict_kernel<2, true><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.d_dt, cs, c.pb);
+        else predict_kernel<3, true><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.d_dt, cs, c.pb);
+    } else {
+        if (c.dim == 1) predict_kernel<1, false><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.d_dt, cs, c.pb);
+        else if (c.dim == 2) predict_kernel<2, false><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.d_dt, cs, c.pb);
+        else predict_kernel<3, false><<<g, THREADS, 0, c.stream>>>(c.st, c.n, c.d_dt, cs, c.pb);
+    }
 }
 
 void launch_correct(Ctx& c)

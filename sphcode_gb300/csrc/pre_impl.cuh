@@ -693,17 +693,18 @@ __global__ void __launch_bounds__(128) pre_walk_kernel(PreArgs<T> a, int stack_c
 
 // Key-ordered T mirrors of the source fields Pre reads per pair.
 template <int D, typename T>
-__global__ void pre_mirror_kernel(State st, int n, typename Vec4<T>::type* mvel, T* mu)
+__global__ void pre_mirror_kernel(State st, int n, typename Vec4<T>::type* mvel, T* mu, double c_sound)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const double u = st.f[F_ENE][i];
     typename Vec4<T>::type v;
     v.x = (T)st.f[F_VEL][i];
     v.y = D > 1 ? (T)st.f[F_VEL + (D > 1 ? 1 : 0)][i] : T(0);
     v.z = D > 2 ? (T)st.f[F_VEL + (D > 2 ? 2 : 0)][i] : T(0);
-    v.w = (T)st.f[F_SOUND][i];
+    v.w = mirror_sound<T>(st, i, u, c_sound);
     mvel[i] = v;
-    mu[i] = (T)st.f[F_ENE][i];
+    mu[i] = (T)u;
 }
 
 static __global__ void pre_reset_kernel(int R, long long* hvs, int* counters, int ncounters)
@@ -728,7 +729,8 @@ void run_pre(Ctx& c, bool initial)
     using V4 = typename Vec4<T>::type;
     auto kern = pre_kernel<D, T, TYPE, K>;
     cudaStream_t s = c.stream;
-    pre_mirror_kernel<D, T><<<ceil_div(c.n, 256), 256, 0, s>>>(c.st, c.n, (V4*)c.mir[0], (T*)c.mir[1]);
+    pre_mirror_kernel<D, T><<<ceil_div(c.n, 256), 256, 0, s>>>(c.st, c.n, (V4*)c.mir[0], (T*)c.mir[1],
+                                                              c.sound_from_ene ? c.p.gamma * (c.p.gamma - 1.0) : 0.0);
     // counters: [0] main work, [1] overflow count, [2] overflow work; plus h/v_sig and Newton
     if (!initial) pre_reset_kernel<<<ceil_div(std::max(c.R, 48), 128), 128, 0, s>>>(c.R, c.d_hvs, c.d_work, 48);
     else pre_reset_kernel<<<1, 64, 0, s>>>(0, c.d_hvs, c.d_work, 48);

@@ -20,7 +20,9 @@ def test_module_path_equals_step_graph(gpu_lib):
     with sphgpu.GpuSimulation(p, f, precision="fp64") as g:
         g.initialize()
         g.step(3)
-        for k in ("pos", "vel", "ene", "dens", "acc", "dene"):
+        # the step graph forms the predicted sound speed in the Pre/Fluid mirrors, the module path
+        # stores it in predict: the same FP64 expression, so the same forces and the same state
+        for k in ("pos", "vel", "ene", "dens", "acc", "dene", "sound", "alpha", "pres"):
             assert rel_err(s.sim.gpu.get(k), g.get(k)) <= 1e-13, k
         assert s.sim.get_time() == pytest.approx(g.scalar("time"), rel=1e-15)
     s.close()
