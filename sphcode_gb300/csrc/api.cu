@@ -282,8 +282,10 @@ void free_state(State& s, bool primary)
 
 void free_ctx(Ctx& c)
 {
-    if (c.graph) cudaGraphExecDestroy(c.graph);
-    if (c.adj_graph) cudaGraphExecDestroy(c.adj_graph);
+    for (int q = 0; q < 2; ++q) {
+        if (c.graph[q]) cudaGraphExecDestroy(c.graph[q]);
+        if (c.adj_graph[q]) cudaGraphExecDestroy(c.adj_graph[q]);
+    }
     tree_free(c);
     free_state(c.st, true);
     c.alt.run = nullptr;
@@ -675,7 +677,6 @@ void check_tree_cap(Ctx& c)
     cudaMemsetAsync(c.d_work + TREE_TRUNC_SLOT, 0, sizeof(int), c.stream);
     cudaStreamSynchronize(c.stream);
     c.depth_cap = std::min(c.key_levels, c.tree_levels + 4);
-    c.graph_valid = false;
     ++c.graph_epoch;
     c.warm = false;
 }
@@ -957,7 +958,6 @@ int sphgpu_initialize(sphgpu_ctx* h)
     sphgpu::run_pre_stage(c);
     sphgpu::launch_fluid(c);
     if (c.p.use_gravity) sphgpu::launch_gravity(c);
-    c.graph_valid = false;
     ++c.graph_epoch;
     const int rc = sphgpu::finish(c, "initialize");
     // later builds split two levels deeper than the initial tree (without gravity)
@@ -986,10 +986,11 @@ int sphgpu_step(sphgpu_ctx* h, int n_steps)
             }
             continue;
         }
-        if (!c.graph_valid) {
-            // the first call on a fresh configuration runs eagerly (caches launch shapes),
-            // then the step is captured once and replayed from then on
-            if (c.graph) { cudaGraphExecDestroy(c.graph); c.graph = nullptr; }
+        const int par = c.parity;
+        if (!sphgpu::step_graph_ready(c, par)) {
+            // the first call on a fresh configuration runs eagerly (caches launch shapes); then
+            // the step of each buffer parity is captured once and replayed from then on
+            if (c.graph[par]) { cudaGraphExecDestroy(c.graph[par]); c.graph[par] = nullptr; }
             if (!c.warm) {
                 sphgpu::run_step(c, false);
                 c.warm = true;
@@ -998,7 +999,7 @@ int sphgpu_step(sphgpu_ctx* h, int n_steps)
             cudaGraph_t g = nullptr;
             cudaError_t e = cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal);
             if (e != cudaSuccess) return sphgpu::cuda_status(c, e, "step capture");
-            sphgpu::run_step(c, false);
+            sphgpu::run_step(c, false);   // the host side of the step (buffer swap) happens here
             e = cudaStreamEndCapture(c.stream, &g);
             if (e != cudaSuccess) return sphgpu::cuda_status(c, e, "step capture");
             {
@@ -1014,13 +1015,17 @@ int sphgpu_step(sphgpu_ctx* h, int n_steps)
                 }
                 c.graph_kernels = nk;
             }
-            e = cudaGraphInstantiate(&c.graph, g, 0);
+            e = cudaGraphInstantiate(&c.graph[par], g, 0);
             cudaGraphDestroy(g);
-            if (e != cudaSuccess) return sphgpu::cuda_status(c, e, "step instantiate");
-            c.graph_valid = true;
+            if (e != cudaSuccess) { c.graph[par] = nullptr; return sphgpu::cuda_status(c, e, "step instantiate"); }
+            c.graph_epoch_of[par] = c.graph_epoch;
+            e = cudaGraphLaunch(c.graph[par], c.stream);
+            if (e != cudaSuccess) return sphgpu::cuda_status(c, e, "step launch");
+            continue;
         }
-        cudaError_t e = cudaGraphLaunch(c.graph, c.stream);
+        cudaError_t e = cudaGraphLaunch(c.graph[par], c.stream);
         if (e != cudaSuccess) return sphgpu::cuda_status(c, e, "step launch");
+        sphgpu::step_reorder_swap(c);   // the replayed step's buffer swap, on the host
     }
     sphgpu::nonfinite_kernel<<<sphgpu::ceil_div(c.n, 256), 256, 0, c.stream>>>(c.st, c.n, c.dim, c.d_err);
     const int rc = sphgpu::finish(c, "step");
@@ -1097,28 +1102,30 @@ int sphgpu_adjoint_step(sphgpu_ctx* h, double* adj, const double* dens_bar, doub
     };
     const void* key[3] = {adj, dens_bar, alpha_bar};
     auto same = [&](const void* const* k) { return k[0] == key[0] && k[1] == key[1] && k[2] == key[2]; };
+    const int par = c.parity;   // the body's reorder swaps the field buffers, as in a step
     if (!c.use_graph || c.timing) {
         body();
-    } else if (c.adj_graph && c.adj_epoch == c.graph_epoch && same(c.adj_key)) {
-        cudaError_t e = cudaGraphLaunch(c.adj_graph, c.stream);
+    } else if (c.adj_graph[par] && c.adj_epoch[par] == c.graph_epoch && same(c.adj_key[par])) {
+        cudaError_t e = cudaGraphLaunch(c.adj_graph[par], c.stream);
         if (e != cudaSuccess) return sphgpu::cuda_status(c, e, "adjoint_step launch");
+        sphgpu::step_reorder_swap(c);
     } else if (!same(c.adj_warm_key)) {
         body();
         for (int q = 0; q < 3; ++q) c.adj_warm_key[q] = key[q];
     } else {
-        if (c.adj_graph) { cudaGraphExecDestroy(c.adj_graph); c.adj_graph = nullptr; }
+        if (c.adj_graph[par]) { cudaGraphExecDestroy(c.adj_graph[par]); c.adj_graph[par] = nullptr; }
         cudaGraph_t g = nullptr;
         cudaError_t e = cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) return sphgpu::cuda_status(c, e, "adjoint_step capture");
         body();
         e = cudaStreamEndCapture(c.stream, &g);
         if (e != cudaSuccess) return sphgpu::cuda_status(c, e, "adjoint_step capture");
-        e = cudaGraphInstantiate(&c.adj_graph, g, 0);
+        e = cudaGraphInstantiate(&c.adj_graph[par], g, 0);
         cudaGraphDestroy(g);
-        if (e != cudaSuccess) { c.adj_graph = nullptr; return sphgpu::cuda_status(c, e, "adjoint_step instantiate"); }
-        for (int q = 0; q < 3; ++q) c.adj_key[q] = key[q];
-        c.adj_epoch = c.graph_epoch;
-        e = cudaGraphLaunch(c.adj_graph, c.stream);
+        if (e != cudaSuccess) { c.adj_graph[par] = nullptr; return sphgpu::cuda_status(c, e, "adjoint_step instantiate"); }
+        for (int q = 0; q < 3; ++q) c.adj_key[par][q] = key[q];
+        c.adj_epoch[par] = c.graph_epoch;
+        e = cudaGraphLaunch(c.adj_graph[par], c.stream);
         if (e != cudaSuccess) return sphgpu::cuda_status(c, e, "adjoint_step launch");
     }
     rc = sphgpu::finish(c, "adjoint_step");
@@ -1327,7 +1334,6 @@ int sphgpu_set_tuning(sphgpu_ctx* h, int which, int value)
     case 6: c.use_graph = value != 0; break;
     default: return SPHGPU_ERR_ARG;
     }
-    c.graph_valid = false;
     ++c.graph_epoch;
     c.warm = false;
     return SPHGPU_OK;
@@ -1389,10 +1395,12 @@ int sphgpu_bench_steps(sphgpu_ctx* h, int n_steps, int flush_l2, double* ms)
         cudaError_t e = cudaMalloc((void**)&c.d_flush, c.flush_bytes);
         if (e != cudaSuccess) { c.d_flush = nullptr; return sphgpu::cuda_status(c, e, "bench flush buffer"); }
     }
-    // make sure the step graph exists (the capture path runs its own steps first)
-    if (c.use_graph && !c.timing && !c.graph_valid) {
-        int rc = sphgpu_step(h, 2);
-        if (rc != SPHGPU_OK) return rc;
+    // make sure the step graphs of both buffer parities exist (the capture path runs its own steps)
+    if (c.use_graph && !c.timing) {
+        for (int tries = 0; tries < 4 && !(sphgpu::step_graph_ready(c, 0) && sphgpu::step_graph_ready(c, 1)); ++tries) {
+            int rc = sphgpu_step(h, 1);
+            if (rc != SPHGPU_OK) return rc;
+        }
     }
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
@@ -1401,8 +1409,12 @@ int sphgpu_bench_steps(sphgpu_ctx* h, int n_steps, int flush_l2, double* ms)
     for (int s = 0; s < n_steps; ++s) {
         if (flush_l2) cudaMemsetAsync(c.d_flush, s & 0xff, c.flush_bytes, c.stream);
         cudaEventRecord(e0, c.stream);
-        if (c.use_graph && !c.timing) cudaGraphLaunch(c.graph, c.stream);
-        else sphgpu::run_step(c, false);
+        if (c.use_graph && !c.timing && sphgpu::step_graph_ready(c, c.parity)) {
+            cudaGraphLaunch(c.graph[c.parity], c.stream);
+            sphgpu::step_reorder_swap(c);
+        } else {
+            sphgpu::run_step(c, false);
+        }
         cudaEventRecord(e1, c.stream);
         cudaError_t e = cudaEventSynchronize(e1);
         if (e != cudaSuccess) { cudaEventDestroy(e0); cudaEventDestroy(e1); return sphgpu::cuda_status(c, e, "bench"); }

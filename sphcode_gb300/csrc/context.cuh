@@ -116,18 +116,21 @@ struct Ctx {
     bool tuned = false;
     unsigned tune_rejects = 0;      // status bits of tuning candidates that were rejected
 
-    // CUDA graph of one integrate() step
-    cudaGraphExec_t graph = nullptr;
-    bool graph_valid = false;
+    // CUDA graphs of one integrate() step, one per parity of the field buffers: a step's reorder
+    // swaps the moved fields between the state's buffers and the alternate ones (step_reorder_swap),
+    // so consecutive steps alternate between two pointer sets
+    int parity = 0;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    int graph_epoch_of[2] = {-1, -1};   // epoch each parity's graph was captured in
     bool use_graph = true;
     bool warm = false;
     int graph_kernels = 0;          // kernel nodes of the captured step
     int graph_epoch = 0;            // bumped whenever captured graphs go stale
-    // graph of one reversed step, keyed by the adjoint buffers it was captured with
-    cudaGraphExec_t adj_graph = nullptr;
-    const void* adj_key[3] = {nullptr, nullptr, nullptr};
+    // graphs of one reversed step per parity, keyed by the adjoint buffers they were captured with
+    cudaGraphExec_t adj_graph[2] = {nullptr, nullptr};
+    const void* adj_key[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
     const void* adj_warm_key[3] = {nullptr, nullptr, nullptr};
-    int adj_epoch = -1;
+    int adj_epoch[2] = {-1, -1};
 
     // stage timing
     cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -191,6 +194,8 @@ void launch_set_kernel_size(Ctx& c);
 void launch_node_moments(Ctx& c);
 TreeView tree_view(const Ctx& c);
 void launch_reorder_fields(Ctx& c, bool all);
+void step_reorder_swap(Ctx& c);
+inline bool step_graph_ready(const Ctx& c, int p) { return c.graph[p] && c.graph_epoch_of[p] == c.graph_epoch; }
 int build_groups(Ctx& c);          // host: fixed chunks per run, uploaded to the device
 
 // ---- pre_dD.cu / fluid_dD.cu / gravity.cu

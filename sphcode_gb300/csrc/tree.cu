@@ -1413,21 +1413,36 @@ void tree_free(Ctx& c)
         if (p) cudaFree(p);
 }
 
+// Inside a step, fields that the stages after the rebuild recompute before reading them need
+// no move: PRES, SML, ACC, DENE always; GRADH for ssph/disph; PHI with gravity; the gsph
+// gradients with the second-order scheme.
+static bool moved_in_step(const Ctx& c, int f)
+{
+    if (!c.st.f[f]) return false;
+    bool recomputed = (f >= F_ACC && f < F_ACC + 3) || f == F_PRES || f == F_DENE || f == F_SML;
+    if (f == F_GRADH && c.p.sph_type != 2) recomputed = true;
+    if (f == F_PHI && c.p.use_gravity) recomputed = true;
+    if (f >= F_GRADD && c.p.sph_type == 2 && c.p.gsph_2nd_order) recomputed = true;
+    return !recomputed;
+}
+
+// The host side of a step's reorder: the moved fields (and the ids) now live in the alternate
+// buffers, which become the state's; the parity of the buffer sets flips.  A replayed step graph
+// does the same on the host after its launch (the graph of each parity has its pointers baked in).
+void step_reorder_swap(Ctx& c)
+{
+    for (int f = 0; f < F_COUNT; ++f)
+        if (moved_in_step(c, f)) std::swap(c.st.f[f], c.alt.f[f]);
+    std::swap(c.st.id, c.alt.id);
+    c.parity ^= 1;
+}
+
 void launch_reorder_fields(Ctx& c, bool all)
 {
-    // Inside a step, fields that the stages after the rebuild recompute before reading them need
-    // no move: PRES, SML, ACC, DENE always; GRADH for ssph/disph; PHI with gravity; the gsph
-    // gradients with the second-order scheme.
     FieldMove fm{};
     for (int f = 0; f < F_COUNT; ++f) {
         if (!c.st.f[f]) continue;
-        if (!all) {
-            bool recomputed = (f >= F_ACC && f < F_ACC + 3) || f == F_PRES || f == F_DENE || f == F_SML;
-            if (f == F_GRADH && c.p.sph_type != 2) recomputed = true;
-            if (f == F_PHI && c.p.use_gravity) recomputed = true;
-            if (f >= F_GRADD && c.p.sph_type == 2 && c.p.gsph_2nd_order) recomputed = true;
-            if (recomputed) continue;
-        }
+        if (!all && !moved_in_step(c, f)) continue;
         fm.src[fm.nf] = c.st.f[f];
         fm.dst[fm.nf] = c.alt.f[f];
         ++fm.nf;
@@ -1436,7 +1451,13 @@ void launch_reorder_fields(Ctx& c, bool all)
     fm.ni = 1;
     if (all) { fm.isrc[1] = c.st.neighbor; fm.idst[1] = c.alt.neighbor; fm.ni = 2; }
     reorder_kernel<<<ceil_div(c.n, 256), 256, 0, c.stream>>>(fm, c.perm, c.n);
-    // copy back, so the state keeps its buffers (the step graph replays fixed pointers)
+    if (!all) {
+        // a step's reorder: the sorted copies become the state (no copy back)
+        step_reorder_swap(c);
+        return;
+    }
+    // a full reorder outside the step loop copies back, so the buffer assignment stays one of
+    // the two that the step graphs were captured with
     FieldMove back{};
     back.nf = fm.nf;
     back.ni = fm.ni;
