@@ -71,7 +71,6 @@ __device__ __forceinline__ T hk_g(T r, T h)
 template <int D, typename T, bool COUNT>
 __global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
 {
-    if (tree_failed(a.work.err)) return;   // the octree of this step was not completed
     using V4 = typename Vec4<T>::type;
     extern __shared__ __align__(16) int2 gstack[];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -85,7 +84,9 @@ __global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
     // data, so none waits at a barrier for the slowest walk of its block
     for (;;) {
         int k = 0;
-        if (lane == 0) k = atomicAdd(a.work.counter, 1);
+        // no more work once the octree of this step is known to be incomplete (checked per work
+        // item: a check at kernel entry kept four more registers live, one block fewer per SM)
+        if (lane == 0) k = tree_failed(a.work.err) ? 0x7fffffff : atomicAdd(a.work.counter, 1);
         k = __shfl_sync(FULL, k, 0);
         const int g = k / a.work.pieces, o = 32 * (k % a.work.pieces);
         if (g >= *a.work.n_groups) break;

@@ -32,32 +32,62 @@ __global__ void bbox_init_kernel(long long* bbox, int R, int D)
     bbox[r * 2 * D + D + k] = dbl_to_ord(-1.7976931348623157e308);
 }
 
+// Bounding box of every run on the ordered-integer images of the coordinates (min / max of the
+// images are those of the doubles).  Each warp takes BBOX_ROWS coalesced rows of 32 particles and
+// keeps per-lane extremes while its run stays the same (runs are contiguous), so a run issues
+// about one atomic per warp and axis instead of one per 32 particles.
+constexpr int BBOX_ROWS = 16;
 template <int D>
 __global__ void bbox_kernel(State st, int n, long long* bbox)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool ok = i < n;
-    const int r = ok ? st.run[i] : -1;
-    const unsigned same = __match_any_sync(FULL, r);
-    const bool whole_warp = same == FULL;
-    if (whole_warp && r < 0) return;   // a warp entirely past the end
+    const int lane = threadIdx.x & 31;
+    const long long base = (long long)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32 * BBOX_ROWS;
+    const long long EMPTY_LO = dbl_to_ord(1.7976931348623157e308), EMPTY_HI = dbl_to_ord(-1.7976931348623157e308);
+    long long lo[D], hi[D];
 #pragma unroll
-    for (int k = 0; k < D; ++k) {
-        double lo = ok ? st.f[F_POS + k][i] : 1.7976931348623157e308;
-        double hi = ok ? st.f[F_POS + k][i] : -1.7976931348623157e308;
-        if (whole_warp) {
-            for (int o = 16; o > 0; o >>= 1) {
-                lo = fmin(lo, __shfl_xor_sync(FULL, lo, o));
-                hi = fmax(hi, __shfl_xor_sync(FULL, hi, o));
-            }
-            if ((threadIdx.x & 31) == 0) {
-                atomicMin(&bbox[r * 2 * D + k], dbl_to_ord(lo));
-                atomicMax(&bbox[r * 2 * D + D + k], dbl_to_ord(hi));
-            }
-        } else if (ok) {
-            atomicMin(&bbox[r * 2 * D + k], dbl_to_ord(lo));
-            atomicMax(&bbox[r * 2 * D + D + k], dbl_to_ord(hi));
+    for (int k = 0; k < D; ++k) { lo[k] = EMPTY_LO; hi[k] = EMPTY_HI; }
+    int cur = -1;
+    auto flush = [&](int r) {
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            atomicMin(&bbox[r * 2 * D + k], lo[k]);
+            atomicMax(&bbox[r * 2 * D + D + k], hi[k]);
+            lo[k] = EMPTY_LO;
+            hi[k] = EMPTY_HI;
         }
+    };
+    for (int q = 0; q < BBOX_ROWS; ++q) {
+        const long long i = base + q * 32 + lane;
+        if (i >= n) break;
+        const int r = st.run[i];
+        if (r != cur) {
+            if (cur >= 0) flush(cur);
+            cur = r;
+        }
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            const long long b = __double_as_longlong(st.f[F_POS + k][i]);
+            if ((b & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL) continue;   // NaN: left out, as fmin/fmax do
+            const long long o = b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
+            lo[k] = o < lo[k] ? o : lo[k];
+            hi[k] = o > hi[k] ? o : hi[k];
+        }
+    }
+    // lanes that end in the same run combine before the atomics
+    const unsigned same = __match_any_sync(FULL, cur);
+    if (same == FULL) {
+        if (cur < 0) return;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            for (int o = 16; o > 0; o >>= 1) {
+                const long long a = __shfl_xor_sync(FULL, lo[k], o), b = __shfl_xor_sync(FULL, hi[k], o);
+                lo[k] = a < lo[k] ? a : lo[k];
+                hi[k] = b > hi[k] ? b : hi[k];
+            }
+        }
+        if (lane == 0) flush(cur);
+    } else if (cur >= 0) {
+        flush(cur);
     }
 }
 
@@ -1474,7 +1504,7 @@ static void make_tree_d(Ctx& c, bool reorder_all, bool full_depth)
     TreeView tv = tree_view(c);
     if (!c.pb.on) {
         bbox_init_kernel<<<ceil_div(R * D, 128), 128, 0, s>>>(c.bbox, R, D);
-        bbox_kernel<D><<<ceil_div(n, 256), 256, 0, s>>>(c.st, n, c.bbox);
+        bbox_kernel<D><<<std::max(1, ceil_div(n, 256 * BBOX_ROWS)), 256, 0, s>>>(c.st, n, c.bbox);
     }
     roots_kernel<D><<<ceil_div(R, 128), 128, 0, s>>>(
         tv, c.nd_center[0], c.nd_center[1], c.nd_center[2], c.nd_edge, c.nd_begin, c.nd_count,
