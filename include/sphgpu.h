@@ -254,7 +254,9 @@ const char* sphgpu_last_error(const sphgpu_ctx* ctx);
  * 34 key table: 0 off, 1 from 2^18 particles on (default), 2 always (reads 0 when a batch has too
  * many runs for its 64 MB): the first eight levels of each run's octree-centre recursion replayed
  * once per tree build into a table that the key computation searches with integer comparisons
- * (the same keys, fewer FP64 additions). */
+ * (the same keys, fewer FP64 additions);
+ * 35 gravity work items: 1 fixed 32-particle chunks of each run's key order, one warp each
+ * (default), 0 the pair kernels' target groups in pieces of 32 (partly filled warps). */
 int sphgpu_set_tuning(sphgpu_ctx* ctx, int which, int value);
 int sphgpu_get_tuning(sphgpu_ctx* ctx, int which, int* value);
 

@@ -292,7 +292,7 @@ void free_ctx(Ctx& c)
     free_state(c.alt, false);
     void* ptrs[] = {c.d_run_begin, c.d_time, c.d_dt, c.d_hvs, c.d_dtmin, c.d_emin, c.d_sums, c.d_err,
                     c.d_newton_fail, c.d_work, c.d_counters, c.d_ovf_list, c.d_ovf_list2, c.d_stage, c.d_aos, c.d_flush,
-                    c.adj_buf, c.adj_mir, c.adj_partials};
+                    c.adj_buf, c.adj_mir, c.adj_partials, c.d_gchunk_begin, c.d_gchunk_count, c.d_gchunk_n};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (void* p : c.mir)
@@ -426,6 +426,23 @@ int create_impl(const sphgpu_params* params, int dim, int n_runs, const int* run
         if (e != cudaSuccess) rc = cuda_status(c, e, "create");
     }
     if (rc == SPHGPU_OK) rc = build_groups(c);
+    if (rc == SPHGPU_OK && c.p.use_gravity) {
+        // gravity work items: consecutive 32-particle chunks of every run (key order), knob 35
+        std::vector<int> gb, gc;
+        for (int r = 0; r < c.R; ++r)
+            for (int b = c.run_begin[r]; b < c.run_begin[r + 1]; b += 32) {
+                gb.push_back(b);
+                gc.push_back(std::min(32, c.run_begin[r + 1] - b));
+            }
+        const int ng = (int)gb.size();
+        cudaError_t e = cudaMalloc((void**)&c.d_gchunk_begin, sizeof(int) * std::max(ng, 1));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&c.d_gchunk_count, sizeof(int) * std::max(ng, 1));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&c.d_gchunk_n, sizeof(int));
+        if (e == cudaSuccess) e = cudaMemcpy(c.d_gchunk_begin, gb.data(), sizeof(int) * ng, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(c.d_gchunk_count, gc.data(), sizeof(int) * ng, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(c.d_gchunk_n, &ng, sizeof(int), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) rc = cuda_status(c, e, "create");
+    }
     if (rc == SPHGPU_OK) {
         cudaMemcpy(c.d_run_begin, c.run_begin.data(), sizeof(int) * (c.R + 1), cudaMemcpyHostToDevice);
         cudaMemset(c.d_time, 0, sizeof(double) * c.R);
@@ -1314,6 +1331,10 @@ int sphgpu_set_tuning(sphgpu_ctx* h, int which, int value)
     case 29: c.bulk_stage = value != 0; break;
     case 32: c.fused_levels = value != 0; c.tree_valid = false; break;
     case 33: c.inject_barrier_timeout = value != 0; break;
+    case 35:
+        if (value < 0 || value > 1) return SPHGPU_ERR_ARG;
+        c.gravity_items = value;
+        break;
     case 34:
         if (value < 0 || value > 2) return SPHGPU_ERR_ARG;
         c.key_table_on = value;
@@ -1373,6 +1394,7 @@ int sphgpu_get_tuning(sphgpu_ctx* h, int which, int* value)
     case 32: *value = c.fused_levels; break;
     case 33: *value = c.inject_barrier_timeout; break;
     case 34: *value = c.key_table ? c.key_table_on : 0; break;
+    case 35: *value = c.gravity_items; break;
     case 13: case 14: case 15: case 16: case 17: {
         cudaStreamSynchronize(c.stream);
         cudaMemcpy(value, c.d_work + sphgpu::FAIL_INFO_SLOT + (which - 13), sizeof(int), cudaMemcpyDeviceToHost);

@@ -169,6 +169,13 @@ struct Ctx {
     int fused_levels = 1;
     // inside run_step: predict leaves the sound speed to the mirror kernels of Pre and Fluid
     bool sound_from_ene = false;
+    // gravity work items (knob 35): 0 the pair kernels' target groups in 32-target pieces, 1 fixed
+    // 32-particle chunks of each run's key order (every lane of a warp holds a target; default,
+    // Evrard 2^20 gravity about 10 % faster than over the groups' partly filled pieces)
+    int gravity_items = 1;
+    int* d_gchunk_begin = nullptr;
+    int* d_gchunk_count = nullptr;
+    int* d_gchunk_n = nullptr;
     int inject_barrier_timeout = 0; // knob 33: the next fused level build's block 0 leaves early (tests)
     GroupPlan* plan = nullptr;
     int plan_cap = 0;

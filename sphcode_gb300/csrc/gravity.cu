@@ -316,9 +316,15 @@ void run_gravity(Ctx& c)
     // deepest stack: 2^D - 1 siblings waiting per level below the root, plus one node's children
     a.stack_cap = 256;
     a.counters = c.count_work ? c.d_counters : nullptr;
-    a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 0, nullptr, nullptr, 0, nullptr,
-                       nullptr, 0, 0, c.d_err, nullptr};
-    a.work.pieces = c.group_threads / 32;
+    if (c.gravity_items == 1 && c.d_gchunk_begin) {
+        a.work = GroupWork{c.d_gchunk_begin, c.d_gchunk_count, c.d_gchunk_n, c.d_work + 0, nullptr, nullptr, 0,
+                           nullptr, nullptr, 0, 0, c.d_err, nullptr};
+        a.work.pieces = 1;
+    } else {
+        a.work = GroupWork{c.g_begin, c.g_count, c.n_groups, c.d_work + 0, nullptr, nullptr, 0, nullptr,
+                           nullptr, 0, 0, c.d_err, nullptr};
+        a.work.pieces = c.group_threads / 32;
+    }
     const int gt = 128;   // four independent warps per block
     const size_t smem = sizeof(int2) * (size_t)a.stack_cap * (gt / 32);
     auto kern = a.counters ? gravity_kernel<D, T, true> : gravity_kernel<D, T, false>;

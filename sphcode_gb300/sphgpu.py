@@ -35,7 +35,7 @@ TUNING = {"group_warps": 0, "fluid_warps": 1, "gravity_warps": 2, "tile_cap": 3,
           "tree_levels": 20, "depth_cap": 21, "tile_limit": 22, "node_limit": 23,
           "tune_fail_mask": 24, "count_work": 25, "leaf_cap1": 27, "pair_sched": 28, "bulk_stage": 29,
           "group_rule": 30, "prewalk": 31, "fused_levels": 32,
-          "inject_barrier_timeout": 33, "key_table": 34}
+          "inject_barrier_timeout": 33, "key_table": 34, "gravity_items": 35}
 
 
 class SphGpuError(RuntimeError):

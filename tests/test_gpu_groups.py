@@ -50,12 +50,13 @@ def test_batch_groups_stay_in_their_run(gpu_lib):
         assert np.bincount(g).max() <= 128
 
 
-@pytest.mark.parametrize("knob", [("group_rule", 0), ("prewalk", 1), ("prewalk", 3)])
+@pytest.mark.parametrize("knob", [("group_rule", 0), ("prewalk", 1), ("prewalk", 3), ("gravity_items", 0)])
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
 @pytest.mark.parametrize("case", ["khi_disph_ac_2d", "evrard_disph_grav_3d"])
 def test_alternative_group_setups_parity(gpu_lib, case, prec, knob):
-    """The former group rule (fixed chunks split once) and the group plans (a walk kernel ahead of
-    the first pass, for FluidForce or both stages) stay selectable and match the oracle."""
+    """The former group rule (fixed chunks split once), the group plans (a walk kernel ahead of
+    the first pass, for FluidForce or both stages) and the gravity walk over the pair groups' pieces
+    instead of fixed 32-particle chunks stay selectable and match the oracle."""
     from oracle import pyoracle
     from sphcode_gb300 import sphgpu
     from test_gpu_parity import FP32_TOL, FP64_TOL, _fields
