@@ -113,8 +113,13 @@ struct AosMap {
     long off_nb;
     size_t stride;
     int nf;
+    int nw;           // 8-byte words of the FP64 members (at most 24)
+    int woff[32];     // each word's byte offset in the record
+    int wslot[32];    // each word's field slot
 };
 
+// AoS -> SoA: a thread per particle reads its record's members (the record's lines are shared
+// through L1 by its loads) and stores them into the fields, coalesced across the warp.
 __global__ void aos_upload_kernel(State st, AosMap m, const unsigned char* aos, int n)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -127,16 +132,27 @@ __global__ void aos_upload_kernel(State st, AosMap m, const unsigned char* aos, 
     if (m.off_nb >= 0) st.neighbor[i] = *reinterpret_cast<const int*>(rec + m.off_nb);
 }
 
+// SoA -> AoS: a warp takes 32 consecutive particles (key order) and writes one record at a time,
+// lane l carrying word l, so each record is written as one contiguous piece instead of as 8-byte
+// pieces of 32 records per store (partial sectors); each lane's field reads run over consecutive
+// particles and are served by L1 between records.  (The same organisation for the upload was
+// slower: there it scatters the field stores instead.)
 __global__ void aos_download_kernel(State st, AosMap m, unsigned char* aos, int n)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    unsigned char* rec = aos + (size_t)st.id[i] * m.stride;
-    for (int q = 0; q < m.nf; ++q) {
-        double* dst = reinterpret_cast<double*>(rec + m.off[q]);
-        for (int k = 0; k < m.width[q]; ++k) dst[k] = st.f[m.slot[q] + k][i];
+    const int lane = threadIdx.x & 31;
+    const int i0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
+    if (i0 >= n) return;
+    const bool mine = lane < m.nw;
+    const double* const fp = mine ? st.f[m.wslot[lane]] : nullptr;
+    const int wo = mine ? m.woff[lane] : 0;
+    const int myid = i0 + lane < n ? st.id[i0 + lane] : 0;
+    const int cnt = min(32, n - i0);
+    for (int r = 0; r < cnt; ++r) {
+        const int id = __shfl_sync(FULL, myid, r);
+        unsigned char* rec = aos + (size_t)id * m.stride;
+        if (mine) *reinterpret_cast<double*>(rec + wo) = fp[i0 + r];
+        if (lane == 31 && m.off_nb >= 0) *reinterpret_cast<int*>(rec + m.off_nb) = st.neighbor[i0 + r];
     }
-    if (m.off_nb >= 0) *reinterpret_cast<int*>(rec + m.off_nb) = st.neighbor[i];
 }
 
 __global__ void nonfinite_kernel(State st, int n, int dim, unsigned* err)
@@ -225,14 +241,26 @@ int cuda_status(Ctx& c, cudaError_t e, const char* what)
 }
 
 // Synchronise the stream and fold launch errors and the device status word into a status.
+// A data movement with no kernel that raises status bits: the launch status and the stream's
+// completion only (the status word is read by the calls whose kernels can set it).
+int finish_sync(Ctx& c, const char* what)
+{
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+    return e == cudaSuccess ? SPHGPU_OK : cuda_status(c, e, what);
+}
+
 int finish(Ctx& c, const char* what)
 {
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
     if (e != cudaSuccess) return cuda_status(c, e, what);
-    unsigned bits = 0;
-    e = cudaMemcpy(&bits, c.d_err, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    // the status bits and the capped-tree flag in one read
+    unsigned words[2] = {0u, 0u};
+    e = cudaMemcpy(words, c.d_err, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_status(c, e, what);
+    const unsigned bits = words[0];
+    c.last_trunc = words[1];
     if (bits) {
         cudaMemsetAsync(c.d_err, 0, sizeof(unsigned), c.stream);
         cudaStreamSynchronize(c.stream);
@@ -402,7 +430,7 @@ int create_impl(const sphgpu_params* params, int dim, int n_runs, const int* run
         A((void**)&c.d_dtmin, sizeof(long long) * R);
         A((void**)&c.d_emin, sizeof(int) * R);
         A((void**)&c.d_sums, sizeof(double) * (R * maxc * 7 + R * 7));
-        A((void**)&c.d_err, sizeof(unsigned));
+        A((void**)&c.d_err, 2 * sizeof(unsigned));   // status bits, capped-tree flag
         A((void**)&c.d_newton_fail, sizeof(int));
         A((void**)&c.d_work, sizeof(int) * 64);
         A((void**)&c.d_counters, sizeof(unsigned long long) * PAIR_COUNTERS);
@@ -447,7 +475,7 @@ int create_impl(const sphgpu_params* params, int dim, int n_runs, const int* run
         cudaMemcpy(c.d_run_begin, c.run_begin.data(), sizeof(int) * (c.R + 1), cudaMemcpyHostToDevice);
         cudaMemset(c.d_time, 0, sizeof(double) * c.R);
         cudaMemset(c.d_dt, 0, sizeof(double) * c.R);
-        cudaMemset(c.d_err, 0, sizeof(unsigned));
+        cudaMemset(c.d_err, 0, 2 * sizeof(unsigned));
         cudaMemset(c.d_newton_fail, 0, sizeof(int));
         cudaMemset(c.d_work, 0, sizeof(int) * 64);
         cudaMemset(c.d_counters, 0, sizeof(unsigned long long) * PAIR_COUNTERS);
@@ -687,11 +715,10 @@ void reset_work_counters(Ctx& c) { cudaMemsetAsync(c.d_work, 0, sizeof(int) * 48
 void check_tree_cap(Ctx& c)
 {
     if (c.p.use_gravity || c.depth_cap <= 0) return;
-    int t = 0;
-    cudaMemcpyAsync(&t, c.d_work + TREE_TRUNC_SLOT, sizeof(int), cudaMemcpyDeviceToHost, c.stream);
-    cudaStreamSynchronize(c.stream);
-    if (!t) return;
-    cudaMemsetAsync(c.d_work + TREE_TRUNC_SLOT, 0, sizeof(int), c.stream);
+    // the flag came with the status bits of the call's finish
+    if (!c.last_trunc) return;
+    c.last_trunc = 0;
+    cudaMemsetAsync(trunc_flag(c), 0, sizeof(int), c.stream);
     cudaStreamSynchronize(c.stream);
     c.depth_cap = std::min(c.key_levels, c.tree_levels + 4);
     ++c.graph_epoch;
@@ -749,6 +776,13 @@ AosMap aos_map(const Ctx& c, const sphgpu_aos_layout* layout)
     }
     m.off_nb = layout->neighbor;
     m.stride = layout->stride;
+    m.nw = 0;
+    for (int q = 0; q < m.nf; ++q)
+        for (int k = 0; k < m.width[q]; ++k) {
+            m.woff[m.nw] = (int)(m.off[q] + 8 * k);
+            m.wslot[m.nw] = m.slot[q] + k;
+            ++m.nw;
+        }
     return m;
 }
 
@@ -847,7 +881,7 @@ int sphgpu_upload_aos(sphgpu_ctx* h, const void* base, const sphgpu_aos_layout* 
     sphgpu::aos_upload_kernel<<<sphgpu::ceil_div(c.n, 256), 256, 0, c.stream>>>(c.st, m, c.d_aos, c.n);
     c.tree_valid = false;
     c.kernel_size_valid = false;
-    return sphgpu::finish(c, "upload_aos");
+    return sphgpu::finish_sync(c, "upload_aos");
 }
 
 int sphgpu_download_aos(sphgpu_ctx* h, void* base, const sphgpu_aos_layout* layout)
@@ -865,7 +899,7 @@ int sphgpu_download_aos(sphgpu_ctx* h, void* base, const sphgpu_aos_layout* layo
     c.aos_stage_stride = layout->stride;
     sphgpu::aos_download_kernel<<<sphgpu::ceil_div(c.n, 256), 256, 0, c.stream>>>(c.st, m, c.d_aos, c.n);
     cudaMemcpyAsync(base, c.d_aos, bytes, cudaMemcpyDeviceToHost, c.stream);
-    return sphgpu::finish(c, "download_aos");
+    return sphgpu::finish_sync(c, "download_aos");
 }
 
 int sphgpu_set_scalar(sphgpu_ctx* h, int which, int run, double value)
@@ -963,7 +997,7 @@ int sphgpu_initialize(sphgpu_ctx* h)
 {
     CTX_OR_FAIL(h);
     sphgpu::launch_init_fields(c);
-    cudaMemsetAsync(c.d_work + sphgpu::TREE_TRUNC_SLOT, 0, sizeof(int), c.stream);
+    cudaMemsetAsync(sphgpu::trunc_flag(c), 0, sizeof(int), c.stream);
     sphgpu::launch_make_tree(c, true, true);
     c.first_pre = true;
     if (c.autotune && !c.tuned) {

@@ -143,8 +143,9 @@ struct Ctx {
     // octree levels split in a step's tree build (0: all key levels).  Without gravity the tree
     // only serves the neighbour walks, whose sets do not depend on where the splitting stops;
     // sphgpu_initialize sets it two levels below the initial tree's depth, and a build that had
-    // to stop splitting early raises it (TREE_TRUNC_SLOT).
+    // to stop splitting early raises it (trunc_flag).
     int depth_cap = 0;
+    unsigned last_trunc = 0;        // capped-tree flag read by the last finish()
     int tree_levels = 0;            // split levels of the last build
     // capacity limits below the allocated ones (0: none), for callers that bound the work of a
     // stage and for tests of the capacity statuses: the source tile of every pair pass (knob 22)
@@ -202,6 +203,7 @@ void launch_node_moments(Ctx& c);
 TreeView tree_view(const Ctx& c);
 void launch_reorder_fields(Ctx& c, bool all);
 void step_reorder_swap(Ctx& c);
+inline int* trunc_flag(const Ctx& c) { return reinterpret_cast<int*>(c.d_err + 1); }
 inline bool step_graph_ready(const Ctx& c, int p) { return c.graph[p] && c.graph_epoch_of[p] == c.graph_epoch; }
 int build_groups(Ctx& c);          // host: fixed chunks per run, uploaded to the device
 
@@ -290,7 +292,7 @@ void launch_plans(const void* kern, Ctx& c, size_t per_warp, F launch)
     launch(nb * c.num_sms, smem);
 }
 constexpr int FAIL_INFO_SLOT = 48;   // d_work[48..52]: the last failing range
-constexpr int TREE_TRUNC_SLOT = 60;  // d_work[60]: a capped tree build left a splittable node
+// d_err[1]: a capped tree build left a splittable node (read together with the status bits)
 constexpr int GRID_BAR_SLOT = 61;    // d_work[61..62]: grid barrier of the fused level build (count, generation)
 template <class Args>
 void launch_pair_passes(Ctx& c, const void* kern, Args& a, int tcap, int elt4, int eltT,

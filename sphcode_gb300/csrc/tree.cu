@@ -1574,7 +1574,7 @@ static void make_tree_d(Ctx& c, bool reorder_all, bool full_depth)
             const unsigned long long* a_keys = c.keys;
             int a_n = n, a_levels = levels, a_lv = lv, a_leaf = c.p.leaf_num, a_cs_cap = cs_cap, a_pool = pool;
             int* a_lvl = c.lvl_start;
-            int* a_tr = c.d_work + TREE_TRUNC_SLOT;
+            int* a_tr = trunc_flag(c);
             unsigned* a_err = c.d_err;
             unsigned* a_bar = reinterpret_cast<unsigned*>(c.d_work + GRID_BAR_SLOT);
             int a_inject = c.inject_barrier_timeout;
@@ -1584,13 +1584,13 @@ static void make_tree_d(Ctx& c, bool reorder_all, bool full_depth)
             cudaLaunchCooperativeKernel((const void*)levels_fused_kernel<D>, dim3(fgrid), dim3(LEVEL_CHUNK), args, 0, s);
         } else {
         level_count_kernel<D><<<cgrid, COUNT_THREADS, 0, s>>>(na, c.keys, n, c.lvl_start, 1, levels, lv,
-                                                             c.p.leaf_num, tmp[1], cs[1], c.d_work + TREE_TRUNC_SLOT);
+                                                             c.p.leaf_num, tmp[1], cs[1], trunc_flag(c));
         for (int l = 1; l <= lv; ++l) {
             level_build_kernel<D><<<grid, LEVEL_CHUNK, 0, s>>>(na, c.lvl_start, l, tmp[l & 1], cs[l % 3],
                                                              cs[(l + 2) % 3], cs_cap, pool, c.d_err);
             level_count_kernel<D><<<cgrid, COUNT_THREADS, 0, s>>>(na, c.keys, n, c.lvl_start, l + 1, levels, lv,
                                                                  c.p.leaf_num, tmp[(l + 1) & 1], cs[(l + 1) % 3],
-                                                                 c.d_work + TREE_TRUNC_SLOT);
+                                                                 trunc_flag(c));
         }
         }
     }
