@@ -65,6 +65,7 @@ struct Ctx {
     int* ck_count = nullptr;
     int num_chunks = 0;
     int *part_begin = nullptr, *part_count = nullptr, *part_n = nullptr;   // split scratch
+    int* scan_tiles = nullptr;      // tile totals of the two-launch scan of part_n
     unsigned char* g_flag = nullptr;   // key-block groups: group-start flag per particle
     // group formation (knob 30): 1 the largest aligned key blocks of at most group_threads
     // particles (default in 2D and 3D), 0 fixed chunks of group_threads particles, each split once

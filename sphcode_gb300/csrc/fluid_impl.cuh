@@ -16,6 +16,16 @@
 
 namespace sphgpu {
 
+// Per-particle gradient record of the second-order Godunov form (T): d rho/dx_k at d(k), dP/dx_k
+// at p(k), dv_k/dx_d at v(k, d), padded to a multiple of four entries (1D: 4, 2D: 8, 3D: 16).
+template <int D>
+struct GradLayout {
+    static constexpr int stride = D == 1 ? 4 : D == 2 ? 8 : 16;
+    __host__ __device__ static constexpr int d(int k) { return k; }
+    __host__ __device__ static constexpr int p(int k) { return D + k; }
+    __host__ __device__ static constexpr int v(int k, int dd) { return 2 * D + D * k + dd; }
+};
+
 template <typename T>
 struct FluidArgs {
     using V4 = typename Vec4<T>::type;
@@ -93,10 +103,10 @@ __device__ __forceinline__ void fluid_target(const FluidArgs<T>& a, int i, int r
         const T dt = (T)a.dt_run[run];
         const T gamma = (T)a.gamma;
         const T alpha_ac = (T)a.alpha_ac;
-        T gi[16];
+        T gi[GradLayout<D>::stride];
         if (TYPE == 2 && a.gsph_2nd) {
 #pragma unroll
-            for (int q = 0; q < 16; ++q) gi[q] = a.grad[(size_t)i * 16 + q];
+            for (int q = 0; q < GradLayout<D>::stride; ++q) gi[q] = a.grad[(size_t)i * GradLayout<D>::stride + q];
         }
 
         Sum<T> acc[D], dene;
@@ -127,7 +137,7 @@ __device__ __forceinline__ void fluid_target(const FluidArgs<T>& a, int i, int r
                     for (int k = 0; k < D; ++k) { ve_i += vi[k] * e[k]; ve_j += vj[k] * e[k]; }
                     T left[4], right[4];
                     if (a.gsph_2nd) {
-                        const T* gj = a.grad + (size_t)j * 16;
+                        const T* gj = a.grad + (size_t)j * GradLayout<D>::stride;
                         const T delta_i = T(0.5) * (T(1) - c_i * dt * r_inv);
                         const T delta_j = T(0.5) * (T(1) - c_j * dt * r_inv);
                         // velocity: e . (grad v) . e * r
@@ -136,7 +146,10 @@ __device__ __forceinline__ void fluid_target(const FluidArgs<T>& a, int i, int r
                         for (int k = 0; k < D; ++k) {
                             T si = T(0), sj = T(0);
 #pragma unroll
-                            for (int d = 0; d < D; ++d) { si += gi[6 + 3 * k + d] * e[d]; sj += gj[6 + 3 * k + d] * e[d]; }
+                            for (int d = 0; d < D; ++d) {
+                                si += gi[GradLayout<D>::v(k, d)] * e[d];
+                                sj += gj[GradLayout<D>::v(k, d)] * e[d];
+                            }
                             dve_i += si * e[k];
                             dve_j += sj * e[k];
                         }
@@ -148,8 +161,8 @@ __device__ __forceinline__ void fluid_target(const FluidArgs<T>& a, int i, int r
                         T ddi = T(0), ddj = T(0), dpi = T(0), dpj = T(0);
 #pragma unroll
                         for (int k = 0; k < D; ++k) {
-                            ddi += gi[k] * e[k]; ddj += gj[k] * e[k];
-                            dpi += gi[3 + k] * e[k]; dpj += gj[3 + k] * e[k];
+                            ddi += gi[GradLayout<D>::d(k)] * e[k]; ddj += gj[GradLayout<D>::d(k)] * e[k];
+                            dpi += gi[GradLayout<D>::p(k)] * e[k]; dpj += gj[GradLayout<D>::p(k)] * e[k];
                         }
                         ddi *= r; ddj *= r; dpi *= r; dpj *= r;
                         const T dd_ij = rho_i - rho_j, dp_ij = p_i - p_j;
@@ -517,16 +530,19 @@ __global__ void fluid_mirror_kernel(State st, int n, typename Vec4<T>::type* rec
     rec1[i] = b;
     rec2[i] = c;
     if (TYPE == 2 && gsph_2nd) {
-        T* g = grad + (size_t)i * 16;
+        T* g = grad + (size_t)i * GradLayout<D>::stride;
+        T v[GradLayout<D>::stride];
 #pragma unroll
-        for (int q = 0; q < 16; ++q) g[q] = T(0);
+        for (int q = 0; q < GradLayout<D>::stride; ++q) v[q] = T(0);
 #pragma unroll
         for (int k = 0; k < D; ++k) {
-            g[k] = (T)st.f[F_GRADD + k][i];
-            g[3 + k] = (T)st.f[F_GRADP + k][i];
+            v[GradLayout<D>::d(k)] = (T)st.f[F_GRADD + k][i];
+            v[GradLayout<D>::p(k)] = (T)st.f[F_GRADP + k][i];
 #pragma unroll
-            for (int d = 0; d < D; ++d) g[6 + 3 * k + d] = (T)st.f[F_GRADV + 3 * k + d][i];
+            for (int d = 0; d < D; ++d) v[GradLayout<D>::v(k, d)] = (T)st.f[F_GRADV + 3 * k + d][i];
         }
+#pragma unroll
+        for (int q = 0; q < GradLayout<D>::stride; ++q) g[q] = v[q];
     }
 }
 

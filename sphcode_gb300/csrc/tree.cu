@@ -1145,6 +1145,65 @@ __global__ void split_groups_kernel(State st, const unsigned long long* keys, co
 }
 
 // Exclusive scan of the per-chunk part counts in one block; total to *n_groups.
+// Exclusive scan of many counts in two launches: tiles of SCAN_TILE counts scanned by one block
+// each (coalesced, four per thread), the tile totals kept; then every block adds the sum of the
+// totals before its tile, and the last block writes the grand total.  The single-block scan
+// below reads thread-contiguous runs (uncoalesced) and took 0.33 ms for 330,000 counts.
+constexpr int SCAN_TILE = 4096;
+__global__ void __launch_bounds__(1024) scan_tiles_kernel(int* v, int n, int* tile_sum)
+{
+    __shared__ int wsum[32];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int base = blockIdx.x * SCAN_TILE + 4 * t;
+    int x[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) x[k] = base + k < n ? v[base + k] : 0;
+    const int own = x[0] + x[1] + x[2] + x[3];
+    int incl = own;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) wsum[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        int s = wsum[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(FULL, s, o);
+            if (lane >= o) s += y;
+        }
+        wsum[lane] = s;
+    }
+    __syncthreads();
+    int run = incl - own + (w > 0 ? wsum[w - 1] : 0);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (base + k < n) v[base + k] = run;
+        run += x[k];
+    }
+    if (t == 1023) tile_sum[blockIdx.x] = wsum[31];
+}
+
+__global__ void __launch_bounds__(1024) scan_add_kernel(int* v, int n, const int* tile_sum, int ntiles, int* total)
+{
+    __shared__ int red[32];
+    const int t = threadIdx.x;
+    int s = 0;
+    for (int q = t; q < (int)blockIdx.x; q += blockDim.x) s += tile_sum[q];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
+    if ((t & 31) == 0) red[t >> 5] = s;
+    __syncthreads();
+    int off = 0;
+    for (int q = 0; q < 32; ++q) off += red[q];
+    const int base = blockIdx.x * SCAN_TILE + 4 * t;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (base + k < n) v[base + k] += off;
+    if (blockIdx.x == ntiles - 1 && t == 0) *total = off + tile_sum[ntiles - 1];
+}
+
 __global__ void scan_parts_kernel(int* nparts, int nchunks, int* n_groups)
 {
     __shared__ int part[1024];
@@ -1413,6 +1472,7 @@ int tree_alloc(Ctx& c)
     A((void**)&c.part_begin, sizeof(int) * GROUP_PARTS * (size_t)max_chunks);
     A((void**)&c.part_count, sizeof(int) * GROUP_PARTS * (size_t)max_chunks);
     A((void**)&c.part_n, sizeof(int) * max_chunks);   // also the block counts of the key-block flags
+    A((void**)&c.scan_tiles, sizeof(int) * (max_chunks / SCAN_TILE + 2));
     A((void**)&c.g_flag, sizeof(unsigned char) * ((size_t)n + 1));
     // group plans of the first pair pass: plans for the first plan_cap groups, their leaves in a
     // pool (groups beyond either walk in the pair kernel)
@@ -1438,7 +1498,7 @@ void tree_free(Ctx& c)
                     c.nd_edge, c.nd_mass, c.nd_ksize, c.lvl_start, c.lvl_tmp, c.chunk_sum, c.bbox,
                     c.node_total, c.g_begin, c.g_count, c.n_groups, c.nd_cf[0], c.nd_cf[1],
                     c.nd_cf[2], c.nd_ef, c.nd_kf, c.ck_begin, c.ck_count, c.radix_dtot, c.nd_grav, c.nd_bnd, c.part_begin,
-                    c.part_count, c.part_n, c.g_flag, c.plan, c.pool_leaves, c.pool_loff};
+                    c.part_count, c.part_n, c.scan_tiles, c.g_flag, c.plan, c.pool_leaves, c.pool_loff};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -1600,14 +1660,26 @@ static void make_tree_d(Ctx& c, bool reorder_all, bool full_depth)
         // key-block groups of at most group_threads particles
         const int nblk = ceil_div(n, GF_THREADS);
         group_flags_kernel<<<nblk, GF_THREADS, 0, s>>>(c.keys, c.st.run, n, c.group_threads, c.g_flag, c.part_n);
-        scan_parts_kernel<<<1, 1024, 0, s>>>(c.part_n, nblk, c.n_groups);
+        if (nblk <= 16384) {
+            scan_parts_kernel<<<1, 1024, 0, s>>>(c.part_n, nblk, c.n_groups);
+        } else {
+            const int nt = ceil_div(nblk, SCAN_TILE);
+            scan_tiles_kernel<<<nt, 1024, 0, s>>>(c.part_n, nblk, c.scan_tiles);
+            scan_add_kernel<<<nt, 1024, 0, s>>>(c.part_n, nblk, c.scan_tiles, nt, c.n_groups);
+        }
         group_write_kernel<<<nblk, GF_THREADS, 0, s>>>(c.g_flag, c.part_n, n, c.group_threads, c.g_begin, c.g_count);
     } else {
         // fixed chunks, each split once where it straddles two distant cells
         split_groups_kernel<D><<<ceil_div(c.num_chunks, 8), 256, 0, s>>>(c.st, c.keys, c.ck_begin, c.ck_count,
                                                                        c.num_chunks, c.part_begin, c.part_count,
                                                                        c.part_n);
-        scan_parts_kernel<<<1, 1024, 0, s>>>(c.part_n, c.num_chunks, c.n_groups);
+        if (c.num_chunks <= 16384) {
+            scan_parts_kernel<<<1, 1024, 0, s>>>(c.part_n, c.num_chunks, c.n_groups);
+        } else {
+            const int nt = ceil_div(c.num_chunks, SCAN_TILE);
+            scan_tiles_kernel<<<nt, 1024, 0, s>>>(c.part_n, c.num_chunks, c.scan_tiles);
+            scan_add_kernel<<<nt, 1024, 0, s>>>(c.part_n, c.num_chunks, c.scan_tiles, nt, c.n_groups);
+        }
         compact_groups_kernel<<<ceil_div(c.num_chunks, 128), 128, 0, s>>>(c.part_begin, c.part_count, c.part_n,
                                                                          c.n_groups, c.num_chunks, c.g_begin,
                                                                          c.g_count);
