@@ -51,6 +51,7 @@ struct Ctx {
     int* lvl_tmp = nullptr;         // per-node child counts of the frontier
     int* nd_bnd = nullptr;          // per split node: its inner child boundaries (2^D - 1 ints)
     int* chunk_sum = nullptr;       // per-1024-node chunk sums
+    int* chunk_off = nullptr;       // their exclusive scan for one level (per-level launches)
     long long* bbox = nullptr;      // per run: D mins then D maxs (ordered-int images)
     int* node_total = nullptr;      // device: number of nodes built
 

@@ -724,7 +724,8 @@ struct NextCount {
 template <int D, bool COUNT>
 __device__ __forceinline__ void build_level(const NodeArrays& na, int* lvl_start, int l, const int* tmp_cur,
                                             const int* cs_cur, int* cs_clear, int cs_cap, int node_cap,
-                                            unsigned* err, int* sc, int* red, const NextCount& nx)
+                                            unsigned* err, int* sc, int* red, const NextCount& nx,
+                                            const int* cs_off = nullptr)
 {
     constexpr int NC = 1 << D;
     static_assert(LEVEL_CHUNK == 1024, "the chunk scan takes 32 warps of 32 nodes");
@@ -732,7 +733,10 @@ __device__ __forceinline__ void build_level(const NodeArrays& na, int* lvl_start
     const int nchunks = (e - s + LEVEL_CHUNK - 1) / LEVEL_CHUNK;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < cs_cap; q += gridDim.x * blockDim.x) cs_clear[q] = 0;
     // block sum of cs_cur[0, m)
+    // with cs_off (the chunk totals' exclusive scan, formed by chunk_offsets_kernel) one load;
+    // otherwise a block sum, which is O(chunks) per chunk and pays only for levels of few chunks
     auto prefix = [&](int m) {
+        if (cs_off) return __ldcg(cs_off + m);
         int v = 0;
         for (int q = threadIdx.x; q < m; q += blockDim.x) v += __ldcg(cs_cur + q);
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
@@ -840,11 +844,56 @@ template <int D>
 __global__ void __launch_bounds__(LEVEL_CHUNK) level_build_kernel(NodeArrays na, int* lvl_start, int l,
                                                                   const int* tmp_cur, const int* cs_cur,
                                                                   int* cs_clear, int cs_cap, int node_cap,
-                                                                  unsigned* err)
+                                                                  unsigned* err, const int* cs_off)
 {
     __shared__ int sc[34];
     __shared__ int red[32];
-    build_level<D, false>(na, lvl_start, l, tmp_cur, cs_cur, cs_clear, cs_cap, node_cap, err, sc, red, NextCount{});
+    build_level<D, false>(na, lvl_start, l, tmp_cur, cs_cur, cs_clear, cs_cap, node_cap, err, sc, red, NextCount{},
+                          cs_off);
+}
+
+// Exclusive scan of the chunk totals of level l (one block, tiles of 4096 with a carry), with the
+// level's total after the last chunk: the chunk offsets level_build_kernel reads.
+__global__ void __launch_bounds__(1024) chunk_offsets_kernel(const int* lvl_start, int l, const int* cs, int* off)
+{
+    __shared__ int wsum[32];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int nch = (lvl_start[l + 1] - lvl_start[l] + LEVEL_CHUNK - 1) / LEVEL_CHUNK;
+    int carry = 0;
+    for (int b0 = 0; b0 < nch; b0 += 4096) {
+        const int base = b0 + 4 * t;
+        int x[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) x[k] = base + k < nch ? __ldcg(cs + base + k) : 0;
+        const int own = x[0] + x[1] + x[2] + x[3];
+        int incl = own;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += y;
+        }
+        __syncthreads();   // the previous tile's readers of wsum are done
+        if (lane == 31) wsum[w] = incl;
+        __syncthreads();
+        if (w == 0) {
+            int v = wsum[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(FULL, v, o);
+                if (lane >= o) v += y;
+            }
+            wsum[lane] = v;
+        }
+        __syncthreads();
+        int run = carry + incl - own + (w > 0 ? wsum[w - 1] : 0);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (base + k < nch) off[base + k] = run;
+            run += x[k];
+        }
+        carry += wsum[31];
+    }
+    if (t == 0) off[nch] = carry;
 }
 
 // Bounded grid-wide barrier of a cooperative launch (all blocks resident): the last block to
@@ -1460,6 +1509,7 @@ int tree_alloc(Ctx& c)
     A((void**)&c.lvl_tmp, sizeof(int) * 2 * (size_t)nc);
     A((void**)&c.nd_bnd, sizeof(int) * ((1 << c.dim) - 1) * nc);
     A((void**)&c.chunk_sum, sizeof(int) * 3 * (size_t)(ceil_div(nc, LEVEL_CHUNK) + 1));
+    A((void**)&c.chunk_off, sizeof(int) * (size_t)(ceil_div(nc, LEVEL_CHUNK) + 2));
     A((void**)&c.bbox, sizeof(long long) * 2 * 3 * c.R);
     A((void**)&c.node_total, sizeof(int));
     const int max_chunks = n / 32 + c.R + 1;
@@ -1492,7 +1542,7 @@ int tree_alloc(Ctx& c)
 
 void tree_free(Ctx& c)
 {
-    void* ptrs[] = {c.keys, c.keys_alt, c.perm, c.perm_alt, c.radix_hist, c.key_table, c.nd_begin, c.nd_count,
+    void* ptrs[] = {c.keys, c.keys_alt, c.perm, c.perm_alt, c.radix_hist, c.key_table, c.chunk_off, c.nd_begin, c.nd_count,
                     c.nd_first, c.nd_nchild, c.nd_parent, c.nd_level, c.nd_arrive, c.nd_center[0],
                     c.nd_center[1], c.nd_center[2], c.nd_com[0], c.nd_com[1], c.nd_com[2],
                     c.nd_edge, c.nd_mass, c.nd_ksize, c.lvl_start, c.lvl_tmp, c.chunk_sum, c.bbox,
@@ -1645,9 +1695,14 @@ static void make_tree_d(Ctx& c, bool reorder_all, bool full_depth)
         } else {
         level_count_kernel<D><<<cgrid, COUNT_THREADS, 0, s>>>(na, c.keys, n, c.lvl_start, 1, levels, lv,
                                                              c.p.leaf_num, tmp[1], cs[1], trunc_flag(c));
+        // chunk offsets from one scan per level: the build's per-chunk block sums are O(chunks)
+        // each, which the levels of large 1D batches (thousands of chunks) pay quadratically
+        const bool offs = true;
         for (int l = 1; l <= lv; ++l) {
+            if (offs) chunk_offsets_kernel<<<1, 1024, 0, s>>>(c.lvl_start, l, cs[l % 3], c.chunk_off);
             level_build_kernel<D><<<grid, LEVEL_CHUNK, 0, s>>>(na, c.lvl_start, l, tmp[l & 1], cs[l % 3],
-                                                             cs[(l + 2) % 3], cs_cap, pool, c.d_err);
+                                                             cs[(l + 2) % 3], cs_cap, pool, c.d_err,
+                                                             offs ? c.chunk_off : nullptr);
             level_count_kernel<D><<<cgrid, COUNT_THREADS, 0, s>>>(na, c.keys, n, c.lvl_start, l + 1, levels, lv,
                                                                  c.p.leaf_num, tmp[(l + 1) & 1], cs[(l + 1) % 3],
                                                                  trunc_flag(c));
