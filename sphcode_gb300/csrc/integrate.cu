@@ -51,6 +51,48 @@ __device__ __forceinline__ DtEstimate dt_estimate(const State& st, int i)
     return d;
 }
 
+// Minimum of v over a block's particles into dst[run]: a warp whose lanes share one run reduces
+// by shuffles, the block's uniform warps of one run combine in shared memory and issue one atomic
+// (one per block instead of one per warp: the per-warp atomics on one address serialised and
+// took most of the kernels' time); lanes of warps that straddle runs add their own values.
+template <typename V>
+__device__ __forceinline__ void block_run_min(int r, V v, V* dst)
+{
+    __shared__ int s_run[THREADS / 32];
+    __shared__ V s_val[THREADS / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned same = __match_any_sync(FULL, r);
+    const bool uniform = same == FULL;
+    if (uniform) {
+        for (int o = 16; o > 0; o >>= 1) {
+            const V u = __shfl_xor_sync(FULL, v, o);
+            v = u < v ? u : v;
+        }
+    } else if (r >= 0) {
+        atomicMin(&dst[r], v);
+    }
+    if (lane == 0) {
+        s_run[w] = uniform ? r : -2;
+        s_val[w] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int nw = blockDim.x >> 5;
+        bool one = s_run[0] >= 0;
+        V m = s_val[0];
+        for (int q = 1; q < nw; ++q) {
+            one = one && s_run[q] == s_run[0];
+            m = s_val[q] < m ? s_val[q] : m;
+        }
+        if (one) {
+            atomicMin(&dst[s_run[0]], m);
+        } else {
+            for (int q = 0; q < nw; ++q)
+                if (s_run[q] >= 0) atomicMin(&dst[s_run[q]], s_val[q]);
+        }
+    }
+}
+
 template <int D>
 __global__ void timestep_estimate_kernel(State st, int n, int* emin)
 {
@@ -62,13 +104,7 @@ __global__ void timestep_estimate_kernel(State st, int n, int* emin)
         const DtEstimate d = dt_estimate<D>(st, i);
         if (!d.wide && d.e >= 0.0f) v = __float_as_int(d.e);   // NaN stays out
     }
-    const unsigned same = __match_any_sync(FULL, r);
-    if (same == FULL) {
-        for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(FULL, v, o));
-        if ((threadIdx.x & 31) == 0 && r >= 0) atomicMin(&emin[r], v);
-    } else if (r >= 0) {
-        atomicMin(&emin[r], v);
-    }
+    block_run_min<int>(r, v, emin);
 }
 
 template <int D>
@@ -89,13 +125,9 @@ __global__ void timestep_min_kernel(State st, int n, double cfl_force, const int
             if (a > 0.0) v = cfl_force * sqrt(st.f[F_SML][i] / a);
         }
     }
-    const unsigned same = __match_any_sync(FULL, r);
-    if (same == FULL) {
-        for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(FULL, v, o));
-        if ((threadIdx.x & 31) == 0 && r >= 0) atomicMin(&dtmin[r], dbl_to_ord(v));
-    } else if (r >= 0) {
-        atomicMin(&dtmin[r], dbl_to_ord(v));
-    }
+    // ordered-integer images: their minimum is the FP64 minimum (a NaN from the FP64 expression
+    // has a positive image above every finite value, as fmin would leave it out)
+    block_run_min<long long>(r, dbl_to_ord(v), dtmin);
 }
 
 // dt = min(cflSound * h_per_v_sig, dt_force); resets the minimum for the next call.
