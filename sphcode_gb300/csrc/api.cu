@@ -155,17 +155,24 @@ __global__ void aos_download_kernel(State st, AosMap m, unsigned char* aos, int 
     }
 }
 
+// A double is not finite when its exponent bits are all set: tested on the bits (integer pipe),
+// not with FP64 compares (1/64 of the FP32 rate, which bounded this kernel).
+__device__ __forceinline__ bool not_finite_bits(double x)
+{
+    return (__double_as_longlong(x) & 0x7ff0000000000000LL) == 0x7ff0000000000000LL;
+}
+
 __global__ void nonfinite_kernel(State st, int n, int dim, unsigned* err)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     bool bad = false;
     for (int k = 0; k < dim; ++k) {
-        bad |= !isfinite(st.f[F_POS + k][i]);
-        bad |= !isfinite(st.f[F_VEL + k][i]);
-        bad |= !isfinite(st.f[F_ACC + k][i]);
+        bad |= not_finite_bits(st.f[F_POS + k][i]);
+        bad |= not_finite_bits(st.f[F_VEL + k][i]);
+        bad |= not_finite_bits(st.f[F_ACC + k][i]);
     }
-    bad |= !isfinite(st.f[F_DENS][i]) || !isfinite(st.f[F_ENE][i]) || !isfinite(st.f[F_SML][i]);
+    bad |= not_finite_bits(st.f[F_DENS][i]) || not_finite_bits(st.f[F_ENE][i]) || not_finite_bits(st.f[F_SML][i]);
     if (bad) atomicOr(err, (unsigned)ERR_NOT_FINITE);
 }
 
@@ -405,6 +412,8 @@ int create_impl(const sphgpu_params* params, int dim, int n_runs, const int* run
         c.pb.lo[k] = params->range_min[k];
         c.pb.hi[k] = params->range_max[k];
         c.pb.len[k] = params->range_max[k] - params->range_min[k];
+        c.pb.lo_o[k] = sphgpu::host_dbl_to_ord(params->range_min[k] + 0.0);
+        c.pb.hi_o[k] = sphgpu::host_dbl_to_ord(params->range_max[k] + 0.0);
         c.pb.lenf[k] = (float)c.pb.len[k];
     }
     c.run_begin.assign(n_runs + 1, 0);

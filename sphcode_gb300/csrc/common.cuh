@@ -97,6 +97,7 @@ struct Periodic {
     int on;
     double lo[3], hi[3], len[3];
     float lenf[3];
+    long long lo_o[3], hi_o[3];   // ordered-integer images of lo and hi (for compares off the FP64 pipe)
 };
 
 // ------------------------------------------------------------------------------------------

@@ -158,8 +158,14 @@ __global__ void predict_kernel(State st, int n, const double* dt_run, double c_s
         st.f[F_VELP + k][i] = vp;
         double x = st.f[F_POS + k][i] + vp * dt;
         if (pb.on) {
-            if (x < pb.lo[k]) x += pb.len[k];
-            else if (x > pb.hi[k]) x -= pb.len[k];
+            // x < lo and x > hi on the ordered-integer images (the same outcomes, NaN and -0.0
+            // included, without two FP64 compares per axis)
+            long long xb = __double_as_longlong(x);
+            const bool nan = (xb & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+            if (xb == (long long)0x8000000000000000ULL) xb = 0;
+            const long long xo = xb >= 0 ? xb : (xb ^ 0x7fffffffffffffffLL);
+            if (!nan && xo < pb.lo_o[k]) x += pb.len[k];
+            else if (!nan && xo > pb.hi_o[k]) x -= pb.len[k];
         }
         st.f[F_POS + k][i] = x;
         st.f[F_VEL + k][i] = v + a * dt;
