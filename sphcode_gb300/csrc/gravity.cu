@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
                 gcc = gp->cc;
             }
             bool open = false;
-            float df[D];
+            float df[D] = {};
             if (in) {
                 T dT[D];
                 bool decided = false;
@@ -198,7 +198,84 @@ __global__ void __launch_bounds__(256) gravity_kernel(GravArgs<T> a)
             const unsigned om = __ballot_sync(FULL, open);
             if (!om) continue;
             const int fc = link.x;
-            if (fc < 0) {
+            if (fc < 0 && !exact_pairs && __popc(om) * link.w <= 32) {
+                // a leaf that few lanes open, transposed: lane q evaluates pair (t, j) = (q / cnt,
+                // b + q % cnt) for the t-th opening lane, the pairs of one target are summed by a
+                // segmented shuffle reduction, and each opening lane adds its leaf sum to its
+                // compensated totals (cnt iterations with a few active lanes become one with all)
+                const int b = link.z, cnt = link.w;
+                const int kopen = __popc(om);
+                if (COUNT && open) n_pair += (unsigned)cnt;
+                T base[D];
+                {
+                    const float cc[3] = {gcc.x, gcc.y, gcc.z};
+#pragma unroll
+                    for (int k = 0; k < D; ++k) base[k] = (T)min_image_f(df[k] - cc[k], a.pb, k);
+                }
+                const bool pv = lane < kopen * cnt;
+                const int t = pv ? lane / cnt : 0;
+                unsigned mm = om;
+                for (int z = 0; z < t; ++z) mm &= mm - 1;
+                const int src = pv ? __ffs(mm) - 1 : 0;
+                T bt[D];
+#pragma unroll
+                for (int k = 0; k < D; ++k) bt[k] = __shfl_sync(FULL, base[k], src);
+                const T hit = __shfl_sync(FULL, hiT, src);
+                T pphi = T(0), pacc[D];
+#pragma unroll
+                for (int k = 0; k < D; ++k) pacc[k] = T(0);
+                if (pv) {
+                    const int j = b + (lane - t * cnt);
+                    const V4 q = a.grel[j];
+                    const T hj = a.gh[j];
+                    T rv[D];
+                    rv[0] = bt[0] - q.x;
+                    if (D > 1) rv[D > 1 ? 1 : 0] = bt[D > 1 ? 1 : 0] - q.y;
+                    if (D > 2) rv[D > 2 ? 2 : 0] = bt[D > 2 ? 2 : 0] - q.z;
+                    T r2 = rv[0] * rv[0];
+#pragma unroll
+                    for (int k = 1; k < D; ++k) r2 += rv[k] * rv[k];
+                    T fsum, gsum;
+                    const T hmax = hit > hj ? hit : hj;
+                    if (r2 >= hmax * hmax && r2 > T(0)) {
+                        const T rinv = rsqrt_t(r2);
+                        fsum = T(2) * rinv;
+                        gsum = fsum * rinv * rinv;
+                    } else {
+                        const T r = sqrt(r2);
+                        fsum = hk_f(r, hit) + hk_f(r, hj);
+                        gsum = hk_g(r, hit) + hk_g(r, hj);
+                    }
+                    const T gm = G * q.w * T(0.5);
+                    pphi = -gm * fsum;
+                    const T c = gm * gsum;
+#pragma unroll
+                    for (int k = 0; k < D; ++k) pacc[k] = -rv[k] * c;
+                }
+                // segmented sums over [t cnt, (t + 1) cnt): the segment's first lane ends with them
+                const int seg_end = pv ? (t + 1) * cnt : lane + 1;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const bool in_seg = lane + o < seg_end;
+                    const T vphi = __shfl_down_sync(FULL, pphi, o);
+                    if (in_seg) pphi += vphi;
+#pragma unroll
+                    for (int k = 0; k < D; ++k) {
+                        const T v = __shfl_down_sync(FULL, pacc[k], o);
+                        if (in_seg) pacc[k] += v;
+                    }
+                }
+                const int from = open ? __popc(om & lanemask_lt()) * cnt : 0;
+                const T sphi = __shfl_sync(FULL, pphi, from);
+                T sacc[D];
+#pragma unroll
+                for (int k = 0; k < D; ++k) sacc[k] = __shfl_sync(FULL, pacc[k], from);
+                if (open) {
+                    phi.add(sphi);
+#pragma unroll
+                    for (int k = 0; k < D; ++k) acc[k].add(sacc[k]);
+                }
+            } else if (fc < 0) {
                 if (open) {
                     const int b = link.z, cnt = link.w;
                     if (COUNT) n_pair += (unsigned)cnt;
