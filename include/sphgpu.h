@@ -252,7 +252,8 @@ const char* sphgpu_last_error(const sphgpu_ctx* ctx);
  * first block leaves without arriving at the first barrier, so the other blocks' wait runs out
  * (one build only; the knob then reads 0);
  * 34 key table: 0 off, 1 from 2^18 particles on (default), 2 always (reads 0 when a batch has too
- * many runs for its 64 MB): the first eight levels of each run's octree-centre recursion replayed
+ * many runs for its 64 MB): the first levels (ten for a single run, fewer for large batches) of
+ * each run's octree-centre recursion replayed
  * once per tree build into a table that the key computation searches with integer comparisons
  * (the same keys, fewer FP64 additions);
  * 35 gravity work items: 1 fixed 32-particle chunks of each run's key order, one warp each

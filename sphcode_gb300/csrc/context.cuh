@@ -37,6 +37,7 @@ struct Ctx {
     int* radix_dtot = nullptr;      // 256 digit totals
     long long* key_table = nullptr; // centres of the first key levels per run and axis (tree.cu)
     int key_table_on = 1;           // knob 34: key table 0 off, 1 from 2^18 particles, 2 always
+    int key_table_levels = 0;       // levels the allocated table holds
     int radix_blocks = 0;
 
     // tree (breadth-first node arrays)

@@ -135,8 +135,10 @@ __global__ void roots_kernel(TreeView tv, double* center0, double* center1, doub
 // so a particle's path through the table equals its path through the recursion.  Entries
 // k < 2^T hold the ordered-integer image of the centre (compared against), entries 2^T <= k < 2^(T+1)
 // the centre itself (where the particle's recursion continues).
-constexpr int KEY_TABLE_LEVELS = 8;
-constexpr int KEY_TABLE_SIZE = 2 << KEY_TABLE_LEVELS;   // entries 1 .. 2^(T+1) - 1 used
+// T is chosen at creation: the most levels, up to KEY_TABLE_LEVELS, whose tables of all runs fit
+// KEY_TABLE_BYTES (a single run takes ten levels; a batch of 4096 1D runs eight).
+constexpr int KEY_TABLE_LEVELS = 10;
+constexpr size_t KEY_TABLE_BYTES = 64u << 20;
 
 __global__ void key_table_kernel(TreeView tv, int R, int D, int T, long long* table)
 {
@@ -1484,9 +1486,12 @@ int tree_alloc(Ctx& c)
     c.radix_blocks = ceil_div(n, RADIX_TILE);
     A((void**)&c.radix_hist, sizeof(int) * 256 * c.radix_blocks);
     A((void**)&c.radix_dtot, sizeof(int) * 256);
-    // key tables (R runs x dim axes x 2^(T+1) entries), skipped for batches too large for 64 MB
-    const size_t kt = (size_t)c.R * c.dim * KEY_TABLE_SIZE;
-    if (kt * sizeof(long long) <= (64u << 20)) A((void**)&c.key_table, sizeof(long long) * kt);
+    // key tables (R runs x dim axes x 2^(T+1) entries) of the most levels that fit (none below 4)
+    c.key_table_levels = 0;
+    for (int t = KEY_TABLE_LEVELS; t >= 4; --t)
+        if ((size_t)c.R * c.dim * ((size_t)2 << t) * sizeof(long long) <= KEY_TABLE_BYTES) { c.key_table_levels = t; break; }
+    if (c.key_table_levels > 0)
+        A((void**)&c.key_table, sizeof(long long) * (size_t)c.R * c.dim * ((size_t)2 << c.key_table_levels));
     A((void**)&c.nd_begin, sizeof(int) * nc);
     A((void**)&c.nd_count, sizeof(int) * nc);
     A((void**)&c.nd_first, sizeof(int) * nc);
@@ -1630,7 +1635,11 @@ static void make_tree_d(Ctx& c, bool reorder_all, bool full_depth)
     // 2^18 particles the table's launch costs more than the FP64 additions it saves (Gresho 65k:
     // +0.4 % per step with it; KHI 786k -1.4 %, the 10.6M-particle ensemble -1.6 %)
     const bool table = c.key_table && (c.key_table_on == 2 || (c.key_table_on == 1 && n >= (1 << 18)));
-    const int T = table ? std::min(KEY_TABLE_LEVELS, lv) : 0;
+    // the table's entries cost about as many FP64 additions as the particles' levels they replace:
+    // keep it below a quarter of the particles (a large batch of small runs takes fewer levels)
+    int T = table ? std::min(c.key_table_levels, lv) : 0;
+    while (T > 0 && (long long)R * D * (2LL << T) * 4 > n) --T;
+    if (T < 4) T = 0;
     if (T > 0) {
         const long long total = (long long)R * D * (2 << T);
         key_table_kernel<<<(int)std::min<long long>(ceil_div((int)std::min<long long>(total, 1LL << 30), 256), 4096), 256, 0, s>>>(
