@@ -707,14 +707,14 @@ __global__ void __launch_bounds__(COUNT_THREADS) level_count_kernel(NodeArrays n
 }
 
 
-// One launch per level: places the children of the level-l nodes (level l + 1: begin, count,
-// centre, edge, parent) from the child counts and boundaries that level_count_kernel found.
-// tmp_cur / cs_cur hold the child counts of the level-l nodes and their per-chunk totals; the
-// launch also clears cs_clear, the totals that the count of level l + 2 fills.  Node indices are
-// breadth-first and, within a level, in key order.
-// With COUNT, each block also counts the children it has just placed (count_nodes_block: split
-// decision, boundaries, child counts into nx.lvl_tmp and nx.chunk_sum), so that the fused build
-// needs one grid barrier per level.
+// Places the children of the level-l nodes (level l + 1: begin, count, centre, edge, parent) from
+// the child counts and boundaries that the count of level l found (one launch per level, or one
+// phase of the fused build).  tmp_cur / cs_cur hold the child counts of the level-l nodes and their
+// per-chunk totals (cs_off, when given, their exclusive scan); the call also clears cs_clear, the
+// totals that the count of level l + 2 fills.  Node indices are breadth-first and, within a level,
+// in key order.  With COUNT, each block also counts the children it has just placed
+// (count_nodes_block: split decision, boundaries, child counts into nx.lvl_tmp and nx.chunk_sum),
+// so that the fused build needs one grid barrier per level.
 struct NextCount {
     const unsigned long long* keys;
     int n, levels, lv, leaf_num;
