@@ -611,24 +611,38 @@ __device__ __forceinline__ void count_nodes_block(const NodeArrays& na, const un
         }
         const int pos = G >= 2 ? group_first_ge<D>(keys, b, b + cnt, shift, c, G, gl, gmask, gshift)
                                : first_ge<D>(keys, b, b + cnt, shift, c);
-        if (gl == 0) {
-            int* slot = na.bnd + (size_t)node * (NC - 1);
-            slot[c - 1] = pos;
-            __threadfence();
-            if (atomicAdd(na.arrive + node, 1) == NC - 2) {
-                __threadfence();
-                int prev = b, nc = 0;
+        if (gl == 0) na.bnd[(size_t)node * (NC - 1) + (c - 1)] = pos;
+    }
+    // every task of these nodes ran in this block: after the barrier each node's boundaries are
+    // visible to all its threads, and the child counts follow without fences or arrival counters
+    __syncthreads();
+    const int lane32 = threadIdx.x & 31;
+    for (int nb = lo_node; nb < hi_node; nb += blockDim.x) {
+        const int node = nb + (int)threadIdx.x;
+        int nc = 0;
+        if (node < hi_node) {
+            int b = __ldcg(na.begin + node), cnt = __ldcg(na.count + node);
+            if (b < 0 || cnt < 0 || b + cnt > n) { b = 0; cnt = 0; }
+            if (cnt > leaf_num && l <= lv) {
+                const int* slot = na.bnd + (size_t)node * (NC - 1);
+                int prev = b;
                 for (int k = 1; k < NC; ++k) {
-                    const int x = k == c ? pos : __ldcg(slot + (k - 1));
+                    const int x = slot[k - 1];
                     nc += x > prev;
                     prev = x;
                 }
                 nc += b + cnt > prev;
                 lvl_tmp[node - s] = nc;
-                atomicAdd(&chunk_sum[(node - s) / LEVEL_CHUNK], nc);
-                na.arrive[node] = 0;
             }
         }
+        // one add per chunk and warp: a warp's 32 consecutive nodes lie in at most two chunks
+        const int chunk = node < hi_node ? (node - s) / LEVEL_CHUNK : -1;
+        const int first = __shfl_sync(FULL, chunk, 0);
+        const int in_first = __reduce_add_sync(FULL, chunk == first ? nc : 0);
+        const int in_second = __reduce_add_sync(FULL, chunk != first ? nc : 0);
+        const unsigned second = __ballot_sync(FULL, chunk >= 0 && chunk != first);
+        if (lane32 == 0 && first >= 0 && in_first) atomicAdd(&chunk_sum[first], in_first);
+        if (second && lane32 == __ffs(second) - 1 && in_second) atomicAdd(&chunk_sum[chunk], in_second);
     }
 }
 
