@@ -41,6 +41,7 @@ struct FluidArgs {
     const V4* rec2;   // {alpha, balsara, u, Y}   Y: disph u/P
     const T* grad;    // gsph: 16 per particle, grad rho [0,D), grad P [3,3+D), grad v [6 + 3k + d]
     double gamma;
+    T gamma_t, gm1_t, alpha_ac_t;   // the same constants in T (formed on the host, no conversions per target)
     int use_ac;
     int ac_gravity;
     double alpha_ac;
@@ -93,16 +94,16 @@ __device__ __forceinline__ void fluid_target(const FluidArgs<T>& a, int i, int r
     const T hinv_i = r0i.w;
         const T rho_i = r1i.x, p_i = r1i.y, c_i = r1i.z, X_i = r1i.w;
         const T al_i = r2i.x, b_i = r2i.y, u_i = r2i.z;
-        const T m_i = (T)st.f[F_MASS][i];
-        const T gm1 = (T)(a.gamma - 1.0);
+        const T m_i = a.xrel[i].w;   // the mass in T, as the sources carry it
+        const T gm1 = a.gm1_t;
         // ssph: P_i/rho_i^2 gradh_i ; disph: (gamma-1)^2 u_i / P_i, (gamma-1)^2 u_i, 1/(m_i u_i)
         const T g2u_i = gm1 * gm1 * u_i;
         const T g2u_per_p_i = g2u_i / p_i;
         const T mu_inv_i = T(1) / (m_i * u_i);
         const T rho2_inv_i = T(1) / (rho_i * rho_i);
         const T dt = (T)a.dt_run[run];
-        const T gamma = (T)a.gamma;
-        const T alpha_ac = (T)a.alpha_ac;
+        const T gamma = a.gamma_t;
+        const T alpha_ac = a.alpha_ac_t;
         T gi[GradLayout<D>::stride];
         if (TYPE == 2 && a.gsph_2nd) {
 #pragma unroll
@@ -356,6 +357,19 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
             group_box<D>(gm, xi, active, hi, a.pb);
             if (!group_walk<D, T>(smem, L, gm, a.tv, run, true, a.pb)) { report_overflow(a.work, gb, gn, gm); continue; }
         }
+        // Relative guard band of the T-precision test r^2 < H^2 for H = max(h_i, h_j) >= h_min
+        // of the group: the component error E (comp_err) at separations ~H is below e_rel H, so
+        // |r2_T - r2| < delta H^2 there.  Group-uniform: formed by thread 0 (its FP64 arithmetic
+        // once per group, not per target) and read after the staging's barriers.
+        // (in the FP32 form formed in FP32 and widened by 0.1 %: a wider band only sends more
+        // pairs to the exact test)
+        if (threadIdx.x == 0) {
+            const T hm = (T)gm->rmin;
+            const T e_rel = (T)comp_err<T>(gm, gm->rmin) / hm * T(1.001) + (T)(Unit<T>::u * 3.0);
+            const T dl = T(2.002) * (T(2.0 * 1.7320508075688772) * e_rel + T(D) * e_rel * e_rel + (T)(8.0 * Unit<T>::u));
+            gm->bandf = (float)dl;
+            gm->bandd = (double)dl;
+        }
         {
             // keep sources within max(R, h_j) of the group box
             BoxAccept<D, T> box;
@@ -372,17 +386,7 @@ __global__ void __launch_bounds__(256) fluid_kernel(FluidArgs<T> a)
         const int ntile = gm->ntile;
         const int nw = (ntile + 31) >> 5;
 
-        // Relative guard band of the T-precision test r^2 < H^2 for H = max(h_i, h_j) >= h_min
-        // of the group: the component error E (comp_err) at separations ~H is below e_rel H, so
-        // |r2_T - r2| < delta H^2 there.
-        // (in the FP32 form formed in FP32 and widened by 0.1 %: a wider band only sends more
-        // pairs to the exact test, and an FP64 divide per target costs 1/64-rate cycles)
-        T delta;
-        {
-            const T hm = (T)gm->rmin;
-            const T e_rel = (T)comp_err<T>(gm, gm->rmin) / hm * T(1.001) + (T)(Unit<T>::u * 3.0);
-            delta = T(2.002) * (T(2.0 * 1.7320508075688772) * e_rel + T(D) * e_rel * e_rel + (T)(8.0 * Unit<T>::u));
-        }
+        const T delta = sizeof(T) == 4 ? (T)gm->bandf : (T)gm->bandd;
         const T dlo = T(1) - delta, dhi = T(1) + delta;
 
         T xo[D];
@@ -579,6 +583,9 @@ void run_fluid(Ctx& c)
     a.rec2 = rec2;
     a.grad = grad;
     a.gamma = c.p.gamma;
+    a.gamma_t = (T)c.p.gamma;
+    a.gm1_t = (T)(c.p.gamma - 1.0);
+    a.alpha_ac_t = (T)c.p.alpha_ac;
     a.use_ac = c.p.use_ac;
     a.ac_gravity = c.p.use_gravity;
     a.alpha_ac = c.p.alpha_ac;

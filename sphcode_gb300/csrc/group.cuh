@@ -85,6 +85,8 @@ struct GroupMisc {
     int ntile;
     int overflow;
     int gidx;           // index of the current work item in the group list (-1: a range of a later pass)
+    float bandf;        // a pair kernel's relative guard band of the group, formed once (FP32 / FP64 form)
+    double bandd;
     double wred[8][8];  // per-warp reduction scratch (at most 8 warps per CTA)
 };
 
