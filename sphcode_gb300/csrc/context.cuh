@@ -173,6 +173,8 @@ struct Ctx {
     int fused_levels = 1;
     // inside run_step: predict leaves the sound speed to the mirror kernels of Pre and Fluid
     bool sound_from_ene = false;
+    // the last PreInteraction wrote FluidForce's source records (cleared by FluidForce)
+    bool fluid_records_fresh = false;
     // gravity work items (knob 35): 0 the pair kernels' target groups in 32-target pieces, 1 fixed
     // 32-particle chunks of each run's key order (every lane of a warp holds a target; default,
     // Evrard 2^20 gravity about 10 % faster than over the groups' partly filled pieces)

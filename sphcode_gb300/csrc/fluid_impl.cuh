@@ -569,8 +569,11 @@ void run_fluid(Ctx& c)
     V4* rec1 = (V4*)c.mir[3];
     V4* rec2 = (V4*)c.mir[4];
     T* grad = (T*)c.mir[5];
-    fluid_mirror_kernel<D, T, TYPE><<<ceil_div(c.n, 256), 256, 0, s>>>(
-        c.st, c.n, rec0, rec1, rec2, grad, c.p.gsph_2nd_order, c.sound_from_ene ? c.p.gamma * (c.p.gamma - 1.0) : 0.0);
+    // the records of a whole step's PreInteraction are current (it wrote them per target)
+    if (!c.fluid_records_fresh)
+        fluid_mirror_kernel<D, T, TYPE><<<ceil_div(c.n, 256), 256, 0, s>>>(
+            c.st, c.n, rec0, rec1, rec2, grad, c.p.gsph_2nd_order, c.sound_from_ene ? c.p.gamma * (c.p.gamma - 1.0) : 0.0);
+    c.fluid_records_fresh = false;
     reset_work_counters(c);
     FluidArgs<T> a{};
     a.st = c.st;

@@ -45,6 +45,12 @@ struct PreArgs {
     unsigned long long* counters;   // PairCounter slots, or nullptr (not counted)
     int bulk_stage;                 // stage the tile with bulk asynchronous copies (knob 29)
     PlanView<T> pv;                 // group plans of the first pass (pv.plan nullptr: none)
+    // inside a whole step (ssph / disph): FluidForce's source records {v, 1/h}, {rho, P, c, X},
+    // {alpha, balsara, u, Y} written by each finished target, as fluid_mirror_kernel would form
+    // them from the fields this stage stores (nullptr: the mirror kernel runs before FluidForce)
+    V4* frec0;
+    V4* frec1;
+    V4* frec2;
 };
 
 template <int D>
@@ -498,6 +504,32 @@ __device__ __forceinline__ void pre_target(const PreArgs<T>& a, int i, int run, 
             st.f[F_BALSARA][i] = balsara_out;
             st.f[F_ALPHA][i] = alpha_out;
             st.neighbor[i] = nnb;
+            if (a.frec0) {
+                // the records fluid_mirror_kernel forms, from the same doubles
+                const double u = st.f[F_ENE][i], gh = (double)gradh;
+                V4 r0, r1, r2;
+                r0.x = vi[0];
+                r0.y = D > 1 ? vi[D > 1 ? 1 : 0] : T(0);
+                r0.z = D > 2 ? vi[D > 2 ? 2 : 0] : T(0);
+                r1.x = (T)dens;
+                r1.y = (T)pres;
+                r1.z = ciT;
+                r2.x = (T)alpha_out;
+                r2.y = (T)balsara_out;
+                r2.z = (T)u;
+                if constexpr (std::is_same<T, float>::value) {
+                    r0.w = __frcp_rn((float)hf);
+                    r1.w = TYPE == 0 ? __fdiv_rn(__fdiv_rn(r1.y, r1.x), r1.x) * (float)gh : (float)gh;
+                    r2.w = TYPE == 1 ? __fdiv_rn(r2.z, r1.y) : 0.0f;
+                } else {
+                    r0.w = (T)(1.0 / hf);
+                    r1.w = TYPE == 0 ? (T)(pres / (dens * dens) * gh) : (T)gh;
+                    r2.w = TYPE == 1 ? (T)(u / pres) : T(0);
+                }
+                a.frec0[i] = r0;
+                a.frec1[i] = r1;
+                a.frec2[i] = r2;
+            }
         }
 }
 
@@ -760,6 +792,13 @@ void run_pre(Ctx& c, bool initial)
     a.nn_over_a = (double)c.p.neighbor_number / volume_const<D>();
     a.counters = c.count_work ? c.d_counters : nullptr;
     a.bulk_stage = c.bulk_stage;
+    // inside a whole step the finished targets also write FluidForce's records (not gsph, whose
+    // records come with its gradients), and FluidForce then skips its mirror kernel
+    const bool frec = !initial && c.sound_from_ene && c.p.sph_type != 2;
+    a.frec0 = frec ? (V4*)c.mir[2] : nullptr;
+    a.frec1 = frec ? (V4*)c.mir[3] : nullptr;
+    a.frec2 = frec ? (V4*)c.mir[4] : nullptr;
+    c.fluid_records_fresh = frec;
     const int tcap = c.tile_cap_pre ? c.tile_cap_pre : default_tile_cap<D>();
     a.pv = PlanView<T>{};
     if ((c.prewalk & 2) && c.pair_sched != 3) {
