@@ -48,17 +48,17 @@ PRE_DENS_FLOPS_PER_PAIR = {("disph", 2): 91, ("disph", 3): 110, ("ssph", 2): 86,
 GRAV_FLOPS_LEAF, GRAV_FLOPS_NODE = 60, 20
 
 
-# Compulsory HBM bytes of the force stage per particle: FP64 reads of pos(D), vel(D), mass,
-# dens, pres, ene, sml, sound, alpha, balsara, gradh + FP32 mirror write/read (48 B) + writes of
-# acc(D), dene.
+# Compulsory HBM bytes of the force stage per particle inside a whole step: FP64 reads of pos(D)
+# and sml, the FP32 source records that PreInteraction wrote (48 B), writes of acc(D), dene.
 def fluid_bytes_per_particle(D):
-    return 8 * (2 * D + 9) + 48 * 2 + 8 * (D + 1)
+    return 8 * (D + 1) + 48 + 8 * (D + 1)
 
 
-# PreInteraction: reads pos(D), vel(D), mass, dens, ene, sound, alpha, balsara and the FP32 mirrors
-# (32 B written and read), writes sml, dens, pres, gradh, balsara, alpha (FP64) and the count.
+# PreInteraction: reads pos(D), vel(D), mass, dens, ene, alpha, balsara and the FP32 mirrors (32 B
+# written and read; the sound speed formed from u), writes sml, dens, pres, gradh, balsara, alpha
+# (FP64), the count and FluidForce's FP32 source records (48 B).
 def pre_bytes_per_particle(D):
-    return 8 * (2 * D + 6) + 32 * 2 + 8 * 6 + 4
+    return 8 * (2 * D + 5) + 32 * 2 + 8 * 6 + 4 + 48
 
 
 # GravityForce: reads pos(D), mass, sml and the FP32 leaf records (16 B), reads and writes acc(D),
